@@ -1,0 +1,366 @@
+"""Benchmark of the FDTD time-stepping hot path (one JSON line on rank 0).
+
+Workload (one "step" of this benchmark = one whole simulation): the
+512 x 384 x 256 room (50.3M nodes) with a 1-voxel solid shell and 40 seeded
+axis-aligned solid boxes (edges 8..64), 20 materials with admittance
+U(0.01, 0.9), a soft impulse source, 8 seeded air-node receivers, 2000 leapfrog
+steps of the SRL forward scheme in FP32.  Metric: node-updates/s, counting the
+X*Y*(Z-2) nodes each leapfrog step updates.
+
+  value  — device-resident: geometry and source table already in HBM, the
+           2000-step run timed with CUDA events on the domain's stream.
+  e2e    — through the C ABI with host buffers: node bytes and source table
+           copied host->device, run, receiver traces copied back, every step.
+  roofline — the update kernel alone, timed with CUDA events on the same
+           stream: 14 algorithmic bytes per node-update (1 class byte is read
+           in place of the reference's 2 node bytes, so actual traffic is 13 B).
+  cpu_baseline — the C++ oracle (a restatement of the reference's update rule)
+           on all host cores over a bounded sample of the same room.
+
+Multi-GPU: the path is replicas only; each rank runs its own copy of the
+workload on its own GPU (no collective in the data path), timing is the max
+over ranks after a barrier.
+
+--impl reference times the CPU restatement of the reference's own update rule
+(the reference itself cannot be built here: it needs Boost, OpenGL and an
+external voxelizer, and its gencodes predate nvcc 13).
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import math
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "node-updates/s"
+DIMS = (512, 384, 256)
+FDTD_STEPS = 2000
+N_REC = 8
+BYTES_PER_UPDATE = {"f32": 14, "f64": 26, "f16": 8, "bf16": 8}
+
+
+def parse():
+    p = argparse.ArgumentParser()
+    p.add_argument("--gpus", type=int, default=1)
+    p.add_argument("--steps", type=int, default=3)
+    p.add_argument("--warmup", type=int, default=3)
+    p.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    p.add_argument("--precision", default="f32", choices=["f32", "f64"])
+    p.add_argument("--fdtd-steps", type=int, default=FDTD_STEPS)
+    p.add_argument("--dims", type=str, default=None, help="X,Y,Z override (testing)")
+    p.add_argument("--no-cpu-baseline", action="store_true")
+    p.add_argument("--cpu-seconds", type=float, default=12.0)
+    return p.parse_args()
+
+
+def dist_env():
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return world, rank, local
+
+
+def make_room(dims):
+    from parallelfdtd_gb300 import rooms
+    room = rooms.boxes_room(dims, n_boxes=40, edge=(8, 64), n_materials=20,
+                            admittance_range=(0.01, 0.9), seed=2)
+    src = room.random_air_nodes(1, seed=8)[0]
+    rec = room.random_air_nodes(N_REC, seed=9)
+    return room, src, rec
+
+
+class ClockSampler:
+    """nvidia-smi clock/throttle sampling while the timed region runs."""
+
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device_index: int):
+        self.dev = device_index
+        self.samples = []
+        self._stop = threading.Event()
+        self._proc = None
+
+    def __enter__(self):
+        try:
+            self._proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.dev), f"--query-gpu={self.Q}",
+                 "--format=csv,noheader,nounits", "-lms", "200"],
+                stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self._t = threading.Thread(target=self._read, daemon=True)
+            self._t.start()
+        except Exception:
+            self._proc = None
+        return self
+
+    def _read(self):
+        for line in self._proc.stdout:
+            parts = [s.strip() for s in line.split(",")]
+            if len(parts) >= 9:
+                self.samples.append(parts)
+
+    def __exit__(self, *exc):
+        if self._proc is not None:
+            self._proc.terminate()
+            try:
+                self._proc.wait(timeout=5)
+            except Exception:
+                self._proc.kill()
+
+    def summary(self):
+        if not self.samples:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"]}
+        sm = [float(s[1]) for s in self.samples if s[1].replace(".", "").isdigit()]
+        mx = [float(s[2]) for s in self.samples if s[2].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[i] for s in self.samples for i in range(4)
+                          if s[5 + i].lower() == "active"})
+        loaded = [v for v in sm if mx and v > 0.5 * max(mx)] or sm
+        return {"sm_mhz": statistics.median(loaded) if loaded else None,
+                "sm_max_mhz": max(mx) if mx else None, "reasons": reasons,
+                "samples": len(self.samples)}
+
+
+def peak_hbm():
+    path = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    try:
+        with open(path) as f:
+            return float(json.load(f)["hbm_gbs"]), "measured"
+    except Exception:
+        return 6800.0, "fallback"
+
+
+def traffic_per_launch(prec):
+    """DRAM bytes per update-kernel launch from the committed ncu summary."""
+    path = os.path.join(ROOT, "profiles", "traffic.json")
+    try:
+        with open(path) as f:
+            t = json.load(f)
+        return t.get(f"update_{prec}_bytes_per_launch")
+    except Exception:
+        return None
+
+
+def cpu_baseline(room, src, rec, budget_s: float):
+    """Oracle on all host cores over a bounded number of steps of the room."""
+    import numpy as np
+    from oracle import oracle as O
+    from parallelfdtd_gb300 import rooms
+    from parallelfdtd_gb300.domain import default_params
+    pos, mat = O.encode_nodes(room.bid, room.mat, centred=False)
+    X, Y, Z = room.dims
+    threads = O.max_threads()
+    args = (pos, mat, room.dims, room.admittance, default_params(),
+            [room.flat(*src)], [1])
+    rec_idx = [room.flat(*r) for r in rec]
+    probe = 2
+    t0 = time.perf_counter()
+    O.run(*args, rooms.impulse(probe)[None], rec_idx, probe, threads=threads)
+    per = (time.perf_counter() - t0) / probe
+    n = max(2, min(200, int(budget_s / max(per, 1e-6))))
+    t0 = time.perf_counter()
+    O.run(*args, rooms.impulse(n)[None], rec_idx, n, threads=threads)
+    dt = time.perf_counter() - t0
+    return {"value": X * Y * (Z - 2) * n / dt, "unit": METRIC, "cores": threads,
+            "kind": "port",
+            "sample": f"{X}x{Y}x{Z} room, {n} of the {FDTD_STEPS} leapfrog steps, FP32 "
+                      f"SRL forward, {threads} OpenMP threads"}
+
+
+def run_reference_arm(a, world, rank):
+    """--impl reference: the CPU restatement of the reference's update rule."""
+    if rank != 0:
+        return 0
+    dims = tuple(int(v) for v in a.dims.split(",")) if a.dims else DIMS
+    room, src, rec = make_room(dims)
+    import numpy as np
+    from oracle import oracle as O
+    from parallelfdtd_gb300 import rooms
+    from parallelfdtd_gb300.domain import default_params
+    pos, mat = O.encode_nodes(room.bid, room.mat, centred=False)
+    X, Y, Z = dims
+    threads = O.max_threads()
+    sample_steps = 10
+    args = (pos, mat, dims, room.admittance, default_params(), [room.flat(*src)], [1],
+            rooms.impulse(sample_steps)[None], [room.flat(*r) for r in rec], sample_steps)
+    for _ in range(a.warmup):
+        O.run(*args, threads=threads, double=(a.precision == "f64"))
+    t0 = time.perf_counter()
+    for _ in range(a.steps):
+        O.run(*args, threads=threads, double=(a.precision == "f64"))
+    dt = (time.perf_counter() - t0) / a.steps
+    value = X * Y * (Z - 2) * sample_steps / dt
+    sample = (f"{X}x{Y}x{Z} room, {sample_steps} leapfrog steps per benchmark step, "
+              f"{a.precision.upper()} SRL forward, {threads} OpenMP threads")
+    line = {
+        "impl": "reference", "metric": METRIC, "value": value, "unit": METRIC,
+        "n_gpus": a.gpus, "steps": a.steps, "warmup": a.warmup, "ms_per_step": dt * 1e3,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": a.precision, "data": "synthetic",
+        "config": {"workload": f"boxes room {X}x{Y}x{Z}, 40 boxes, 20 materials, soft impulse, "
+                               f"{N_REC} receivers, SRL forward (CPU sample of {sample_steps} steps)",
+                   "parallelism": "host threads", "l2": "inputs larger than L2"},
+        "cpu_baseline": {"value": value, "unit": METRIC, "cores": threads, "kind": "port",
+                         "sample": sample},
+        "e2e": {"value": value, "unit": METRIC, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+def main():
+    a = parse()
+    world, rank, local = dist_env()
+    if a.impl == "reference":
+        return run_reference_arm(a, world, rank)
+
+    import numpy as np
+    import torch
+    import __graft_entry__ as g
+    g.build()
+    from parallelfdtd_gb300 import _lib as L
+    from parallelfdtd_gb300 import rooms
+    from parallelfdtd_gb300.domain import Domain, default_params
+
+    torch.cuda.set_device(local)
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl" if torch.cuda.is_available() else "gloo")
+    dims = tuple(int(v) for v in a.dims.split(",")) if a.dims else DIMS
+    S = a.fdtd_steps
+    room, src, rec = make_room(dims)
+    X, Y, Z = dims
+    updates_per_run = X * Y * (Z - 2) * S
+    prec = a.precision
+    samples = rooms.impulse(S)[None].astype(np.float64 if prec == "f64" else np.float32)
+    d = Domain(dims, prec, device=local)
+    d.set_voxels(room.bid, room.mat, centred=False)
+    pos_host, mat_host = d.get_nodes()
+    d.set_materials(room.admittance)
+    d.set_params(default_params())
+    d.set_scheme("forward")
+    d.set_sources([src], [1], samples)
+    d.set_receivers(rec)
+    esize = 8 if prec == "f64" else 4
+    stream = torch.cuda.ExternalStream(d.stream_ptr())
+    d_out = torch.zeros(N_REC * S, dtype=torch.float64 if prec == "f64" else torch.float32,
+                        device=f"cuda:{local}")
+
+    def barrier():
+        torch.cuda.synchronize()
+        if world > 1:
+            import torch.distributed as dist
+            dist.barrier()
+
+    def run_device():
+        L.call("pfdtd_run_device", d.handle, S, d_out.data_ptr())
+
+    # ---- device-resident timing ------------------------------------------
+    for _ in range(a.warmup):
+        run_device()
+    barrier()
+    l0 = L.load().pfdtd_kernel_launches()
+    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    with ClockSampler(local) as clk:
+        with torch.cuda.stream(stream):
+            ev0.record(stream)
+        for _ in range(a.steps):
+            run_device()
+        with torch.cuda.stream(stream):
+            ev1.record(stream)
+        barrier()
+    launches = L.load().pfdtd_kernel_launches() - l0
+    ms = ev0.elapsed_time(ev1) / a.steps
+    t_local = ms
+    if world > 1:
+        import torch.distributed as dist
+        t = torch.tensor([ms], device=f"cuda:{local}")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        ms = float(t.item())
+    value = updates_per_run * world / (ms * 1e-3)
+
+    # ---- dominant kernel alone (same stream, same arguments) ---------------
+    prof_iters = 50
+    k0, k1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    with torch.cuda.stream(stream):
+        k0.record(stream)
+    import ctypes as C
+    L.call("pfdtd_profile_update", d.handle, prof_iters)
+    with torch.cuda.stream(stream):
+        k1.record(stream)
+    torch.cuda.synchronize()
+    kms = k0.elapsed_time(k1) / prof_iters
+    nodes = X * Y * (Z - 2)
+    algo_bytes = BYTES_PER_UPDATE[prec] * nodes
+    achieved = algo_bytes / (kms * 1e-3) / 1e9
+    peak, peak_kind = peak_hbm()
+    traffic = traffic_per_launch(prec)
+
+    # ---- end to end through the C ABI with host buffers ------------------------
+    out_host = np.zeros((N_REC, S), dtype=np.float64 if prec == "f64" else np.float32)
+    sec = C.c_double()
+    for _ in range(max(1, a.warmup)):
+        d.set_nodes(pos_host, mat_host)
+        d.set_sources([src], [1], samples)
+        d.run(S, out=out_host)
+    barrier()
+    t0 = time.perf_counter()
+    for _ in range(a.steps):
+        d.set_nodes(pos_host, mat_host)
+        d.set_sources([src], [1], samples)
+        d.run(S, out=out_host)
+    barrier()
+    e2e_s = (time.perf_counter() - t0) / a.steps
+    if world > 1:
+        import torch.distributed as dist
+        t = torch.tensor([e2e_s], device=f"cuda:{local}", dtype=torch.float64)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        e2e_s = float(t.item())
+    e2e = {"value": updates_per_run * world / e2e_s, "unit": METRIC,
+           "h2d_bytes_per_step": int(2 * room.n_nodes + samples.nbytes),
+           "d2h_bytes_per_step": int(N_REC * S * esize)}
+
+    if rank == 0:
+        base = None
+        if not a.no_cpu_baseline and world == 1:
+            base = cpu_baseline(room, src, rec, a.cpu_seconds)
+        line = {
+            "metric": METRIC, "value": value, "unit": METRIC, "n_gpus": world,
+            "steps": a.steps, "warmup": a.warmup, "ms_per_step": ms,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+            "dtype": prec, "data": "synthetic",
+            "config": {"workload": f"boxes room {X}x{Y}x{Z}, 40 boxes (edges 8-64), 20 materials "
+                                   f"U(0.01,0.9), soft impulse, {N_REC} air receivers, {S} "
+                                   f"leapfrog steps, SRL forward, {prec}",
+                       "fdtd_steps_per_step": S, "nodes": X * Y * Z,
+                       "parallelism": f"replicas x{world}",
+                       "l2": "inputs larger than L2 (fields 2 x 201 MB + 50 MB classes)"},
+            "e2e": e2e,
+            "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                         "frac": achieved / peak, "traffic": traffic,
+                         "kernel": "k_update_zmarch", "kernel_ms": kms,
+                         "algorithmic_bytes_per_launch": algo_bytes,
+                         "peak_kind": f"of {peak_kind}"},
+            "clocks": clk.summary(),
+            "gpu_launches": int(launches),
+            "cpu_baseline": base,
+        }
+        print(json.dumps(line), flush=True)
+    d.close()
+    if world > 1:
+        import torch.distributed as dist
+        dist.destroy_process_group()
+    return 0
+
+
+if __name__ == "__main__":
+    sys.exit(main())

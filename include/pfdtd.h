@@ -1,0 +1,218 @@
+/*
+ * pfdtd.h — C ABI of the GB300 FDTD time-stepping library (libpfdtd.so).
+ *
+ * One opaque domain handle holds one whole simulation grid on one GPU: the
+ * node bytes, two pressure fields (current and past), the material table,
+ * the simulation parameters, the sources and the receivers.  Every function
+ * returns an int status (PFDTD_OK = 0) and never throws; the message of the
+ * last failure on the calling thread is available from pfdtd_last_error().
+ * Pointers are plain host pointers unless a function says otherwise.
+ *
+ * Grid layout is the reference's: flat arrays, x fastest,
+ * index = z*X*Y + y*X + x (ParallelFDTD src/kernels/cudaMesh.h:247-249).
+ * Node bytes are the scheme-encoded "position" bytes and material bytes the
+ * reference keeps on the device (src/kernels/cudaMesh.h:90-91):
+ *   forward scheme (SRL_FORWARD): bit7 = inside switch, bits0-6 = K, the
+ *     number of air neighbours (src/kernels/cudaMesh.cu:328-361);
+ *   centred scheme (SRL): bit7 = inside, DIR_X/Y/Z = 0x01/0x02/0x04,
+ *     SIGN_X/Y/Z = 0x10/0x20/0x40 (src/kernels/cudaMesh.h:35-44).
+ *
+ * The entry points below replace, for a non-C++ caller, the path
+ * CudaMesh::setupMesh -> CudaMesh::makePartition -> launchFDTD3d /
+ * launchFDTD3dDouble / launchFDTD3dStep (src/kernels/cudaMesh.h:648-838,
+ * src/kernels/kernels3d.h:49-90).  The C++ classes with the reference's own
+ * names and signatures sit on top of these (include/pfdtd/).
+ */
+#ifndef PFDTD_H
+#define PFDTD_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* Status codes. */
+#define PFDTD_OK 0
+#define PFDTD_INTERRUPTED 1        /* run stopped by the interrupt callback */
+#define PFDTD_ERR_ARG (-1)         /* invalid argument or size */
+#define PFDTD_ERR_CUDA (-2)        /* a CUDA runtime call failed */
+#define PFDTD_ERR_MATERIAL (-3)    /* a node's material index lies outside the table */
+#define PFDTD_ERR_NOMEM (-4)       /* device allocation failed */
+#define PFDTD_ERR_STATE (-5)       /* call out of order (e.g. run before geometry) */
+#define PFDTD_ERR_UNSUPPORTED (-6) /* combination not built (e.g. scheme x precision) */
+
+/* Field storage precision. */
+#define PFDTD_F32 0
+#define PFDTD_F64 1
+#define PFDTD_F16 2  /* fp16 storage, fp32 arithmetic */
+#define PFDTD_BF16 3 /* bf16 storage, fp32 arithmetic */
+
+/* Update schemes, numbered as the reference's UpdateType
+ * (src/base/SimulationParameters.h:39).  SHARED runs the forward rule: the
+ * reference's shared-memory variant reads and rewrites its shared tile
+ * without a barrier in between (src/kernels/kernels3d.cu:572-603). */
+#define PFDTD_SRL_FORWARD 0
+#define PFDTD_SHARED 1
+#define PFDTD_SRL 2
+
+/* Source types (src/base/SrcRec.h:33). */
+#define PFDTD_SRC_HARD 0
+#define PFDTD_SRC_SOFT 1
+#define PFDTD_SRC_TRANSPARENT 2
+
+/* Reference-behaviour switches (bit flags for pfdtd_set_quirks). */
+#define PFDTD_QUIRK_MATIDX 1 /* forward kernel material index m*20*octave (kernels3d.cu:513) */
+#define PFDTD_QUIRK_SOFTSRC 2 /* soft source overwrites instead of adding (cudaMesh.h:366) */
+
+/* Field selectors. */
+#define PFDTD_FIELD_CURRENT 0
+#define PFDTD_FIELD_PAST 1
+
+typedef struct pfdtd_domain pfdtd_domain;
+
+/* Callbacks with the reference's signatures (src/App.h:33-34). */
+typedef int (*pfdtd_interrupt_fn)(void);
+typedef void (*pfdtd_progress_fn)(int step, int max_step, float seconds_per_step);
+
+/* Message of the last failing call on this thread ("" if none). */
+const char* pfdtd_last_error(void);
+
+/* Library version string. */
+const char* pfdtd_version(void);
+
+/* Number of visible CUDA devices (0 if none), as App::queryDevices
+ * (src/App.cpp:91-112). */
+int pfdtd_device_count(int* count);
+
+/* Create a domain of dim_x * dim_y * dim_z nodes on `device` and allocate
+ * its fields (zeroed) and node bytes (zeroed = all solid).  Replaces
+ * CudaMesh::makePartition (src/kernels/cudaMesh.h:648-751) with one whole
+ * domain.  dim_z >= 3. */
+int pfdtd_create(int64_t dim_x, int64_t dim_y, int64_t dim_z, int precision, int device,
+                 pfdtd_domain** out);
+int pfdtd_destroy(pfdtd_domain* d);
+int pfdtd_get_dims(const pfdtd_domain* d, int64_t dims[3]);
+int pfdtd_get_precision(const pfdtd_domain* d, int* precision);
+
+/* Reference-behaviour switches, PFDTD_QUIRK_* bits; default 0. */
+int pfdtd_set_quirks(pfdtd_domain* d, int quirks);
+
+/* Copy scheme-encoded node bytes (pos) and material bytes (mat), N each.
+ * on_device != 0: the pointers are device pointers on the domain's device. */
+int pfdtd_set_nodes(pfdtd_domain* d, const uint8_t* pos, const uint8_t* mat, int on_device);
+
+/* Device pointers of the domain's node bytes (N each, owned by the domain). */
+int pfdtd_get_node_ptrs(pfdtd_domain* d, uint8_t** d_pos, uint8_t** d_mat);
+/* Copy the node bytes to the host (N each; either pointer may be null). */
+int pfdtd_get_nodes(pfdtd_domain* d, uint8_t* pos, uint8_t* mat);
+/* Declare that node bytes were written through those pointers. */
+int pfdtd_nodes_changed(pfdtd_domain* d);
+
+/* Material table [n_mat * n_coef] (admittances), row per unique material,
+ * as MaterialHandler::getMaterialCoefficientPtr(Double)
+ * (src/base/MaterialHandler.cpp:100-164).  Values are double on the ABI and
+ * rounded to the domain's arithmetic type (float for every precision but
+ * PFDTD_F64) exactly as the reference would hold them. */
+int pfdtd_set_materials(pfdtd_domain* d, const double* table, int n_mat, int n_coef);
+
+/* Parameter vector [lambda, lambda^2, 1/3, octave] as
+ * SimulationParameters::getParameterPtr(Double) (SimulationParameters.cpp:379-396). */
+int pfdtd_set_params(pfdtd_domain* d, const double params[4]);
+
+/* Sources: n positions (x,y,z triples, element coordinates), type per source
+ * (PFDTD_SRC_*), and a sample table [n * n_samples] (row per source) in the
+ * domain's arithmetic type (float, or double for PFDTD_F64).  Sources whose z
+ * lies outside the grid are skipped, as CudaMesh::setSample does
+ * (cudaMesh.h:322-338). */
+int pfdtd_set_sources(pfdtd_domain* d, int n, const int64_t* xyz, const int32_t* type,
+                      const void* samples, int64_t n_samples);
+
+/* Receivers: n positions (x,y,z triples).  A receiver whose z lies outside
+ * the grid is skipped and its output row left untouched
+ * (kernels3d.cu:66-78, :164-173). */
+int pfdtd_set_receivers(pfdtd_domain* d, int n, const int64_t* xyz);
+
+/* Update scheme used by the next run/step (PFDTD_SRL_FORWARD, _SHARED, _SRL). */
+int pfdtd_set_scheme(pfdtd_domain* d, int scheme);
+
+/* Run `steps` leapfrog steps from step index 0 (launchFDTD3d,
+ * src/kernels/kernels3d.cu:31-203): per step inject sources into the current
+ * field, update z = 1..Z-2 into the past field, swap, record receivers.
+ * out: host buffer [n_rec * steps] in the arithmetic type, row per receiver.
+ * The interrupt callback is polled and the progress callback called every
+ * 100 steps.  seconds_per_step (optional) receives wall time / steps.
+ * Returns PFDTD_INTERRUPTED if stopped early (rows hold the steps done). */
+int pfdtd_run(pfdtd_domain* d, int64_t steps, void* out, pfdtd_interrupt_fn interrupt_cb,
+              pfdtd_progress_fn progress_cb, double* seconds_per_step);
+
+/* Same as pfdtd_run but with the output left on the device: d_out is a device
+ * buffer [n_rec * steps] in the arithmetic type.  No host synchronisation
+ * inside; the work is queued on the domain's stream (pfdtd_get_stream). */
+int pfdtd_run_device(pfdtd_domain* d, int64_t steps, void* d_out);
+
+/* Queue `iters` update-kernel launches alone (no sources, no receivers),
+ * swapping the fields after each, on the domain's stream; no synchronisation.
+ * Used to time the update kernel with events recorded around it. */
+int pfdtd_profile_update(pfdtd_domain* d, int iters);
+
+/* One step in capture mode (launchFDTD3dStep, kernels3d.cu:376-482): inject
+ * samples[step], update, swap unless the step direction changed, then write
+ * receiver values to out[r*num_steps + step] (host) when out is non-null. */
+int pfdtd_step(pfdtd_domain* d, int64_t step, int step_direction, void* out, int64_t num_steps);
+
+/* Single-node access (CudaMesh::setSample/addSample/getSample,
+ * cudaMesh.h:320-404, :497-565), element coordinates, current field. */
+int pfdtd_set_sample(pfdtd_domain* d, int64_t x, int64_t y, int64_t z, double value);
+int pfdtd_add_sample(pfdtd_domain* d, int64_t x, int64_t y, int64_t z, double value);
+int pfdtd_get_sample(pfdtd_domain* d, int64_t x, int64_t y, int64_t z, double* value);
+
+/* Swap current and past fields (CudaMesh::flipPressurePointers, cudaMesh.h:766-779). */
+int pfdtd_flip(pfdtd_domain* d);
+/* Zero both fields (CudaMesh::resetPressures, cudaMesh.h:782-791). */
+int pfdtd_reset_fields(pfdtd_domain* d);
+/* Device pointer of a field (PFDTD_FIELD_*); element 0 is node (0,0,0). */
+int pfdtd_get_field_ptr(pfdtd_domain* d, int which, void** d_ptr);
+/* Copy a whole field to / from the host (N elements of the storage type). */
+int pfdtd_download_field(pfdtd_domain* d, int which, void* host);
+int pfdtd_upload_field(pfdtd_domain* d, int which, const void* host);
+
+/* Slice capture (captureSliceFast / captureSliceKernel,
+ * src/kernels/visualizationUtils.cu:130-254, :500-527): orientation 0 = xy
+ * (slice = z), 1 = xz (slice = y), 2 = yz (slice = x).  p_out receives the
+ * current pressure as float and pos_out the node bytes (either may be null);
+ * sizes X*Y, X*Z and Y*Z respectively.  A slice past the grid returns
+ * PFDTD_ERR_ARG and writes nothing, as the reference skips the capture. */
+int pfdtd_capture_slice(pfdtd_domain* d, int orientation, int64_t slice, float* p_out,
+                        uint8_t* pos_out);
+
+/* CUDA stream (cudaStream_t) the domain queues its work on. */
+int pfdtd_get_stream(pfdtd_domain* d, void** stream);
+
+/* Launches of library kernels since load (for accounting in benchmarks). */
+int64_t pfdtd_kernel_launches(void);
+
+/* ---- Device-side mesh set-up (the reference runs these on the GPU) ---- */
+
+/* Translate voxelizer boundary ids (0..27) in place into scheme bytes:
+ * forward (toBilbao, cudaMesh.cu:328-361) when centred == 0, else centred
+ * (toKowalczyk, :363-480).  d_pos, d_mat: device pointers, n nodes. */
+int pfdtd_encode_nodes(int centred, uint8_t* d_pos, uint8_t* d_mat, int64_t n, int device);
+
+/* Count air and boundary nodes (calcBoundaries, cudaMesh.cu:500-514). */
+int pfdtd_count_boundaries(const uint8_t* d_pos, int64_t n, uint8_t air_value,
+                           uint8_t outside_value, int device, uint32_t* air,
+                           uint32_t* boundary);
+
+/* Pad a byte mesh to multiples of the block size (padWithZeros,
+ * cudaMesh.cu:253-304).  d_in holds in_len readable bytes; d_out must hold
+ * the padded size, returned in out_dims. Pass d_out = NULL to query dims. */
+int pfdtd_pad_mesh(const uint8_t* d_in, int64_t in_len, const uint32_t dims[3], uint32_t bx,
+                   uint32_t by, uint32_t bz, uint8_t* d_out, uint32_t out_dims[3], int device);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* PFDTD_H */

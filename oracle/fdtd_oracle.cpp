@@ -1,0 +1,415 @@
+// ---------------------------------------------------------------------------
+// CPU ORACLE — test infrastructure only.
+//
+// This file restates, in plain C++, the arithmetic of ParallelFDTD's
+// time-stepping hot path so that the CUDA implementation can be checked
+// against it.  Only the tests, the smoke check and the CPU-baseline leg of
+// the benchmark load it; nothing in the product links or calls it.
+//
+// Parity pin: the reference cannot be built here (Boost, GL and the external
+// voxelizer are missing, its gencodes predate nvcc 13), so this restatement is
+// pinned against the known-answer values the reference's own unit tests hold
+// (tests/SimulationParametersTest.cpp, tests/MaterialHandlerTest.cpp,
+// tests/CudaMeshTest.cpp) and against its partition-invariance property.
+// Field values themselves have no golden vectors in the reference.
+//
+// Every function cites the reference file:line it follows.  Build with
+// -ffp-contract=off so that every product is rounded before it is summed,
+// exactly as written in the reference source.
+// ---------------------------------------------------------------------------
+#include <cmath>
+#include <cstdint>
+#include <cstring>
+#include <cstdlib>
+#include <vector>
+#ifdef _OPENMP
+#include <omp.h>
+#endif
+
+namespace {
+
+// cudaMesh.h:35-44 — node byte bit masks.
+constexpr unsigned kInsideSwitch = 7;
+constexpr unsigned kForwardMask = 0x7F;
+constexpr unsigned kCenteredMask = 0x80;
+constexpr unsigned kDirX = 0x01, kDirY = 0x02, kDirZ = 0x04;
+constexpr unsigned kSignX = 0x10, kSignY = 0x20, kSignZ = 0x40;
+
+// cudaMesh.cu:328-361 (toBilbao): voxelizer boundary id 0..27 -> forward K.
+void to_bilbao(uint8_t* pos, uint8_t* mat) {
+  unsigned k = *pos;
+  if (k == 0) { *pos = 0; *mat = 0; return; }
+  if (k <= 8) { *pos = 3 | 0x80; return; }
+  if (k <= 20) { *pos = 4 | 0x80; return; }
+  if (k <= 26) { *pos = 5 | 0x80; return; }
+  if (k == 27) { *pos = 6 | 0x80; return; }
+  // k > 27: left unchanged, as in the reference.
+}
+
+// cudaMesh.cu:363-480 (toKowalczyk): boundary id -> centred DIR/SIGN bits.
+// The table lists, per id, the bits the reference assigns.
+const uint8_t kKowalczykTable[28] = {
+    0,
+    kSignZ | kDirX | kDirY | kDirZ | kCenteredMask,                  // 1
+    kSignZ | kSignX | kDirX | kDirY | kDirZ | kCenteredMask,         // 2
+    kSignZ | kSignY | kDirX | kDirY | kDirZ | kCenteredMask,         // 3
+    kSignZ | kSignY | kSignX | kDirX | kDirY | kDirZ | kCenteredMask, // 4
+    kDirX | kDirY | kDirZ | kCenteredMask,                           // 5
+    kSignX | kDirX | kDirY | kDirZ | kCenteredMask,                  // 6
+    kSignY | kDirX | kDirY | kDirZ | kCenteredMask,                  // 7
+    kSignY | kSignX | kDirX | kDirY | kDirZ | kCenteredMask,         // 8
+    kDirY | kDirZ | kSignZ | kCenteredMask,                          // 9
+    kDirY | kDirZ | kSignZ | kSignY | kCenteredMask,                 // 10
+    kDirX | kDirZ | kSignZ | kCenteredMask,                          // 11
+    kDirX | kDirZ | kSignZ | kSignX | kCenteredMask,                 // 12
+    kDirY | kDirZ | kCenteredMask,                                   // 13
+    kDirY | kDirZ | kSignY | kCenteredMask,                          // 14
+    kDirX | kDirZ | kCenteredMask,                                   // 15
+    kDirX | kDirZ | kSignX | kCenteredMask,                          // 16
+    kDirY | kDirX | kCenteredMask,                                   // 17
+    kDirX | kDirY | kSignX | kCenteredMask,                          // 18
+    kDirX | kDirY | kSignY | kCenteredMask,                          // 19
+    kDirY | kDirX | kSignY | kSignX | kCenteredMask,                 // 20
+    kDirZ | kSignZ | kCenteredMask,                                  // 21
+    kDirY | kSignY | kCenteredMask,                                  // 22
+    kDirY | kCenteredMask,                                           // 23
+    kDirX | kSignX | kCenteredMask,                                  // 24
+    kDirX | kCenteredMask,                                           // 25
+    kDirZ | kCenteredMask,                                           // 26
+    kCenteredMask,                                                   // 27
+};
+
+void to_kowalczyk(uint8_t* pos, uint8_t* mat) {
+  unsigned k = *pos;
+  if (k == 0) { *pos = 0; *mat = 0; return; }
+  if (k <= 27) { *pos = kKowalczykTable[k]; return; }
+}
+
+// Material-table index of a node.  Forward kernel (kernels3d.cu:513) parses
+// `m*20*+octave` as m*20*octave (ref_quirk bit 0); the intended rule, and the
+// centred kernel's (kernels3d.cu:639), is m*20+octave.
+template <typename T>
+bool material_index(unsigned m, T octave, bool quirk_mat, unsigned n_entries,
+                    unsigned* out) {
+  unsigned idx;
+  if (quirk_mat)
+    idx = (unsigned)((T)(m * 20u) * octave);
+  else
+    idx = (unsigned)((T)(m * 20u) + octave);
+  if (idx >= n_entries) return false;
+  *out = idx;
+  return true;
+}
+
+struct RunDesc {
+  int scheme;   // 0 forward (Bilbao), 1 centred (Kowalczyk)
+  int quirks;   // bit0: forward material index m*20*octave; bit1: soft source overwrites
+  int64_t X, Y, Z;
+  const uint8_t* pos;
+  const uint8_t* mat;
+  const void* table;  // [n_mat*20] of T
+  int n_mat;
+  const void* params; // [4] of T: lambda, lambda^2, 1/3, octave
+  int n_src;
+  const int64_t* src_idx;  // flat index, -1 = not in the domain
+  const int32_t* src_type; // 0 hard, 1 soft, 2 transparent (added like soft)
+  const void* src_samples; // [n_src * steps] of T
+  int n_rec;
+  const int64_t* rec_idx;
+  int64_t steps;
+  int threads;
+};
+
+// One leapfrog update over z in [1, Z-2] writing into Pp.
+// Forward rule: kernels3d.cu:485-529.  Centred rule: kernels3d.cu:608-665.
+template <typename T>
+int update(const RunDesc& d, const T* P, T* Pp, const std::vector<T>& beta_tab,
+           const std::vector<uint8_t>& valid) {
+  const T* prm = (const T*)d.params;
+  const T l = prm[0], l2 = prm[1];
+  const int64_t X = d.X, XY = d.X * d.Y, Z = d.Z;
+  (void)l;
+#pragma omp parallel for schedule(static) num_threads(d.threads)
+  for (int64_t z = 1; z < Z - 1; ++z) {
+    for (int64_t c = z * XY; c < (z + 1) * XY; ++c) {
+      const unsigned pos = d.pos[c];
+      const unsigned key = (pos << 8) | d.mat[c];
+      const T beta = beta_tab[key];
+      const T p = P[c];
+      const T pp = Pp[c];
+      T ret;
+      if (d.scheme == 0) {
+        const T position = (T)(pos & kForwardMask);
+        const T sw = (T)(pos >> kInsideSwitch);
+        const T S = P[c + XY] + P[c - XY] + P[c + X] + P[c - X] + P[c + 1] + P[c - 1];
+        ret = sw * ((T)1 / ((T)1 + beta)) *
+              (((T)2 - position * l2) * p + l2 * S - ((T)1 - beta) * pp);
+      } else {
+        const T sw = (T)(pos >> kInsideSwitch);
+        const T dx = (T)(pos & kDirX), dy = (T)((pos & kDirY) >> 1),
+                dz = (T)((pos & kDirZ) >> 2);
+        T pz[2], py[2], px[2];
+        pz[1] = P[c - XY];
+        pz[0] = P[c + XY];
+        py[0] = P[c - X];
+        py[1] = P[c + X];
+        px[0] = P[c - 1];
+        px[1] = P[c + 1];
+        const int sx = (pos & kSignX) >> 4, sy = (pos & kSignY) >> 5,
+                  sz = (pos & kSignZ) >> 6;
+        const T Sb = px[sx] * dx + py[sy] * dy + pz[sz] * dz;
+        const T S = (px[0] + px[1] + py[0] + py[1] + pz[0] + pz[1] + Sb) * l2;
+        ret = (S - ((T)2 - (T)6 * l2) * p + (beta - (T)1) * pp) * sw *
+              ((T)1 / ((T)1 + beta));
+      }
+      Pp[c] = ret;
+    }
+  }
+  return 0;
+}
+
+// Per-(pos, mat) beta, computed with the reference's expressions
+// (forward kernels3d.cu:514, centred kernels3d.cu:640).
+template <typename T>
+int beta_table(const RunDesc& d, std::vector<T>& beta, std::vector<uint8_t>& valid) {
+  const T* prm = (const T*)d.params;
+  const T* tab = (const T*)d.table;
+  const unsigned n_entries = (unsigned)d.n_mat * 20u;
+  beta.assign(65536, (T)0);
+  valid.assign(65536, 0);
+  // Presence scan: only keys present in the grid must have a valid index.
+  std::vector<uint8_t> present(65536, 0);
+  const int64_t N = d.X * d.Y * d.Z;
+  for (int64_t i = d.X * d.Y; i < N - d.X * d.Y; ++i)
+    present[((unsigned)d.pos[i] << 8) | d.mat[i]] = 1;
+  for (unsigned key = 0; key < 65536; ++key) {
+    if (!present[key]) continue;
+    const unsigned pos = key >> 8, m = key & 0xFF;
+    unsigned mi;
+    const bool quirk = (d.scheme == 0) && (d.quirks & 1);
+    if (!material_index<T>(m, prm[3], quirk, n_entries, &mi)) return -3;
+    const T Y = tab[mi];
+    if (d.scheme == 0) {
+      const T position = (T)(pos & kForwardMask);
+      beta[key] = (T)0.5 * (Y * ((T)6 - position) * prm[0]);
+    } else {
+      const T dx = (T)(pos & kDirX), dy = (T)((pos & kDirY) >> 1),
+              dz = (T)((pos & kDirZ) >> 2);
+      beta[key] = Y * prm[0] * (dx + dy + dz);
+    }
+    valid[key] = 1;
+  }
+  return 0;
+}
+
+// Step loop of launchFDTD3d / launchFDTD3dDouble (kernels3d.cu:83-181):
+// inject sources into P (:93-104), update (:109-153), swap (:160),
+// record receivers from the new P (:164-173).
+template <typename T>
+int run(const RunDesc& d, T* P, T* Pp, T* out) {
+  if (d.X < 1 || d.Y < 1 || d.Z < 3) return -1;
+  std::vector<T> beta;
+  std::vector<uint8_t> valid;
+  int rc = beta_table<T>(d, beta, valid);
+  if (rc) return rc;
+  const T* samples = (const T*)d.src_samples;
+  const int64_t N = d.X * d.Y * d.Z;
+  for (int64_t step = 0; step < d.steps; ++step) {
+    for (int i = 0; i < d.n_src; ++i) {
+      const int64_t idx = d.src_idx[i];
+      if (idx < 0 || idx >= N) continue;
+      const T v = samples[(int64_t)i * d.steps + step];
+      if (d.src_type[i] == 0 || (d.quirks & 2))
+        P[idx] = v;      // setSample, cudaMesh.h:322-338 (and Q4 addSample)
+      else
+        P[idx] = P[idx] + v;  // intended addSample, cudaMesh.h:349-369
+    }
+    update<T>(d, P, Pp, beta, valid);
+    T* t = P; P = Pp; Pp = t;
+    for (int r = 0; r < d.n_rec; ++r) {
+      const int64_t idx = d.rec_idx[r];
+      if (idx < 0 || idx >= N) continue;
+      out[(int64_t)r * d.steps + step] = P[idx];
+    }
+  }
+  // Leave the caller's first buffer holding the current field: after an odd
+  // number of swaps the roles of the two buffers are exchanged.
+  if ((d.steps & 1) != 0) {
+    std::vector<T> cur_copy(P, P + N);      // P is the caller's second buffer
+    std::memcpy(P, Pp, sizeof(T) * N);
+    std::memcpy(Pp, cur_copy.data(), sizeof(T) * N);
+  }
+  return 0;
+}
+
+// SimulationParameters.cpp:262-298 (getRegularSourceSample) in float.
+float regular_sample_f(int input_type, uint32_t step, uint32_t fs, const float* data,
+                       uint32_t data_len) {
+  float sample = 0.f;
+  switch (input_type) {
+    case 0:  // IMPULSE
+      sample += (step == 1) ? 1.f : 0.f;
+      break;
+    case 1: {  // GAUSSIAN, t0 = 40, width = 4
+      float t0 = 40, width = 4;
+      float e = ((float)(step - t0) / width);
+      sample += expf(-0.5f * (e * e));
+      break;
+    }
+    case 3:  // DATA
+      sample += (step < data_len) ? data[step] : 0.f;
+      break;
+    case 2: {  // SINE, 120 Hz
+      float freq = 120;
+      float t = (float)step / (float)fs;
+      sample += sinf(2.f * (float)3.14159265358979323846 * freq * t);
+      break;
+    }
+  }
+  return sample;
+}
+
+// SimulationParameters.cpp:312-348 (getRegularSourceSampleDouble).
+double regular_sample_d(int input_type, uint32_t step, uint32_t fs, const double* data,
+                        uint32_t data_len) {
+  double sample = 0.0;
+  switch (input_type) {
+    case 0:
+      sample += (step == 1) ? 1.0 : 0.0;
+      break;
+    case 1: {
+      double t0 = 40, width = 4;
+      double e = ((float)(step - t0) / width);
+      sample += exp(-0.5f * (e * e));
+      break;
+    }
+    case 3:
+      sample += (step < data_len) ? data[step] : 0.0;
+      break;
+    case 2: {
+      double freq = 120;
+      double t = (double)step / (double)fs;
+      sample += sin(2.f * (double)3.14159265358979323846 * freq * t);
+      break;
+    }
+  }
+  return sample;
+}
+
+}  // namespace
+
+extern "C" {
+
+// cudaMesh.cu:155-251 scheme translation, element_type dispatch as in
+// cudaMesh.cu:70-73 is done by the caller.
+void oracle_encode_nodes(int centred, uint8_t* pos, uint8_t* mat, int64_t n) {
+  for (int64_t i = 0; i < n; ++i) {
+    if (centred) to_kowalczyk(pos + i, mat + i);
+    else to_bilbao(pos + i, mat + i);
+  }
+}
+
+// cudaMesh.cu:500-514 (calcBoundaries).
+void oracle_count_boundaries(const uint8_t* pos, int64_t n, uint8_t air_value,
+                             uint8_t outside_value, uint32_t* air, uint32_t* boundary) {
+  uint32_t a = 0, b = 0;
+  for (int64_t i = 0; i < n; ++i) {
+    if (pos[i] == air_value) ++a;
+    if (pos[i] != outside_value && pos[i] != air_value) ++b;
+  }
+  *air = a;
+  *boundary = b;
+}
+
+// cudaMesh.cu:253-304 (padWithZeros for one byte mesh).  `in_len` is the
+// number of readable input bytes; reads past it (which the reference performs
+// when a dimension is padded) yield 0.
+void oracle_pad(const uint8_t* in, int64_t in_len, const uint32_t dims[3],
+                uint32_t bx, uint32_t by, uint32_t bz, uint8_t* out,
+                uint32_t out_dims[3]) {
+  uint32_t dx = dims[0], dy = dims[1], dz = dims[2];
+  uint32_t padX = 0, padY = 0, padZ = 0;
+  if (dx % bx) padX = bx - dx % bx;
+  if (dy % by) padY = by - dy % by;
+  if (dz % bz) padZ = bz - dz % bz;
+  const uint64_t nx = dx + padX, ny = dy + padY, nz = dz + padZ;
+  if (out) {
+    std::memset(out, 0, nx * ny * nz);
+    for (uint64_t z = 0; z < dz; ++z)
+      for (uint64_t y = 0; y < ny; ++y)
+        for (uint64_t x = 0; x < nx; ++x) {
+          if (x < (uint64_t)dx + 1 && x > 0 && y < (uint64_t)dy + 1 && y > 0 && z > 0) {
+            uint64_t old_idx = z * dx * dy + y * dx + x;
+            uint64_t new_idx = z * (dx + padX) * (dy + padY) + y * (dx + padX) + x;
+            out[new_idx] = (old_idx < (uint64_t)in_len) ? in[old_idx] : 0;
+          }
+        }
+  }
+  out_dims[0] = (uint32_t)nx;
+  out_dims[1] = (uint32_t)ny;
+  out_dims[2] = (uint32_t)nz;
+}
+
+// SimulationParameters.cpp:139-148 / :300-310: one source sample (float).
+// src_type 2 = transparent: s(n) - sum_{i<n} h[n-i] s(i).
+float oracle_source_sample_f32(int src_type, int input_type, uint32_t step, uint32_t fs,
+                               const float* data, uint32_t data_len, const float* grid_ir,
+                               uint32_t ir_len) {
+  float sample = 0.f;
+  if (src_type == 2) {
+    float acc = 0.f;
+    for (uint32_t i = 0; i < step; ++i) {
+      float h = (step - i < ir_len) ? grid_ir[step - i] : 0.f;
+      acc += h * regular_sample_f(input_type, i, fs, data, data_len);
+    }
+    sample += regular_sample_f(input_type, step, fs, data, data_len) - acc;
+  } else {
+    sample += regular_sample_f(input_type, step, fs, data, data_len);
+  }
+  return sample;
+}
+
+// SimulationParameters.cpp:150-159 / :350-360 (double).
+double oracle_source_sample_f64(int src_type, int input_type, uint32_t step, uint32_t fs,
+                                const double* data, uint32_t data_len, const float* grid_ir,
+                                uint32_t ir_len) {
+  double sample = 0.0;
+  if (src_type == 2) {
+    double acc = 0.0;
+    for (uint32_t i = 0; i < step; ++i) {
+      float h = (step - i < ir_len) ? grid_ir[step - i] : 0.f;
+      acc += h * regular_sample_d(input_type, i, fs, data, data_len);
+    }
+    sample += regular_sample_d(input_type, step, fs, data, data_len) - acc;
+  } else {
+    sample += regular_sample_d(input_type, step, fs, data, data_len);
+  }
+  return sample;
+}
+
+// Full run (kernels3d.cu:31-203 float, :205-374 double).  P and Pp hold the
+// initial (current, past) fields and receive the final ones; out receives
+// [n_rec * steps] receiver samples, row per receiver (kernels3d.cu:183-191).
+// Returns 0, or -1 bad dims, -3 material index out of the table.
+int oracle_run(int precision, int scheme, int quirks, int64_t X, int64_t Y, int64_t Z,
+               const uint8_t* pos, const uint8_t* mat, const void* table, int n_mat,
+               const void* params, int n_src, const int64_t* src_idx,
+               const int32_t* src_type, const void* src_samples, int n_rec,
+               const int64_t* rec_idx, int64_t steps, void* P, void* Pp, void* out,
+               int threads) {
+  RunDesc d{scheme, quirks, X, Y, Z, pos, mat, table, n_mat, params, n_src, src_idx,
+            src_type, src_samples, n_rec, rec_idx, steps, threads > 0 ? threads : 1};
+  if (precision == 1)
+    return run<double>(d, (double*)P, (double*)Pp, (double*)out);
+  return run<float>(d, (float*)P, (float*)Pp, (float*)out);
+}
+
+int oracle_max_threads(void) {
+#ifdef _OPENMP
+  return omp_get_max_threads();
+#else
+  return 1;
+#endif
+}
+
+}  // extern "C"

@@ -1,0 +1,159 @@
+// Internal declarations shared by the CUDA translation units of libpfdtd.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <cuda_fp16.h>
+#include <cuda_bf16.h>
+#include <stdint.h>
+
+#include <atomic>
+#include <string>
+#include <vector>
+
+#include "pfdtd.h"
+
+namespace pfdtd {
+
+// ---------------------------------------------------------------------------
+// Error reporting: one message per host thread, read by pfdtd_last_error().
+void set_error(const std::string& msg);
+int fail(int code, const std::string& msg);
+int cuda_fail(cudaError_t e, const char* what, const char* file, int line);
+
+#define PFDTD_CK(call)                                                       \
+  do {                                                                       \
+    cudaError_t e_ = (call);                                                 \
+    if (e_ != cudaSuccess) return ::pfdtd::cuda_fail(e_, #call, __FILE__, __LINE__); \
+  } while (0)
+
+extern std::atomic<int64_t> g_launches;
+inline void count_launch(int64_t n = 1) { g_launches.fetch_add(n, std::memory_order_relaxed); }
+
+// ---------------------------------------------------------------------------
+// Arithmetic with explicit rounding.  Every product and sum is rounded on its
+// own (no fused multiply-add), in the order the reference source writes it,
+// so that the device results equal a -ffp-contract=off CPU evaluation.
+template <typename T> struct Rn;
+template <> struct Rn<float> {
+  static __device__ __forceinline__ float mul(float a, float b) { return __fmul_rn(a, b); }
+  static __device__ __forceinline__ float add(float a, float b) { return __fadd_rn(a, b); }
+  static __device__ __forceinline__ float sub(float a, float b) { return __fsub_rn(a, b); }
+};
+template <> struct Rn<double> {
+  static __device__ __forceinline__ double mul(double a, double b) { return __dmul_rn(a, b); }
+  static __device__ __forceinline__ double add(double a, double b) { return __dadd_rn(a, b); }
+  static __device__ __forceinline__ double sub(double a, double b) { return __dsub_rn(a, b); }
+};
+
+// Storage type -> arithmetic type.
+template <typename S> struct Store;
+template <> struct Store<float> {
+  using A = float;
+  static __device__ __forceinline__ float load(float v) { return v; }
+  static __device__ __forceinline__ float store(float v) { return v; }
+};
+template <> struct Store<double> {
+  using A = double;
+  static __device__ __forceinline__ double load(double v) { return v; }
+  static __device__ __forceinline__ double store(double v) { return v; }
+};
+template <> struct Store<__half> {
+  using A = float;
+  static __device__ __forceinline__ float load(__half v) { return __half2float(v); }
+  static __device__ __forceinline__ __half store(float v) { return __float2half_rn(v); }
+};
+template <> struct Store<__nv_bfloat16> {
+  using A = float;
+  static __device__ __forceinline__ float load(__nv_bfloat16 v) { return __bfloat162float(v); }
+  static __device__ __forceinline__ __nv_bfloat16 store(float v) { return __float2bfloat16_rn(v); }
+};
+
+// ---------------------------------------------------------------------------
+// Per-class coefficient table on the device.  A class is one distinct
+// (position byte, material byte) pair present in the grid; the kernels read a
+// class id per node instead of the two bytes.
+//   forward: out = a * ((b*p + l2*S) - c*pp)
+//   centred: out = a * ((l2*(S6 + Sb) - b*p) + c*pp),  pos = DIR/SIGN bits
+template <typename A>
+struct ClassTab {
+  const A* a;
+  const A* b;
+  const A* c;
+  const uint32_t* pos;
+  int n;
+};
+
+struct GraphCache {
+  cudaGraphExec_t exec = nullptr;
+  int64_t key[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+};
+
+}  // namespace pfdtd
+
+// The opaque domain handle.
+struct pfdtd_domain {
+  int device = 0;
+  int sm_count = 152;
+  int precision = PFDTD_F32;
+  int scheme = PFDTD_SRL_FORWARD;
+  int quirks = 0;
+  int64_t X = 0, Y = 0, Z = 0, XY = 0, N = 0;
+  size_t esize = 4;          // storage bytes per field element
+  int64_t margin = 0;        // elements before node 0 / after node N-1
+  void* field_base[2] = {nullptr, nullptr};
+  int cur = 0;               // index of the current field
+  uint8_t* d_pos = nullptr;
+  uint8_t* d_mat = nullptr;
+  bool nodes_set = false;
+
+  // material table and parameters (host copies, arithmetic type widened to double)
+  std::vector<double> materials;
+  int n_mat = 0, n_coef = 20;
+  double params[4] = {0.57735026918962576, 1.0 / 3.0, 1.0 / 3.0, 0.0};
+
+  // class table
+  bool classes_dirty = true;
+  int class_scheme = -1;
+  int n_classes = 0;
+  int cls_bytes = 1;
+  void* d_cls = nullptr;     // per node class id (uint8 or uint16)
+  void* d_ctab = nullptr;    // coefficient arrays (a|b|c in arithmetic type, then pos u32)
+  int64_t class_version = 0;
+
+  // sources / receivers
+  int n_src = 0;
+  int64_t n_samples = 0;
+  int64_t* d_src_idx = nullptr;
+  int32_t* d_src_mode = nullptr;   // 0 overwrite, 1 add
+  void* d_src_samples = nullptr;   // [n_src * n_samples], arithmetic type
+  std::vector<int64_t> src_idx_h;
+  std::vector<int32_t> src_type_h;
+  std::vector<uint8_t> src_samples_h;
+  int n_rec = 0;
+  int64_t* d_rec_idx = nullptr;
+  std::vector<int64_t> rec_idx_h;
+  int64_t io_version = 0;
+
+  // run scratch
+  int64_t* d_step = nullptr;
+  void* d_rec_out = nullptr;
+  size_t rec_out_bytes = 0;
+  cudaStream_t stream = nullptr;
+  pfdtd::GraphCache graph;
+  int past_step_direction = 1;
+
+  size_t arith_size() const { return precision == PFDTD_F64 ? 8 : 4; }
+  void* field(int which) const {
+    return (char*)field_base[which] + (size_t)margin * esize;
+  }
+  void* cur_field() const { return field(cur); }
+  void* past_field() const { return field(1 - cur); }
+};
+
+namespace pfdtd {
+// Implemented in stencil.cu
+int launch_update(pfdtd_domain* d, const void* cur, void* past, cudaStream_t s);
+int launch_io(pfdtd_domain* d, void* cur, void* rec_out, int64_t rec_ld, int64_t inject_end,
+              cudaStream_t s);
+int build_classes(pfdtd_domain* d);
+}  // namespace pfdtd

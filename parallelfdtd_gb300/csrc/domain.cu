@@ -1,0 +1,676 @@
+// C ABI of libpfdtd: domain lifecycle, node/material/parameter set-up,
+// sources and receivers, the step loop and field access.
+//
+// The step loop of launchFDTD3d (ParallelFDTD src/kernels/kernels3d.cu:83-181)
+// runs here entirely on the device: source samples and receiver buffers live
+// in HBM, one small kernel per step records the receivers and injects the
+// sources, one update kernel advances the field, and the pointer swap is a
+// change of kernel arguments.  Chunks of kChunk steps are captured once into
+// a CUDA graph and replayed; the host only polls the interrupt callback and
+// reports progress between chunks.
+#include "common.cuh"
+
+#include <chrono>
+#include <cstring>
+#include <mutex>
+
+namespace pfdtd {
+
+static thread_local std::string t_error;
+std::atomic<int64_t> g_launches{0};
+
+void set_error(const std::string& msg) { t_error = msg; }
+int fail(int code, const std::string& msg) {
+  t_error = msg;
+  return code;
+}
+int cuda_fail(cudaError_t e, const char* what, const char* file, int line) {
+  t_error = std::string(what) + " failed: " + cudaGetErrorString(e) + " (" + file + ":" +
+            std::to_string(line) + ")";
+  return e == cudaErrorMemoryAllocation ? PFDTD_ERR_NOMEM : PFDTD_ERR_CUDA;
+}
+
+namespace {
+
+constexpr int64_t kChunk = 50;  // steps per captured graph (even: parity preserved)
+
+size_t storage_size(int precision) {
+  switch (precision) {
+    case PFDTD_F32: return 4;
+    case PFDTD_F64: return 8;
+    case PFDTD_F16: return 2;
+    case PFDTD_BF16: return 2;
+  }
+  return 0;
+}
+
+// Flat index of element (x, y, z) with the reference's arithmetic
+// (cudaMesh.h:247-249); -1 when z lies outside the grid (the reference then
+// finds no partition and skips the node, cudaMesh.h:251-266) or the flat
+// index falls outside the allocation.
+int64_t flat_index(const pfdtd_domain* d, int64_t x, int64_t y, int64_t z) {
+  if (z < 0 || z >= d->Z) return -1;
+  const int64_t i = z * d->XY + y * d->X + x;
+  if (i < 0 || i >= d->N) return -1;
+  return i;
+}
+
+int check_domain(const pfdtd_domain* d) {
+  if (!d) return fail(PFDTD_ERR_ARG, "null domain");
+  return PFDTD_OK;
+}
+
+// Convert a host double to the storage type.
+void to_storage(int precision, double v, void* out) {
+  switch (precision) {
+    case PFDTD_F32: { float f = (float)v; std::memcpy(out, &f, 4); break; }
+    case PFDTD_F64: std::memcpy(out, &v, 8); break;
+    case PFDTD_F16: { __half h = __float2half_rn((float)v); std::memcpy(out, &h, 2); break; }
+    case PFDTD_BF16: { __nv_bfloat16 h = __float2bfloat16_rn((float)v); std::memcpy(out, &h, 2); break; }
+  }
+}
+
+double from_storage(int precision, const void* in) {
+  switch (precision) {
+    case PFDTD_F32: { float f; std::memcpy(&f, in, 4); return f; }
+    case PFDTD_F64: { double v; std::memcpy(&v, in, 8); return v; }
+    case PFDTD_F16: { __half h; std::memcpy(&h, in, 2); return __half2float(h); }
+    case PFDTD_BF16: { __nv_bfloat16 h; std::memcpy(&h, in, 2); return __bfloat162float(h); }
+  }
+  return 0.0;
+}
+
+struct DeviceGuard {
+  int prev = -1;
+  explicit DeviceGuard(int dev) {
+    cudaGetDevice(&prev);
+    if (prev != dev) cudaSetDevice(dev);
+  }
+  ~DeviceGuard() {
+    int now = -1;
+    cudaGetDevice(&now);
+    if (prev >= 0 && now != prev) cudaSetDevice(prev);
+  }
+};
+
+int ensure_rec_out(pfdtd_domain* d, int64_t steps) {
+  const size_t need = (size_t)std::max(d->n_rec, 1) * (size_t)std::max<int64_t>(steps, 1) *
+                      d->arith_size();
+  if (need <= d->rec_out_bytes) return PFDTD_OK;
+  if (d->d_rec_out) PFDTD_CK(cudaFree(d->d_rec_out));
+  d->d_rec_out = nullptr;
+  d->rec_out_bytes = 0;
+  if (cudaMalloc(&d->d_rec_out, need) != cudaSuccess)
+    return fail(PFDTD_ERR_NOMEM, "receiver buffer allocation failed");
+  d->rec_out_bytes = need;
+  return PFDTD_OK;
+}
+
+// One step on the device: io (record previous, inject this) + update + swap.
+int enqueue_step(pfdtd_domain* d, void* rec_out, int64_t rec_ld, int64_t inject_end,
+                 cudaStream_t s) {
+  int rc = launch_io(d, d->cur_field(), rec_out, rec_ld, inject_end, s);
+  if (rc) return rc;
+  rc = launch_update(d, d->cur_field(), d->past_field(), s);
+  if (rc) return rc;
+  d->cur = 1 - d->cur;
+  return PFDTD_OK;
+}
+
+// A graph of kChunk steps starting from the domain's current field.
+int get_chunk_graph(pfdtd_domain* d, void* rec_out, int64_t rec_ld, int64_t inject_end,
+                    cudaGraphExec_t* exec) {
+  const int64_t key[8] = {d->cur, kChunk, d->class_version, d->io_version,
+                          (int64_t)(intptr_t)rec_out, rec_ld, inject_end,
+                          (int64_t)(intptr_t)d->d_cls};
+  if (d->graph.exec && std::memcmp(key, d->graph.key, sizeof(key)) == 0) {
+    *exec = d->graph.exec;
+    return PFDTD_OK;
+  }
+  if (d->graph.exec) {
+    cudaGraphExecDestroy(d->graph.exec);
+    d->graph.exec = nullptr;
+  }
+  cudaStream_t s = d->stream;
+  PFDTD_CK(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal));
+  const int cur0 = d->cur;
+  const int64_t before = g_launches.load();
+  int rc = PFDTD_OK;
+  for (int64_t i = 0; i < kChunk && rc == PFDTD_OK; ++i)
+    rc = enqueue_step(d, rec_out, rec_ld, inject_end, s);
+  g_launches.store(before);  // captured, not launched
+  d->cur = cur0;
+  cudaGraph_t graph = nullptr;
+  cudaError_t e = cudaStreamEndCapture(s, &graph);
+  if (rc != PFDTD_OK) {
+    if (graph) cudaGraphDestroy(graph);
+    return rc;
+  }
+  if (e != cudaSuccess) return cuda_fail(e, "cudaStreamEndCapture", __FILE__, __LINE__);
+  e = cudaGraphInstantiate(&d->graph.exec, graph, 0);
+  cudaGraphDestroy(graph);
+  if (e != cudaSuccess) return cuda_fail(e, "cudaGraphInstantiate", __FILE__, __LINE__);
+  std::memcpy(d->graph.key, key, sizeof(key));
+  *exec = d->graph.exec;
+  return PFDTD_OK;
+}
+
+int prepare_run(pfdtd_domain* d) {
+  if (!d->nodes_set) return fail(PFDTD_ERR_STATE, "node bytes not set");
+  if (d->n_mat <= 0) return fail(PFDTD_ERR_STATE, "material table not set");
+  return build_classes(d);
+}
+
+// Queue `steps` steps recording into rec_out (device, [n_rec * steps]).
+// Between chunks `between(k_done)` may be called after waiting for chunk
+// completion; it returns non-zero to stop.
+template <typename F>
+int enqueue_run(pfdtd_domain* d, int64_t steps, void* rec_out, F&& between, bool* stopped,
+                int64_t* steps_queued) {
+  cudaStream_t s = d->stream;
+  PFDTD_CK(cudaMemsetAsync(d->d_step, 0, sizeof(int64_t), s));
+  const int64_t chunks = steps / kChunk;
+  const int64_t rem = steps - chunks * kChunk;
+  cudaEvent_t ev[2] = {nullptr, nullptr};
+  PFDTD_CK(cudaEventCreateWithFlags(&ev[0], cudaEventDisableTiming));
+  PFDTD_CK(cudaEventCreateWithFlags(&ev[1], cudaEventDisableTiming));
+  int rc = PFDTD_OK;
+  int64_t queued = 0;
+  *stopped = false;
+  for (int64_t k = 0; k < chunks; ++k) {
+    if (k >= 2) {
+      cudaError_t e = cudaEventSynchronize(ev[k % 2]);
+      if (e != cudaSuccess) { rc = cuda_fail(e, "cudaEventSynchronize", __FILE__, __LINE__); break; }
+      if (between((k - 1) * kChunk)) { *stopped = true; break; }
+    }
+    cudaGraphExec_t exec = nullptr;
+    rc = get_chunk_graph(d, rec_out, steps, steps, &exec);
+    if (rc) break;
+    cudaError_t e = cudaGraphLaunch(exec, s);
+    if (e != cudaSuccess) { rc = cuda_fail(e, "cudaGraphLaunch", __FILE__, __LINE__); break; }
+    count_launch(2 * kChunk);
+    e = cudaEventRecord(ev[k % 2], s);
+    if (e != cudaSuccess) { rc = cuda_fail(e, "cudaEventRecord", __FILE__, __LINE__); break; }
+    queued += kChunk;
+  }
+  if (rc == PFDTD_OK && !*stopped) {
+    for (int64_t i = 0; i < rem && rc == PFDTD_OK; ++i) {
+      rc = enqueue_step(d, rec_out, steps, steps, s);
+      if (rc == PFDTD_OK) ++queued;
+    }
+  }
+  // Record the receivers of the last step done; never inject.
+  if (rc == PFDTD_OK) rc = launch_io(d, d->cur_field(), rec_out, steps, 0, s);
+  cudaEventDestroy(ev[0]);
+  cudaEventDestroy(ev[1]);
+  *steps_queued = queued;
+  return rc;
+}
+
+}  // namespace
+}  // namespace pfdtd
+
+using namespace pfdtd;
+
+extern "C" {
+
+const char* pfdtd_last_error(void) { return t_error.c_str(); }
+
+const char* pfdtd_version(void) { return "pfdtd-gb300 0.1 (sm_103a)"; }
+
+int64_t pfdtd_kernel_launches(void) { return g_launches.load(); }
+
+int pfdtd_device_count(int* count) {
+  if (!count) return fail(PFDTD_ERR_ARG, "null count");
+  int n = 0;
+  cudaError_t e = cudaGetDeviceCount(&n);
+  if (e != cudaSuccess) {
+    cudaGetLastError();
+    n = 0;
+  }
+  *count = n;
+  return PFDTD_OK;
+}
+
+int pfdtd_create(int64_t dim_x, int64_t dim_y, int64_t dim_z, int precision, int device,
+                 pfdtd_domain** out) {
+  if (!out) return fail(PFDTD_ERR_ARG, "null output handle");
+  *out = nullptr;
+  if (dim_x < 1 || dim_y < 1 || dim_z < 3)
+    return fail(PFDTD_ERR_ARG, "grid must be at least 1 x 1 x 3 nodes");
+  if (dim_x > (1 << 30) || dim_y > (1 << 30) || dim_z > (1 << 30) ||
+      dim_x * dim_y > (int64_t)1 << 31)
+    return fail(PFDTD_ERR_ARG, "grid dimension too large");
+  const size_t es = storage_size(precision);
+  if (es == 0) return fail(PFDTD_ERR_ARG, "unknown precision");
+  int ndev = 0;
+  if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) {
+    cudaGetLastError();
+    return fail(PFDTD_ERR_CUDA, "no CUDA device available");
+  }
+  if (device < 0 || device >= ndev) return fail(PFDTD_ERR_ARG, "device index out of range");
+  DeviceGuard g(device);
+  pfdtd_domain* d = new pfdtd_domain();
+  d->device = device;
+  cudaDeviceGetAttribute(&d->sm_count, cudaDevAttrMultiProcessorCount, device);
+  d->precision = precision;
+  d->X = dim_x;
+  d->Y = dim_y;
+  d->Z = dim_z;
+  d->XY = dim_x * dim_y;
+  d->N = d->XY * dim_z;
+  d->esize = es;
+  // Margins of one row plus a 256-byte-aligned pad on both sides of each
+  // field keep every row-wise access of a tile with halo inside the
+  // allocation; the reference allocates N + 1 + X (cudaMesh.h:717-718).
+  const int64_t align = 256 / (int64_t)es;
+  d->margin = ((dim_x + 64 + align - 1) / align) * align;
+  const size_t fbytes = (size_t)(d->N + 2 * d->margin) * es;
+  auto cleanup = [&](int code, const char* msg) {
+    pfdtd_destroy(d);
+    return fail(code, msg);
+  };
+  if (cudaStreamCreateWithFlags(&d->stream, cudaStreamNonBlocking) != cudaSuccess)
+    return cleanup(PFDTD_ERR_CUDA, "stream creation failed");
+  for (int i = 0; i < 2; ++i) {
+    if (cudaMalloc(&d->field_base[i], fbytes) != cudaSuccess) {
+      cudaGetLastError();
+      return cleanup(PFDTD_ERR_NOMEM, "field allocation failed");
+    }
+    if (cudaMemsetAsync(d->field_base[i], 0, fbytes, d->stream) != cudaSuccess)
+      return cleanup(PFDTD_ERR_CUDA, "field clear failed");
+  }
+  if (cudaMalloc((void**)&d->d_pos, (size_t)d->N + 1 + dim_x) != cudaSuccess ||
+      cudaMalloc((void**)&d->d_mat, (size_t)d->N + 1 + dim_x) != cudaSuccess) {
+    cudaGetLastError();
+    return cleanup(PFDTD_ERR_NOMEM, "node byte allocation failed");
+  }
+  cudaMemsetAsync(d->d_pos, 0, (size_t)d->N + 1 + dim_x, d->stream);
+  cudaMemsetAsync(d->d_mat, 0, (size_t)d->N + 1 + dim_x, d->stream);
+  if (cudaMalloc((void**)&d->d_step, sizeof(int64_t)) != cudaSuccess)
+    return cleanup(PFDTD_ERR_NOMEM, "step counter allocation failed");
+  if (cudaStreamSynchronize(d->stream) != cudaSuccess)
+    return cleanup(PFDTD_ERR_CUDA, "domain initialisation failed");
+  *out = d;
+  return PFDTD_OK;
+}
+
+int pfdtd_destroy(pfdtd_domain* d) {
+  if (!d) return PFDTD_OK;
+  DeviceGuard g(d->device);
+  if (d->stream) cudaStreamSynchronize(d->stream);
+  if (d->graph.exec) cudaGraphExecDestroy(d->graph.exec);
+  void* ptrs[] = {d->field_base[0], d->field_base[1], d->d_pos, d->d_mat, d->d_cls,
+                  d->d_ctab, d->d_src_idx, d->d_src_mode, d->d_src_samples, d->d_rec_idx,
+                  d->d_step, d->d_rec_out};
+  for (void* p : ptrs)
+    if (p) cudaFree(p);
+  if (d->stream) cudaStreamDestroy(d->stream);
+  delete d;
+  return PFDTD_OK;
+}
+
+int pfdtd_get_dims(const pfdtd_domain* d, int64_t dims[3]) {
+  if (int rc = check_domain(d)) return rc;
+  dims[0] = d->X;
+  dims[1] = d->Y;
+  dims[2] = d->Z;
+  return PFDTD_OK;
+}
+
+int pfdtd_get_precision(const pfdtd_domain* d, int* precision) {
+  if (int rc = check_domain(d)) return rc;
+  *precision = d->precision;
+  return PFDTD_OK;
+}
+
+int pfdtd_set_quirks(pfdtd_domain* d, int quirks) {
+  if (int rc = check_domain(d)) return rc;
+  if (quirks & ~(PFDTD_QUIRK_MATIDX | PFDTD_QUIRK_SOFTSRC))
+    return fail(PFDTD_ERR_ARG, "unknown quirk bits");
+  if ((quirks ^ d->quirks) & PFDTD_QUIRK_MATIDX) d->classes_dirty = true;
+  if ((quirks ^ d->quirks) & PFDTD_QUIRK_SOFTSRC) {
+    d->quirks = quirks;
+    // Re-derive source modes.
+    if (d->n_src > 0) {
+      std::vector<int32_t> mode(d->n_src);
+      for (int i = 0; i < d->n_src; ++i)
+        mode[i] = (d->src_type_h[i] == PFDTD_SRC_HARD || (quirks & PFDTD_QUIRK_SOFTSRC)) ? 0 : 1;
+      DeviceGuard g(d->device);
+      PFDTD_CK(cudaMemcpy(d->d_src_mode, mode.data(), mode.size() * 4, cudaMemcpyHostToDevice));
+      d->io_version++;
+    }
+  }
+  d->quirks = quirks;
+  return PFDTD_OK;
+}
+
+int pfdtd_set_scheme(pfdtd_domain* d, int scheme) {
+  if (int rc = check_domain(d)) return rc;
+  if (scheme != PFDTD_SRL_FORWARD && scheme != PFDTD_SHARED && scheme != PFDTD_SRL)
+    return fail(PFDTD_ERR_UNSUPPORTED, "unknown update scheme");
+  const int eff_old = d->scheme == PFDTD_SRL ? PFDTD_SRL : PFDTD_SRL_FORWARD;
+  const int eff_new = scheme == PFDTD_SRL ? PFDTD_SRL : PFDTD_SRL_FORWARD;
+  if (eff_old != eff_new) d->classes_dirty = true;
+  d->scheme = scheme;
+  return PFDTD_OK;
+}
+
+int pfdtd_set_nodes(pfdtd_domain* d, const uint8_t* pos, const uint8_t* mat, int on_device) {
+  if (int rc = check_domain(d)) return rc;
+  if (!pos || !mat) return fail(PFDTD_ERR_ARG, "null node pointer");
+  DeviceGuard g(d->device);
+  const cudaMemcpyKind k = on_device ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice;
+  PFDTD_CK(cudaMemcpyAsync(d->d_pos, pos, (size_t)d->N, k, d->stream));
+  PFDTD_CK(cudaMemcpyAsync(d->d_mat, mat, (size_t)d->N, k, d->stream));
+  PFDTD_CK(cudaStreamSynchronize(d->stream));
+  d->nodes_set = true;
+  d->classes_dirty = true;
+  return PFDTD_OK;
+}
+
+int pfdtd_get_node_ptrs(pfdtd_domain* d, uint8_t** d_pos, uint8_t** d_mat) {
+  if (int rc = check_domain(d)) return rc;
+  if (d_pos) *d_pos = d->d_pos;
+  if (d_mat) *d_mat = d->d_mat;
+  return PFDTD_OK;
+}
+
+int pfdtd_get_nodes(pfdtd_domain* d, uint8_t* pos, uint8_t* mat) {
+  if (int rc = check_domain(d)) return rc;
+  DeviceGuard g(d->device);
+  PFDTD_CK(cudaStreamSynchronize(d->stream));
+  if (pos) PFDTD_CK(cudaMemcpy(pos, d->d_pos, (size_t)d->N, cudaMemcpyDeviceToHost));
+  if (mat) PFDTD_CK(cudaMemcpy(mat, d->d_mat, (size_t)d->N, cudaMemcpyDeviceToHost));
+  return PFDTD_OK;
+}
+
+int pfdtd_nodes_changed(pfdtd_domain* d) {
+  if (int rc = check_domain(d)) return rc;
+  d->nodes_set = true;
+  d->classes_dirty = true;
+  return PFDTD_OK;
+}
+
+int pfdtd_set_materials(pfdtd_domain* d, const double* table, int n_mat, int n_coef) {
+  if (int rc = check_domain(d)) return rc;
+  if (!table || n_mat <= 0 || n_coef <= 0) return fail(PFDTD_ERR_ARG, "empty material table");
+  d->materials.assign(table, table + (size_t)n_mat * n_coef);
+  d->n_mat = n_mat;
+  d->n_coef = n_coef;
+  d->classes_dirty = true;
+  return PFDTD_OK;
+}
+
+int pfdtd_set_params(pfdtd_domain* d, const double params[4]) {
+  if (int rc = check_domain(d)) return rc;
+  if (!params) return fail(PFDTD_ERR_ARG, "null parameter vector");
+  for (int i = 0; i < 4; ++i) d->params[i] = params[i];
+  d->classes_dirty = true;
+  return PFDTD_OK;
+}
+
+int pfdtd_set_sources(pfdtd_domain* d, int n, const int64_t* xyz, const int32_t* type,
+                      const void* samples, int64_t n_samples) {
+  if (int rc = check_domain(d)) return rc;
+  if (n < 0 || (n > 0 && (!xyz || !type || (!samples && n_samples > 0))) || n_samples < 0)
+    return fail(PFDTD_ERR_ARG, "invalid source arrays");
+  DeviceGuard g(d->device);
+  for (void** p : {(void**)&d->d_src_idx, (void**)&d->d_src_mode, &d->d_src_samples})
+    if (*p) {
+      PFDTD_CK(cudaFree(*p));
+      *p = nullptr;
+    }
+  d->n_src = n;
+  d->n_samples = n_samples;
+  d->src_idx_h.assign(n, -1);
+  d->src_type_h.assign(type, type + n);
+  std::vector<int32_t> mode(n);
+  for (int i = 0; i < n; ++i) {
+    d->src_idx_h[i] = flat_index(d, xyz[3 * i], xyz[3 * i + 1], xyz[3 * i + 2]);
+    if (type[i] < 0 || type[i] > 2) return fail(PFDTD_ERR_ARG, "unknown source type");
+    mode[i] = (type[i] == PFDTD_SRC_HARD || (d->quirks & PFDTD_QUIRK_SOFTSRC)) ? 0 : 1;
+  }
+  const size_t sbytes = (size_t)n * (size_t)n_samples * d->arith_size();
+  d->src_samples_h.assign((const uint8_t*)samples, (const uint8_t*)samples + sbytes);
+  const size_t n1 = std::max(n, 1);
+  PFDTD_CK(cudaMalloc((void**)&d->d_src_idx, n1 * sizeof(int64_t)));
+  PFDTD_CK(cudaMalloc((void**)&d->d_src_mode, n1 * sizeof(int32_t)));
+  PFDTD_CK(cudaMalloc(&d->d_src_samples, std::max<size_t>(sbytes, 16)));
+  if (n > 0) {
+    PFDTD_CK(cudaMemcpy(d->d_src_idx, d->src_idx_h.data(), n * sizeof(int64_t), cudaMemcpyHostToDevice));
+    PFDTD_CK(cudaMemcpy(d->d_src_mode, mode.data(), n * sizeof(int32_t), cudaMemcpyHostToDevice));
+    if (sbytes) PFDTD_CK(cudaMemcpy(d->d_src_samples, samples, sbytes, cudaMemcpyHostToDevice));
+  }
+  d->io_version++;
+  return PFDTD_OK;
+}
+
+int pfdtd_set_receivers(pfdtd_domain* d, int n, const int64_t* xyz) {
+  if (int rc = check_domain(d)) return rc;
+  if (n < 0 || (n > 0 && !xyz)) return fail(PFDTD_ERR_ARG, "invalid receiver array");
+  DeviceGuard g(d->device);
+  if (d->d_rec_idx) {
+    PFDTD_CK(cudaFree(d->d_rec_idx));
+    d->d_rec_idx = nullptr;
+  }
+  d->n_rec = n;
+  d->rec_idx_h.assign(n, -1);
+  for (int i = 0; i < n; ++i)
+    d->rec_idx_h[i] = flat_index(d, xyz[3 * i], xyz[3 * i + 1], xyz[3 * i + 2]);
+  PFDTD_CK(cudaMalloc((void**)&d->d_rec_idx, std::max(n, 1) * sizeof(int64_t)));
+  if (n > 0)
+    PFDTD_CK(cudaMemcpy(d->d_rec_idx, d->rec_idx_h.data(), n * sizeof(int64_t), cudaMemcpyHostToDevice));
+  d->io_version++;
+  return PFDTD_OK;
+}
+
+int pfdtd_run(pfdtd_domain* d, int64_t steps, void* out, pfdtd_interrupt_fn interrupt_cb,
+              pfdtd_progress_fn progress_cb, double* seconds_per_step) {
+  if (int rc = check_domain(d)) return rc;
+  if (steps < 0) return fail(PFDTD_ERR_ARG, "negative step count");
+  if (d->n_rec > 0 && !out && steps > 0) return fail(PFDTD_ERR_ARG, "null output buffer");
+  DeviceGuard g(d->device);
+  const auto t0 = std::chrono::steady_clock::now();
+  int rc = prepare_run(d);
+  if (rc) return rc;
+  if (steps == 0) {
+    if (seconds_per_step) *seconds_per_step = 0.0;
+    return PFDTD_OK;
+  }
+  if (interrupt_cb && interrupt_cb()) {
+    if (seconds_per_step) *seconds_per_step = 0.0;
+    return PFDTD_INTERRUPTED;
+  }
+  rc = ensure_rec_out(d, steps);
+  if (rc) return rc;
+  const size_t rec_bytes = (size_t)d->n_rec * (size_t)steps * d->arith_size();
+  if (rec_bytes) PFDTD_CK(cudaMemsetAsync(d->d_rec_out, 0, rec_bytes, d->stream));
+  // Progress is reported for every step index that is a multiple of 100
+  // (PROGRESS_MOD, kernels3d.h:36) once the chunk holding it has finished.
+  int64_t next_progress = 0;
+  auto between = [&](int64_t done) -> int {
+    if (progress_cb) {
+      const double el =
+          std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+      for (; next_progress < done; next_progress += 100)
+        progress_cb((int)next_progress, (int)steps, (float)(el / (double)done));
+    }
+    return (interrupt_cb && interrupt_cb()) ? 1 : 0;
+  };
+  bool stopped = false;
+  int64_t queued = 0;
+  rc = enqueue_run(d, steps, d->d_rec_out, between, &stopped, &queued);
+  if (rc) return rc;
+  // Rows of receivers outside the grid are left untouched (kernels3d.cu:184-191).
+  const size_t row = (size_t)steps * d->arith_size();
+  for (int r = 0; r < d->n_rec; ++r)
+    if (d->rec_idx_h[r] >= 0)
+      PFDTD_CK(cudaMemcpyAsync((char*)out + r * row, (char*)d->d_rec_out + r * row, row,
+                               cudaMemcpyDeviceToHost, d->stream));
+  PFDTD_CK(cudaStreamSynchronize(d->stream));
+  const double el = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+  if (progress_cb && !stopped) between(queued);
+  if (seconds_per_step) *seconds_per_step = queued > 0 ? el / (double)queued : 0.0;
+  return stopped ? PFDTD_INTERRUPTED : PFDTD_OK;
+}
+
+int pfdtd_run_device(pfdtd_domain* d, int64_t steps, void* d_out) {
+  if (int rc = check_domain(d)) return rc;
+  if (steps < 0) return fail(PFDTD_ERR_ARG, "negative step count");
+  if (d->n_rec > 0 && !d_out && steps > 0) return fail(PFDTD_ERR_ARG, "null output buffer");
+  DeviceGuard g(d->device);
+  int rc = prepare_run(d);
+  if (rc || steps == 0) return rc;
+  bool stopped = false;
+  int64_t queued = 0;
+  return enqueue_run(d, steps, d_out, [](int64_t) { return 0; }, &stopped, &queued);
+}
+
+int pfdtd_profile_update(pfdtd_domain* d, int iters) {
+  if (int rc = check_domain(d)) return rc;
+  if (iters < 0) return fail(PFDTD_ERR_ARG, "negative iteration count");
+  DeviceGuard g(d->device);
+  int rc = prepare_run(d);
+  if (rc) return rc;
+  for (int i = 0; i < iters && rc == PFDTD_OK; ++i) {
+    rc = launch_update(d, d->cur_field(), d->past_field(), d->stream);
+    d->cur = 1 - d->cur;
+  }
+  return rc;
+}
+
+int pfdtd_step(pfdtd_domain* d, int64_t step, int step_direction, void* out, int64_t num_steps) {
+  if (int rc = check_domain(d)) return rc;
+  if (step < 0) return fail(PFDTD_ERR_ARG, "negative step index");
+  DeviceGuard g(d->device);
+  int rc = prepare_run(d);
+  if (rc) return rc;
+  cudaStream_t s = d->stream;
+  // Inject samples[step] (no receiver record), then update.
+  PFDTD_CK(cudaMemcpyAsync(d->d_step, &step, sizeof(int64_t), cudaMemcpyHostToDevice, s));
+  rc = launch_io(d, d->cur_field(), nullptr, 0, INT64_MAX, s);
+  if (rc) return rc;
+  rc = launch_update(d, d->cur_field(), d->past_field(), s);
+  if (rc) return rc;
+  // kernels3d.cu:462-465: swap only while the direction is unchanged.
+  if (d->past_step_direction == step_direction) d->cur = 1 - d->cur;
+  d->past_step_direction = step_direction;
+  PFDTD_CK(cudaStreamSynchronize(s));
+  if (out && d->n_rec > 0 && step < num_steps) {
+    std::vector<uint8_t> v(d->esize);
+    for (int r = 0; r < d->n_rec; ++r) {
+      const int64_t i = d->rec_idx_h[r];
+      if (i < 0) continue;
+      PFDTD_CK(cudaMemcpy(v.data(), (char*)d->cur_field() + (size_t)i * d->esize, d->esize,
+                          cudaMemcpyDeviceToHost));
+      const double val = from_storage(d->precision, v.data());
+      if (d->precision == PFDTD_F64)
+        ((double*)out)[(int64_t)r * num_steps + step] = val;
+      else
+        ((float*)out)[(int64_t)r * num_steps + step] = (float)val;
+    }
+  }
+  return PFDTD_OK;
+}
+
+static int sample_ptr(pfdtd_domain* d, int64_t x, int64_t y, int64_t z, char** p) {
+  const int64_t i = flat_index(d, x, y, z);
+  if (i < 0) return fail(PFDTD_ERR_ARG, "element outside the grid");
+  *p = (char*)d->cur_field() + (size_t)i * d->esize;
+  return PFDTD_OK;
+}
+
+int pfdtd_set_sample(pfdtd_domain* d, int64_t x, int64_t y, int64_t z, double value) {
+  if (int rc = check_domain(d)) return rc;
+  DeviceGuard g(d->device);
+  char* p;
+  if (int rc = sample_ptr(d, x, y, z, &p)) return rc;
+  uint8_t v[8];
+  to_storage(d->precision, value, v);
+  PFDTD_CK(cudaStreamSynchronize(d->stream));
+  PFDTD_CK(cudaMemcpy(p, v, d->esize, cudaMemcpyHostToDevice));
+  return PFDTD_OK;
+}
+
+int pfdtd_add_sample(pfdtd_domain* d, int64_t x, int64_t y, int64_t z, double value) {
+  if (int rc = check_domain(d)) return rc;
+  DeviceGuard g(d->device);
+  char* p;
+  if (int rc = sample_ptr(d, x, y, z, &p)) return rc;
+  uint8_t v[8];
+  PFDTD_CK(cudaStreamSynchronize(d->stream));
+  PFDTD_CK(cudaMemcpy(v, p, d->esize, cudaMemcpyDeviceToHost));
+  // Sum in the arithmetic type of the domain.
+  double cur = from_storage(d->precision, v);
+  double sum;
+  if (d->precision == PFDTD_F64) sum = cur + value;
+  else sum = (double)((float)cur + (float)value);
+  to_storage(d->precision, sum, v);
+  PFDTD_CK(cudaMemcpy(p, v, d->esize, cudaMemcpyHostToDevice));
+  return PFDTD_OK;
+}
+
+int pfdtd_get_sample(pfdtd_domain* d, int64_t x, int64_t y, int64_t z, double* value) {
+  if (int rc = check_domain(d)) return rc;
+  if (!value) return fail(PFDTD_ERR_ARG, "null value pointer");
+  DeviceGuard g(d->device);
+  char* p;
+  if (int rc = sample_ptr(d, x, y, z, &p)) return rc;
+  uint8_t v[8];
+  PFDTD_CK(cudaStreamSynchronize(d->stream));
+  PFDTD_CK(cudaMemcpy(v, p, d->esize, cudaMemcpyDeviceToHost));
+  *value = from_storage(d->precision, v);
+  return PFDTD_OK;
+}
+
+int pfdtd_flip(pfdtd_domain* d) {
+  if (int rc = check_domain(d)) return rc;
+  d->cur = 1 - d->cur;
+  return PFDTD_OK;
+}
+
+int pfdtd_reset_fields(pfdtd_domain* d) {
+  if (int rc = check_domain(d)) return rc;
+  DeviceGuard g(d->device);
+  const size_t fbytes = (size_t)(d->N + 2 * d->margin) * d->esize;
+  for (int i = 0; i < 2; ++i) PFDTD_CK(cudaMemsetAsync(d->field_base[i], 0, fbytes, d->stream));
+  PFDTD_CK(cudaStreamSynchronize(d->stream));
+  return PFDTD_OK;
+}
+
+int pfdtd_get_field_ptr(pfdtd_domain* d, int which, void** d_ptr) {
+  if (int rc = check_domain(d)) return rc;
+  if (!d_ptr || (which != 0 && which != 1)) return fail(PFDTD_ERR_ARG, "invalid field selector");
+  *d_ptr = which == PFDTD_FIELD_CURRENT ? d->cur_field() : d->past_field();
+  return PFDTD_OK;
+}
+
+int pfdtd_download_field(pfdtd_domain* d, int which, void* host) {
+  void* p = nullptr;
+  if (int rc = pfdtd_get_field_ptr(d, which, &p)) return rc;
+  if (!host) return fail(PFDTD_ERR_ARG, "null host buffer");
+  DeviceGuard g(d->device);
+  PFDTD_CK(cudaStreamSynchronize(d->stream));
+  PFDTD_CK(cudaMemcpy(host, p, (size_t)d->N * d->esize, cudaMemcpyDeviceToHost));
+  return PFDTD_OK;
+}
+
+int pfdtd_upload_field(pfdtd_domain* d, int which, const void* host) {
+  void* p = nullptr;
+  if (int rc = pfdtd_get_field_ptr(d, which, &p)) return rc;
+  if (!host) return fail(PFDTD_ERR_ARG, "null host buffer");
+  DeviceGuard g(d->device);
+  PFDTD_CK(cudaStreamSynchronize(d->stream));
+  PFDTD_CK(cudaMemcpy(p, host, (size_t)d->N * d->esize, cudaMemcpyHostToDevice));
+  return PFDTD_OK;
+}
+
+int pfdtd_get_stream(pfdtd_domain* d, void** stream) {
+  if (int rc = check_domain(d)) return rc;
+  if (!stream) return fail(PFDTD_ERR_ARG, "null stream pointer");
+  *stream = (void*)d->stream;
+  return PFDTD_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,293 @@
+// Leapfrog pressure update kernels (SRL forward and centred, frequency-
+// independent boundaries) and the per-step source/receiver kernel.
+//
+// Update rules follow ParallelFDTD src/kernels/kernels3d.cu:485-529
+// (forward / Bilbao) and :608-665 (centred / Kowalczyk) operation for
+// operation; the coefficients that depend only on the node's (position,
+// material) pair are evaluated once per class on the host with the same
+// expressions (classes_host.cpp), and every remaining product and sum is
+// issued with an explicitly rounded intrinsic so nothing is contracted.
+#include "common.cuh"
+
+#include <algorithm>
+#include <cstring>
+
+namespace pfdtd {
+
+namespace {
+
+constexpr int kBX = 32;   // threads along x (one warp = one row segment)
+constexpr int kBY = 8;    // rows per block
+
+// z-marching update.  One thread owns the column (x, y) for z in [z0, z1):
+// P at z-1, z, z+1 stays in registers while the x/y neighbours at plane z are
+// read through the read-only cache (they are other threads' centre values).
+// Neighbour addressing is by flat offsets (+-1, +-X, +-X*Y) exactly as the
+// reference indexes, so a node on an outer x or y face sees the same wrapped
+// neighbour the reference kernel reads.
+template <typename S, typename C, int SCHEME>
+__global__ void __launch_bounds__(kBX * kBY)
+k_update_zmarch(const C* __restrict__ cls, const S* __restrict__ P, S* __restrict__ Pp,
+                ClassTab<typename Store<S>::A> tab, int X, int Y, int64_t XY, int z_last,
+                int zc, typename Store<S>::A l2) {
+  using A = typename Store<S>::A;
+  using R = Rn<A>;
+  using St = Store<S>;
+  constexpr bool kSmemTab = (sizeof(C) == 1);
+  __shared__ A sa[kSmemTab ? 256 : 1], sb[kSmemTab ? 256 : 1], sc[kSmemTab ? 256 : 1];
+  __shared__ uint32_t sp[kSmemTab ? 256 : 1];
+  if (kSmemTab) {
+    const int t = threadIdx.y * kBX + threadIdx.x;
+    for (int i = t; i < tab.n; i += kBX * kBY) {
+      sa[i] = tab.a[i];
+      sb[i] = tab.b[i];
+      sc[i] = tab.c[i];
+      sp[i] = tab.pos[i];
+    }
+    __syncthreads();
+  }
+  const int x = blockIdx.x * kBX + threadIdx.x;
+  const int y = blockIdx.y * kBY + threadIdx.y;
+  const int z0 = 1 + blockIdx.z * zc;
+  const int z1 = min(z0 + zc, z_last);
+  if (x >= X || y >= Y || z0 >= z1) return;
+  int64_t idx = (int64_t)z0 * XY + (int64_t)y * X + x;
+  A pm = St::load(P[idx - XY]);
+  A pc = St::load(P[idx]);
+  for (int z = z0; z < z1; ++z, idx += XY) {
+    const A pn = St::load(P[idx + XY]);
+    const A xm = St::load(P[idx - 1]);
+    const A xp = St::load(P[idx + 1]);
+    const A ym = St::load(P[idx - X]);
+    const A yp = St::load(P[idx + X]);
+    const unsigned c = cls[idx];
+    const A pp = St::load(Pp[idx]);
+    A ca, cb, cc;
+    uint32_t cp;
+    if (kSmemTab) {
+      ca = sa[c]; cb = sb[c]; cc = sc[c]; cp = sp[c];
+    } else {
+      ca = __ldg(tab.a + c); cb = __ldg(tab.b + c); cc = __ldg(tab.c + c); cp = __ldg(tab.pos + c);
+    }
+    A out;
+    if (SCHEME == 0) {
+      // S = P[z+1] + P[z-1] + P[y+1] + P[y-1] + P[x+1] + P[x-1]  (kernels3d.cu:525)
+      const A s6 = R::add(R::add(R::add(R::add(R::add(pn, pm), yp), ym), xp), xm);
+      // sw/(1+beta) * ((2 - K l2) p + l2 S - (1 - beta) pp)     (kernels3d.cu:526)
+      out = R::mul(ca, R::sub(R::add(R::mul(cb, pc), R::mul(l2, s6)), R::mul(cc, pp)));
+    } else {
+      // Mirrored boundary neighbour per axis (kernels3d.cu:642-659).
+      const A dx = (A)(cp & 1u), dy = (A)((cp >> 1) & 1u), dz = (A)((cp >> 2) & 1u);
+      const A bx = (cp & 0x10u) ? xp : xm;
+      const A by = (cp & 0x20u) ? yp : ym;
+      const A bz = (cp & 0x40u) ? pm : pn;
+      const A sb6 = R::add(R::add(R::mul(bx, dx), R::mul(by, dy)), R::mul(bz, dz));
+      const A s7 = R::add(R::add(R::add(R::add(R::add(R::add(xm, xp), ym), yp), pn), pm), sb6);
+      const A s = R::mul(s7, l2);
+      // (S - (2 - 6 l2) p + (beta - 1) pp) * sw / (1 + beta)  (kernels3d.cu:663)
+      out = R::mul(ca, R::add(R::sub(s, R::mul(cb, pc)), R::mul(cc, pp)));
+    }
+    Pp[idx] = St::store(out);
+    pm = pc;
+    pc = pn;
+  }
+}
+
+// Between two updates: record receivers from the current field for the step
+// just finished (kernels3d.cu:164-173), then inject this step's source
+// samples into the current field in source order (kernels3d.cu:93-104).
+template <typename S>
+__global__ void k_step_io(S* __restrict__ cur, int64_t* __restrict__ d_step, int n_rec,
+                          const int64_t* __restrict__ rec_idx,
+                          typename Store<S>::A* __restrict__ rec_out,
+                          int64_t rec_ld, int n_src, const int64_t* __restrict__ src_idx,
+                          const int32_t* __restrict__ src_mode,
+                          const typename Store<S>::A* __restrict__ samples, int64_t n_samples,
+                          int64_t inject_end) {
+  using A = typename Store<S>::A;
+  using St = Store<S>;
+  const int64_t n = *d_step;
+  if (n > 0 && rec_out != nullptr) {
+    for (int r = threadIdx.x; r < n_rec; r += blockDim.x) {
+      const int64_t i = rec_idx[r];
+      if (i >= 0 && n - 1 < rec_ld) rec_out[(int64_t)r * rec_ld + (n - 1)] = St::load(cur[i]);
+    }
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    if (n < inject_end && n < n_samples) {
+      for (int k = 0; k < n_src; ++k) {
+        const int64_t i = src_idx[k];
+        if (i < 0) continue;
+        const A v = samples[(int64_t)k * n_samples + n];
+        if (src_mode[k] == 0)
+          cur[i] = St::store(v);
+        else
+          cur[i] = St::store(Rn<A>::add(St::load(cur[i]), v));
+      }
+    }
+    *d_step = n + 1;
+  }
+}
+
+// Presence of (pos, mat) keys over the updated planes z = 1..Z-2.
+__global__ void k_key_presence(const uint8_t* __restrict__ pos, const uint8_t* __restrict__ mat,
+                               int64_t begin, int64_t end, uint8_t* __restrict__ present) {
+  for (int64_t i = begin + blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < end;
+       i += (int64_t)gridDim.x * blockDim.x)
+    present[((unsigned)pos[i] << 8) | mat[i]] = 1;
+}
+
+template <typename C>
+__global__ void k_map_classes(const uint8_t* __restrict__ pos, const uint8_t* __restrict__ mat,
+                              int64_t n, const uint16_t* __restrict__ lut, C* __restrict__ cls) {
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
+       i += (int64_t)gridDim.x * blockDim.x)
+    cls[i] = (C)lut[((unsigned)pos[i] << 8) | mat[i]];
+}
+
+template <typename S, typename C, int SCHEME>
+int launch_update_t(pfdtd_domain* d, const void* cur, void* past, cudaStream_t s) {
+  using A = typename Store<S>::A;
+  const int64_t nz = d->Z - 2;
+  if (nz <= 0) return PFDTD_OK;
+  const int gx = (int)((d->X + kBX - 1) / kBX);
+  const int gy = (int)((d->Y + kBY - 1) / kBY);
+  // Enough z-chunks for several waves of 8 resident blocks on each SM.
+  const int64_t target = (int64_t)d->sm_count * 8 * 4;
+  int64_t zc = std::max<int64_t>(8, (nz * (int64_t)gx * gy + target - 1) / target);
+  zc = std::min<int64_t>(zc, nz);
+  const int gz = (int)((nz + zc - 1) / zc);
+  const size_t as = sizeof(A);
+  const char* tb = (const char*)d->d_ctab;
+  ClassTab<A> tab{(const A*)tb, (const A*)(tb + as * d->n_classes),
+                  (const A*)(tb + 2 * as * d->n_classes),
+                  (const uint32_t*)(tb + 3 * as * d->n_classes), d->n_classes};
+  k_update_zmarch<S, C, SCHEME><<<dim3(gx, gy, gz), dim3(kBX, kBY), 0, s>>>(
+      (const C*)d->d_cls, (const S*)cur, (S*)past, tab, (int)d->X, (int)d->Y, d->XY,
+      (int)(d->Z - 1), (int)zc, (A)d->params[1]);
+  count_launch();
+  PFDTD_CK(cudaGetLastError());
+  return PFDTD_OK;
+}
+
+template <typename S>
+int launch_update_s(pfdtd_domain* d, const void* cur, void* past, cudaStream_t s) {
+  const bool centred = (d->class_scheme == PFDTD_SRL);
+  if (d->cls_bytes == 1)
+    return centred ? launch_update_t<S, uint8_t, 1>(d, cur, past, s)
+                   : launch_update_t<S, uint8_t, 0>(d, cur, past, s);
+  return centred ? launch_update_t<S, uint16_t, 1>(d, cur, past, s)
+                 : launch_update_t<S, uint16_t, 0>(d, cur, past, s);
+}
+
+template <typename S>
+int launch_io_t(pfdtd_domain* d, void* cur, void* rec_out, int64_t rec_ld, int64_t inject_end,
+                cudaStream_t s) {
+  using A = typename Store<S>::A;
+  const int threads = std::max(32, std::min(1024, ((d->n_rec + 31) / 32) * 32));
+  k_step_io<S><<<1, threads, 0, s>>>((S*)cur, d->d_step, d->n_rec, d->d_rec_idx, (A*)rec_out,
+                                    rec_ld, d->n_src, d->d_src_idx, d->d_src_mode,
+                                    (const A*)d->d_src_samples, d->n_samples, inject_end);
+  count_launch();
+  PFDTD_CK(cudaGetLastError());
+  return PFDTD_OK;
+}
+
+}  // namespace
+
+// Host-side class coefficient evaluation (classes_host.cpp).
+int eval_class_coefs(int precision, int scheme, int quirks, const double* params,
+                     const std::vector<double>& materials, int n_mat, int n_coef,
+                     const std::vector<uint16_t>& keys, std::vector<uint8_t>& out_tab);
+
+int launch_update(pfdtd_domain* d, const void* cur, void* past, cudaStream_t s) {
+  switch (d->precision) {
+    case PFDTD_F32: return launch_update_s<float>(d, cur, past, s);
+    case PFDTD_F64: return launch_update_s<double>(d, cur, past, s);
+    case PFDTD_F16: return launch_update_s<__half>(d, cur, past, s);
+    case PFDTD_BF16: return launch_update_s<__nv_bfloat16>(d, cur, past, s);
+  }
+  return fail(PFDTD_ERR_UNSUPPORTED, "unknown precision");
+}
+
+int launch_io(pfdtd_domain* d, void* cur, void* rec_out, int64_t rec_ld, int64_t inject_end,
+              cudaStream_t s) {
+  switch (d->precision) {
+    case PFDTD_F32: return launch_io_t<float>(d, cur, rec_out, rec_ld, inject_end, s);
+    case PFDTD_F64: return launch_io_t<double>(d, cur, rec_out, rec_ld, inject_end, s);
+    case PFDTD_F16: return launch_io_t<__half>(d, cur, rec_out, rec_ld, inject_end, s);
+    case PFDTD_BF16: return launch_io_t<__nv_bfloat16>(d, cur, rec_out, rec_ld, inject_end, s);
+  }
+  return fail(PFDTD_ERR_UNSUPPORTED, "unknown precision");
+}
+
+// Build the class ids and the coefficient table for the domain's current
+// scheme, quirks, parameters and materials.
+int build_classes(pfdtd_domain* d) {
+  const int scheme = (d->scheme == PFDTD_SRL) ? PFDTD_SRL : PFDTD_SRL_FORWARD;
+  if (!d->classes_dirty && d->class_scheme == scheme) return PFDTD_OK;
+  if (!d->nodes_set) return fail(PFDTD_ERR_STATE, "node bytes not set");
+  if (d->n_mat <= 0) return fail(PFDTD_ERR_STATE, "material table not set");
+  cudaStream_t s = d->stream;
+  uint8_t* d_present = nullptr;
+  PFDTD_CK(cudaMallocAsync((void**)&d_present, 65536, s));
+  PFDTD_CK(cudaMemsetAsync(d_present, 0, 65536, s));
+  const int64_t begin = d->XY, end = d->N - d->XY;
+  if (end > begin) {
+    const int64_t blocks = std::min<int64_t>((end - begin + 255) / 256, 152 * 32);
+    k_key_presence<<<(int)blocks, 256, 0, s>>>(d->d_pos, d->d_mat, begin, end, d_present);
+    count_launch();
+    PFDTD_CK(cudaGetLastError());
+  }
+  std::vector<uint8_t> present(65536);
+  PFDTD_CK(cudaMemcpyAsync(present.data(), d_present, 65536, cudaMemcpyDeviceToHost, s));
+  PFDTD_CK(cudaStreamSynchronize(s));
+  PFDTD_CK(cudaFreeAsync(d_present, s));
+  std::vector<uint16_t> keys;
+  std::vector<uint16_t> lut(65536, 0);
+  for (int k = 0; k < 65536; ++k)
+    if (present[k]) {
+      lut[k] = (uint16_t)keys.size();
+      keys.push_back((uint16_t)k);
+    }
+  if (keys.empty()) keys.push_back(0);  // grid without updated planes
+  std::vector<uint8_t> tab;
+  int rc = eval_class_coefs(d->precision, scheme, d->quirks, d->params, d->materials, d->n_mat,
+                            d->n_coef, keys, tab);
+  if (rc != PFDTD_OK) return rc;
+  const int n_classes = (int)keys.size();
+  const int cls_bytes = n_classes <= 256 ? 1 : 2;
+  if (d->d_cls == nullptr || cls_bytes > d->cls_bytes) {
+    if (d->d_cls) PFDTD_CK(cudaFree(d->d_cls));
+    d->d_cls = nullptr;
+    if (cudaMalloc(&d->d_cls, (size_t)d->N * cls_bytes + 64) != cudaSuccess)
+      return fail(PFDTD_ERR_NOMEM, "class id allocation failed");
+  }
+  d->cls_bytes = cls_bytes;
+  if (d->d_ctab) PFDTD_CK(cudaFree(d->d_ctab));
+  d->d_ctab = nullptr;
+  PFDTD_CK(cudaMalloc(&d->d_ctab, tab.size()));
+  PFDTD_CK(cudaMemcpyAsync(d->d_ctab, tab.data(), tab.size(), cudaMemcpyHostToDevice, s));
+  uint16_t* d_lut = nullptr;
+  PFDTD_CK(cudaMallocAsync((void**)&d_lut, 65536 * sizeof(uint16_t), s));
+  PFDTD_CK(cudaMemcpyAsync(d_lut, lut.data(), 65536 * sizeof(uint16_t), cudaMemcpyHostToDevice, s));
+  const int64_t blocks = std::min<int64_t>((d->N + 255) / 256, 152 * 32);
+  if (cls_bytes == 1)
+    k_map_classes<uint8_t><<<(int)blocks, 256, 0, s>>>(d->d_pos, d->d_mat, d->N, d_lut,
+                                                        (uint8_t*)d->d_cls);
+  else
+    k_map_classes<uint16_t><<<(int)blocks, 256, 0, s>>>(d->d_pos, d->d_mat, d->N, d_lut,
+                                                         (uint16_t*)d->d_cls);
+  count_launch();
+  PFDTD_CK(cudaGetLastError());
+  PFDTD_CK(cudaFreeAsync(d_lut, s));
+  PFDTD_CK(cudaStreamSynchronize(s));
+  d->n_classes = n_classes;
+  d->class_scheme = scheme;
+  d->classes_dirty = false;
+  d->class_version++;
+  return PFDTD_OK;
+}
+
+}  // namespace pfdtd

@@ -1,0 +1,215 @@
+"""Domain: Python handle over the C ABI's pfdtd_domain (include/pfdtd.h).
+
+A Domain is one whole grid on one GPU.  Arrays cross the boundary as numpy
+arrays (host memory); every call goes straight to libpfdtd.so.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import math
+from typing import Callable, Optional, Sequence, Tuple
+
+import numpy as np
+
+from . import _lib as L
+
+_PREC = {"f32": L.F32, "f64": L.F64, "f16": L.F16, "bf16": L.BF16}
+_SCHEME = {"forward": L.SRL_FORWARD, "srl_forward": L.SRL_FORWARD, "shared": L.SHARED,
+           "centred": L.SRL, "centered": L.SRL, "srl": L.SRL}
+_STORE_DTYPE = {L.F32: np.float32, L.F64: np.float64, L.F16: np.float16, L.BF16: np.uint16}
+
+
+def precision_code(p) -> int:
+    return _PREC[p] if isinstance(p, str) else int(p)
+
+
+def scheme_code(s) -> int:
+    return _SCHEME[s] if isinstance(s, str) else int(s)
+
+
+def arith_dtype(precision: int):
+    """numpy dtype of the arithmetic type (samples, receiver outputs)."""
+    return np.float64 if precision == L.F64 else np.float32
+
+
+def default_params(octave: int = 0) -> np.ndarray:
+    """[lambda, lambda^2, 1/3, octave] at lambda = 1/sqrt(3), as the reference's
+    SimulationParameters::getParameterPtrDouble (SimulationParameters.cpp:389-396)."""
+    lam = 1.0 / math.sqrt(3.0)
+    return np.array([lam, lam * lam, 1.0 / 3.0, float(octave)], dtype=np.float64)
+
+
+def _ptr(a: np.ndarray) -> C.c_void_p:
+    return C.c_void_p(a.ctypes.data)
+
+
+class Domain:
+    """One FDTD grid on one GPU (pfdtd_create ... pfdtd_destroy)."""
+
+    def __init__(self, dims: Sequence[int], precision="f32", device: int = 0):
+        self._lib = L.load()
+        X, Y, Z = (int(v) for v in dims)
+        self.dims = (X, Y, Z)
+        self.n = X * Y * Z
+        self.precision = precision_code(precision)
+        h = C.c_void_p()
+        L.call("pfdtd_create", X, Y, Z, self.precision, int(device), C.byref(h))
+        self._h = h
+        self.n_rec = 0
+        self.n_src = 0
+
+    # -- lifecycle -------------------------------------------------------
+    @property
+    def handle(self) -> C.c_void_p:
+        if self._h is None:
+            raise RuntimeError("domain closed")
+        return self._h
+
+    def close(self) -> None:
+        if getattr(self, "_h", None) is not None:
+            self._lib.pfdtd_destroy(self._h)
+            self._h = None
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    # -- set-up ----------------------------------------------------------
+    def set_quirks(self, quirks: int) -> None:
+        L.call("pfdtd_set_quirks", self.handle, int(quirks))
+
+    def set_scheme(self, scheme) -> None:
+        L.call("pfdtd_set_scheme", self.handle, scheme_code(scheme))
+
+    def set_nodes(self, pos: np.ndarray, mat: np.ndarray) -> None:
+        pos = np.ascontiguousarray(pos, dtype=np.uint8).reshape(-1)
+        mat = np.ascontiguousarray(mat, dtype=np.uint8).reshape(-1)
+        if pos.size != self.n or mat.size != self.n:
+            raise ValueError("node arrays must hold X*Y*Z bytes")
+        L.call("pfdtd_set_nodes", self.handle, _ptr(pos), _ptr(mat), 0)
+
+    def set_voxels(self, bid: np.ndarray, mat: np.ndarray, centred: bool) -> None:
+        """Upload voxelizer ids 0..27 and translate them on the device
+        (toBilbao / toKowalczyk)."""
+        self.set_nodes(bid, mat)
+        p, m = C.c_void_p(), C.c_void_p()
+        L.call("pfdtd_get_node_ptrs", self.handle, C.byref(p), C.byref(m))
+        L.call("pfdtd_encode_nodes", 1 if centred else 0, p, m, self.n, self.device_index)
+        L.call("pfdtd_nodes_changed", self.handle)
+
+    @property
+    def device_index(self) -> int:
+        return 0
+
+    def get_nodes(self) -> Tuple[np.ndarray, np.ndarray]:
+        pos = np.empty(self.n, dtype=np.uint8)
+        mat = np.empty(self.n, dtype=np.uint8)
+        L.call("pfdtd_get_nodes", self.handle, _ptr(pos), _ptr(mat))
+        return pos, mat
+
+    def count_boundaries(self, air_value: int, outside_value: int = 0) -> Tuple[int, int]:
+        p, m = C.c_void_p(), C.c_void_p()
+        L.call("pfdtd_get_node_ptrs", self.handle, C.byref(p), C.byref(m))
+        a, b = C.c_uint32(), C.c_uint32()
+        L.call("pfdtd_count_boundaries", p, self.n, air_value, outside_value, self.device_index,
+               C.byref(a), C.byref(b))
+        return int(a.value), int(b.value)
+
+    def set_materials(self, table: np.ndarray) -> None:
+        t = np.ascontiguousarray(table, dtype=np.float64)
+        if t.ndim == 1:
+            t = t.reshape(-1, 20)
+        L.call("pfdtd_set_materials", self.handle,
+               t.ctypes.data_as(C.POINTER(C.c_double)), t.shape[0], t.shape[1])
+
+    def set_params(self, params: Optional[Sequence[float]] = None) -> None:
+        p = np.ascontiguousarray(default_params() if params is None else params, dtype=np.float64)
+        L.call("pfdtd_set_params", self.handle, p.ctypes.data_as(C.POINTER(C.c_double)))
+
+    def set_sources(self, xyz: np.ndarray, types: Sequence[int], samples: np.ndarray) -> None:
+        xyz = np.ascontiguousarray(np.asarray(xyz, dtype=np.int64).reshape(-1, 3))
+        types = np.ascontiguousarray(np.asarray(types, dtype=np.int32).reshape(-1))
+        dt = arith_dtype(self.precision)
+        smp = np.ascontiguousarray(np.asarray(samples, dtype=dt).reshape(xyz.shape[0], -1))
+        self.n_src = xyz.shape[0]
+        L.call("pfdtd_set_sources", self.handle, xyz.shape[0],
+               xyz.ctypes.data_as(C.POINTER(C.c_int64)),
+               types.ctypes.data_as(C.POINTER(C.c_int32)), _ptr(smp), smp.shape[1])
+        self._src_keep = (xyz, types, smp)
+
+    def set_receivers(self, xyz: np.ndarray) -> None:
+        xyz = np.ascontiguousarray(np.asarray(xyz, dtype=np.int64).reshape(-1, 3))
+        self.n_rec = xyz.shape[0]
+        L.call("pfdtd_set_receivers", self.handle, xyz.shape[0],
+               xyz.ctypes.data_as(C.POINTER(C.c_int64)))
+
+    # -- running ---------------------------------------------------------
+    def run(self, steps: int, interrupt: Optional[Callable[[], bool]] = None,
+            progress: Optional[Callable[[int, int, float], None]] = None,
+            out: Optional[np.ndarray] = None) -> Tuple[np.ndarray, float, int]:
+        """Run `steps` steps from step 0; returns (receivers [n_rec, steps],
+        seconds per step, status)."""
+        dt = arith_dtype(self.precision)
+        if out is None:
+            out = np.zeros((max(self.n_rec, 0), steps), dtype=dt)
+        icb = L.INTERRUPT_FN(lambda: 1 if interrupt() else 0) if interrupt else L.INTERRUPT_FN()
+        pcb = L.PROGRESS_FN(progress) if progress else L.PROGRESS_FN()
+        sec = C.c_double()
+        st = L.call("pfdtd_run", self.handle, int(steps), _ptr(out) if out.size else None,
+                    icb, pcb, C.byref(sec))
+        return out, float(sec.value), st
+
+    def step(self, step: int, direction: int = 1, out: Optional[np.ndarray] = None,
+             num_steps: int = 0) -> None:
+        L.call("pfdtd_step", self.handle, int(step), int(direction),
+               _ptr(out) if out is not None else None, int(num_steps))
+
+    # -- field access ----------------------------------------------------
+    def set_sample(self, x, y, z, v) -> None:
+        L.call("pfdtd_set_sample", self.handle, x, y, z, float(v))
+
+    def add_sample(self, x, y, z, v) -> None:
+        L.call("pfdtd_add_sample", self.handle, x, y, z, float(v))
+
+    def get_sample(self, x, y, z) -> float:
+        v = C.c_double()
+        L.call("pfdtd_get_sample", self.handle, x, y, z, C.byref(v))
+        return float(v.value)
+
+    def flip(self) -> None:
+        L.call("pfdtd_flip", self.handle)
+
+    def reset_fields(self) -> None:
+        L.call("pfdtd_reset_fields", self.handle)
+
+    def download_field(self, which: int = L.FIELD_CURRENT) -> np.ndarray:
+        a = np.empty(self.n, dtype=_STORE_DTYPE[self.precision])
+        L.call("pfdtd_download_field", self.handle, int(which), _ptr(a))
+        return a
+
+    def upload_field(self, which: int, data: np.ndarray) -> None:
+        a = np.ascontiguousarray(data, dtype=_STORE_DTYPE[self.precision]).reshape(-1)
+        if a.size != self.n:
+            raise ValueError("field must hold X*Y*Z values")
+        L.call("pfdtd_upload_field", self.handle, int(which), _ptr(a))
+
+    def capture_slice(self, orientation: int, slice_idx: int) -> Tuple[np.ndarray, np.ndarray]:
+        X, Y, Z = self.dims
+        w, h = {0: (X, Y), 1: (X, Z), 2: (Y, Z)}[orientation]
+        p = np.empty((h, w), dtype=np.float32)
+        q = np.empty((h, w), dtype=np.uint8)
+        L.call("pfdtd_capture_slice", self.handle, int(orientation), int(slice_idx), _ptr(p), _ptr(q))
+        return p, q
+
+    def stream_ptr(self) -> int:
+        s = C.c_void_p()
+        L.call("pfdtd_get_stream", self.handle, C.byref(s))
+        return s.value or 0

@@ -1,0 +1,335 @@
+"""GPU parity: the CUDA path through the C ABI against the CPU oracle.
+
+The kernels evaluate the reference's update rule with every product and sum
+rounded separately and the per-class coefficients computed with the
+reference's expressions, so receiver traces and fields are expected to be
+bit-identical to the oracle (compiled with -ffp-contract=off).  The
+tolerance written in the spec contract (relative L2 <= 1e-5 for FP32,
+<= 1e-12 for FP64) is checked as well and reported on failure.
+"""
+import os
+
+import numpy as np
+import pytest
+
+from parallelfdtd_gb300 import rooms
+from parallelfdtd_gb300 import _lib as L
+from parallelfdtd_gb300.domain import Domain, default_params
+
+pytestmark = pytest.mark.gpu
+HERE = os.path.dirname(os.path.abspath(__file__))
+TOL = {"f32": 1e-5, "f64": 1e-12}
+
+
+@pytest.fixture(scope="module")
+def O(built):
+    from oracle import oracle
+    return oracle
+
+
+def rel_l2(a, b):
+    return float(np.linalg.norm(np.asarray(a, np.float64) - b) / max(np.linalg.norm(b), 1e-300))
+
+
+def assert_parity(gpu, ref, prec):
+    err = rel_l2(gpu, ref)
+    assert err <= TOL[prec], f"relative L2 {err:.3e} > {TOL[prec]}"
+    assert np.array_equal(gpu, ref), f"not bit-identical (relative L2 {err:.3e})"
+
+
+def run_both(O, room, prec, centred, srcs, rec, samples, steps, quirks=0, params=None):
+    params = default_params() if params is None else params
+    dbl = prec == "f64"
+    with Domain(room.dims, prec) as d:
+        d.set_voxels(room.bid, room.mat, centred=centred)
+        d.set_materials(room.admittance)
+        d.set_params(params)
+        d.set_scheme("centred" if centred else "forward")
+        d.set_quirks(quirks)
+        d.set_sources([s[0] for s in srcs], [s[1] for s in srcs], samples)
+        d.set_receivers(rec)
+        gpu, _, st = d.run(steps)
+        assert st == 0
+        P = d.download_field(L.FIELD_CURRENT)
+        Pp = d.download_field(L.FIELD_PAST)
+    pos, mat = O.encode_nodes(room.bid, room.mat, centred)
+    ref, rP, rPp = O.run(pos, mat, room.dims, room.admittance, params,
+                         [room.flat(*s[0]) for s in srcs], [s[1] for s in srcs], samples,
+                         [room.flat(*r) for r in rec], steps, scheme=2 if centred else 0,
+                         quirks=quirks, double=dbl)
+    return gpu, ref, (P, Pp), (rP, rPp)
+
+
+def c1_room():
+    return rooms.shoebox((64, 64, 64), n_materials=6, admittance_range=(0.01, 0.5), seed=1)
+
+
+@pytest.mark.parametrize("prec", ["f32", "f64"])
+def test_c1_shoebox_forward(gpu, O, prec):
+    """64^3 shoebox, 6 wall materials, soft Gaussian (sigma 5) at the centre,
+    receiver (16, 40, 24), 500 steps, SRL forward."""
+    room = c1_room()
+    steps = 500
+    pulse = rooms.gaussian_pulse(steps, 5.0)
+    g, r, (P, Pp), (rP, rPp) = run_both(O, room, prec, False, [((32, 32, 32), 1)],
+                                        [(16, 40, 24)], pulse[None], steps)
+    assert np.abs(r).max() > 1e-4
+    assert_parity(g, r, prec)
+    assert np.array_equal(P, rP) and np.array_equal(Pp, rPp)
+
+
+@pytest.mark.parametrize("prec", ["f32", "f64"])
+def test_centred_boxes_room(gpu, O, prec):
+    room = rooms.boxes_room((96, 64, 48), n_boxes=8, edge=(6, 20), n_materials=12, seed=4)
+    steps = 300
+    srcs = [(p, 1) for p in room.random_air_nodes(2, seed=1)]
+    rec = room.random_air_nodes(4, seed=2)
+    pulse = rooms.gaussian_pulse(steps, 4.0)
+    g, r, (P, _), (rP, _) = run_both(O, room, prec, True, srcs, rec,
+                                     np.stack([pulse, -0.5 * pulse]), steps)
+    assert_parity(g, r, prec)
+    assert np.array_equal(P, rP)
+
+
+@pytest.mark.parametrize("quirks", [L.QUIRK_MATIDX, L.QUIRK_SOFTSRC,
+                                    L.QUIRK_MATIDX | L.QUIRK_SOFTSRC])
+def test_reference_quirks(gpu, O, quirks):
+    room = rooms.shoebox((40, 36, 32), seed=5)
+    steps = 200
+    pulse = rooms.gaussian_pulse(steps, 4.0)
+    g, r, _, _ = run_both(O, room, "f32", False, [((20, 18, 16), 1)], [(8, 9, 10)],
+                          pulse[None], steps, quirks=quirks)
+    assert_parity(g, r, "f32")
+
+
+def test_octave_selects_coefficient(gpu, O):
+    room = rooms.shoebox((40, 36, 32), seed=5)
+    room.admittance[:, 3] *= 0.5
+    steps = 150
+    pulse = rooms.gaussian_pulse(steps, 4.0)
+    params = default_params(octave=3)
+    for centred in (False, True):
+        g, r, _, _ = run_both(O, room, "f32", centred, [((20, 18, 16), 1)], [(8, 9, 10)],
+                              pulse[None], steps, params=params)
+        assert_parity(g, r, "f32")
+
+
+def test_golden_fixture(gpu, O):
+    g = np.load(os.path.join(HERE, "golden", "oracle_small.npz"))
+    room = rooms.Room(tuple(int(v) for v in g["dims"]), g["bid"], g["mat"], g["admittance"])
+    pulse = g["pulse"]
+    srcs = [(tuple(int(v) for v in g["src"][0]), 1), (tuple(int(v) for v in g["src"][1]), 0)]
+    rec = [tuple(int(v) for v in r) for r in g["rec"]]
+    for centred in (False, True):
+        for prec in ("f32", "f64"):
+            with Domain(room.dims, prec) as d:
+                d.set_voxels(room.bid, room.mat, centred)
+                d.set_materials(room.admittance)
+                d.set_params()
+                d.set_scheme("centred" if centred else "forward")
+                d.set_sources([s[0] for s in srcs], [s[1] for s in srcs],
+                              np.stack([pulse, 0.5 * pulse]))
+                d.set_receivers(rec)
+                out, _, _ = d.run(pulse.size)
+            key = f"rec_{'centred' if centred else 'forward'}_{prec}"
+            assert np.array_equal(out, g[key]), key
+
+
+def test_multiple_sources_same_node_in_order(gpu, O):
+    """Hard then soft source at one node: applied in source order."""
+    room = rooms.shoebox((32, 30, 28), seed=6)
+    steps = 120
+    pulse = rooms.gaussian_pulse(steps, 3.0)
+    srcs = [((10, 10, 10), 0), ((10, 10, 10), 1), ((20, 15, 12), 2)]
+    g, r, _, _ = run_both(O, room, "f32", False, srcs, [(10, 10, 10), (5, 5, 5)],
+                          np.stack([pulse, 0.25 * pulse, -pulse]), steps)
+    assert_parity(g, r, "f32")
+
+
+def test_odd_sizes_and_edges(gpu, O):
+    """X not a multiple of 32, Z = 3 (a single updated plane), receivers and
+    sources outside the grid are skipped, step counts around the graph chunk."""
+    for dims, steps in [((37, 13, 11), 51), ((33, 7, 3), 7), ((5, 5, 64), 101)]:
+        room = rooms.shoebox(dims, seed=7)
+        X, Y, Z = dims
+        pulse = rooms.gaussian_pulse(steps, 2.0, t0=6.0)
+        src = (X // 2, Y // 2, Z // 2)
+        g, r, (P, Pp), (rP, rPp) = run_both(
+            O, room, "f32", False, [(src, 1), ((1, 1, Z + 5), 1)],
+            [src, (1, 1, Z), (X - 2, Y - 2, max(Z - 2, 1))], np.stack([pulse, pulse]), steps)
+        assert np.array_equal(g, r)
+        assert (g[1] == 0).all()
+        assert np.array_equal(P, rP) and np.array_equal(Pp, rPp)
+
+
+def test_full_size_grid_short_run(gpu, O):
+    """The 512 x 384 x 256 room with 40 boxes, 20 materials: bit-identical
+    receivers and fields after a short run (the full 2000-step run is the
+    benchmark; its size-independent checks are in test_properties_gpu)."""
+    room = rooms.boxes_room((512, 384, 256), n_boxes=40, edge=(8, 64), n_materials=20, seed=2)
+    steps = 12
+    rec = room.random_air_nodes(8, seed=9)
+    src = room.random_air_nodes(1, seed=8)[0]
+    g, r, (P, _), (rP, _) = run_both(O, room, "f32", False, [(src, 1)], rec,
+                                     rooms.impulse(steps)[None], steps)
+    assert np.array_equal(g, r)
+    assert np.array_equal(P, rP)
+
+
+def test_step_mode_equals_run(gpu, O):
+    room = rooms.shoebox((40, 36, 32), seed=3)
+    steps = 60
+    pulse = rooms.gaussian_pulse(steps, 3.0).astype(np.float32)
+    rec = [(8, 9, 10), (30, 20, 25)]
+    with Domain(room.dims, "f32") as d:
+        d.set_voxels(room.bid, room.mat, False)
+        d.set_materials(room.admittance)
+        d.set_params()
+        d.set_sources([(20, 18, 16)], [1], pulse[None])
+        d.set_receivers(rec)
+        run_out, _, _ = d.run(steps)
+        P_run = d.download_field(L.FIELD_CURRENT)
+        d.reset_fields()
+        step_out = np.zeros((2, steps), np.float32)
+        for s in range(steps):
+            d.step(s, 1, step_out, steps)
+        P_step = d.download_field(L.FIELD_CURRENT)
+    assert np.array_equal(run_out, step_out)
+    assert np.array_equal(P_run, P_step)
+
+
+def test_time_reversal_step_direction(gpu, O):
+    """A change of step direction skips the swap (kernels3d.cu:462-465)."""
+    room = rooms.shoebox((24, 20, 18), seed=3)
+    with Domain(room.dims, "f32") as d:
+        d.set_voxels(room.bid, room.mat, False)
+        d.set_materials(room.admittance)
+        d.set_params()
+        d.set_sources([(12, 10, 9)], [1], rooms.gaussian_pulse(30, 2.0, 5.0)[None])
+        for s in range(10):
+            d.step(s, 1)
+        a = d.download_field(L.FIELD_CURRENT)
+        d.step(10, -1)  # direction changed: no swap, current field unchanged
+        b = d.download_field(L.FIELD_CURRENT)
+    assert np.array_equal(a, b)
+
+
+def test_samples_and_flip(gpu):
+    room = rooms.shoebox((20, 20, 20), seed=1)
+    with Domain(room.dims, "f32") as d:
+        d.set_sample(0, 0, 0, 3.0)
+        assert d.get_sample(0, 0, 0) == 3.0
+        d.add_sample(0, 0, 0, 3.0)
+        assert d.get_sample(0, 0, 0) == 6.0  # tests/CudaMeshTest.cpp:308-318
+        d.set_sample(7, 7, 7, 1.0)
+        assert d.get_sample(7, 7, 7) == 1.0
+        d.flip()
+        assert d.get_sample(7, 7, 7) == 0.0
+        d.flip()
+        assert d.get_sample(7, 7, 7) == 1.0
+        d.reset_fields()
+        assert d.get_sample(7, 7, 7) == 0.0
+        with pytest.raises(L.PfdtdError):
+            d.get_sample(0, 0, 25)
+
+
+def test_device_setup_matches_oracle(gpu, O):
+    room = rooms.boxes_room((64, 40, 36), n_boxes=6, edge=(4, 12), seed=12)
+    for centred in (False, True):
+        with Domain(room.dims, "f32") as d:
+            d.set_voxels(room.bid, room.mat, centred)
+            pos, mat = d.get_nodes()
+            air_value = 0x80 if centred else 0x86
+            counts = d.count_boundaries(air_value)
+        rpos, rmat = O.encode_nodes(room.bid, room.mat, centred)
+        assert np.array_equal(pos, rpos) and np.array_equal(mat, rmat)
+        assert counts == O.count_boundaries(rpos, air_value)
+
+
+def test_device_padding_matches_oracle(gpu, O, lib):
+    import ctypes as C
+    rng = np.random.default_rng(0)
+    for dims, block in [((20, 20, 20), (32, 4, 2)), ((50, 37, 9), (32, 4, 1)), ((64, 64, 8), (32, 4, 1))]:
+        n = dims[0] * dims[1] * dims[2]
+        mesh = rng.integers(0, 28, n).astype(np.uint8)
+        ref, rdims = O.pad(mesh, dims, block)
+        # device round trip through a domain's node buffer as scratch input
+        with Domain((n, 1, 3), "f32") as src_d, Domain((len(ref), 1, 3), "f32") as dst_d:
+            src_d.set_nodes(np.concatenate([mesh, np.zeros(2 * n, np.uint8)]),
+                            np.zeros(3 * n, np.uint8))
+            sp, dp = C.c_void_p(), C.c_void_p()
+            L.call("pfdtd_get_node_ptrs", src_d.handle, C.byref(sp), None)
+            L.call("pfdtd_get_node_ptrs", dst_d.handle, C.byref(dp), None)
+            d3 = (C.c_uint32 * 3)(*dims)
+            od = (C.c_uint32 * 3)()
+            L.call("pfdtd_pad_mesh", sp, n, d3, block[0], block[1], block[2], dp, od, 0)
+            out, _ = dst_d.get_nodes()
+        assert tuple(od) == rdims
+        assert np.array_equal(out[:len(ref)], ref)
+
+
+def test_slice_capture(gpu, O):
+    room = rooms.shoebox((40, 36, 32), seed=3)
+    steps = 40
+    pulse = rooms.gaussian_pulse(steps, 3.0)
+    with Domain(room.dims, "f32") as d:
+        d.set_voxels(room.bid, room.mat, False)
+        d.set_materials(room.admittance)
+        d.set_params()
+        d.set_sources([(20, 18, 16)], [1], pulse[None])
+        d.run(steps)
+        P = d.download_field(L.FIELD_CURRENT).reshape(32, 36, 40)
+        pos, _ = d.get_nodes()
+        pos = pos.reshape(32, 36, 40)
+        xy, qxy = d.capture_slice(0, 16)
+        xz, qxz = d.capture_slice(1, 18)
+        yz, qyz = d.capture_slice(2, 20)
+        with pytest.raises(L.PfdtdError):
+            d.capture_slice(0, 32)
+    assert np.array_equal(xy, P[16]) and np.array_equal(qxy, pos[16])
+    # xz / yz leave the last z row uncaptured, as the reference's limit does
+    assert np.array_equal(xz[:-1], P[:-1, 18, :]) and (xz[-1] == 0).all()
+    assert np.array_equal(yz[:-1], P[:-1, :, 20]) and (qyz[-1] == 0).all()
+
+
+def test_interrupt_and_progress(gpu):
+    room = rooms.shoebox((48, 40, 32), seed=3)
+    steps = 1000
+    pulse = rooms.gaussian_pulse(steps, 3.0)
+    seen = []
+    calls = {"n": 0}
+
+    def interrupt():
+        calls["n"] += 1
+        return calls["n"] > 3
+
+    with Domain(room.dims, "f32") as d:
+        d.set_voxels(room.bid, room.mat, False)
+        d.set_materials(room.admittance)
+        d.set_params()
+        d.set_sources([(24, 20, 16)], [1], pulse[None])
+        d.set_receivers([(10, 10, 10)])
+        full, _, st = d.run(steps, progress=lambda s, m, t: seen.append((s, m)))
+        assert st == 0 and [s for s, _ in seen] == list(range(0, steps, 100))
+        part, _, st = d.run(steps, interrupt=interrupt)
+    assert st == L.INTERRUPTED
+    done = int(np.count_nonzero(part[0]))
+    assert 0 < done < steps
+    k = np.flatnonzero(part[0])[-1] + 1
+    assert np.array_equal(part[0, :k], full[0, :k]) and (part[0, k:] == 0).all()
+
+
+def test_errors_are_status_codes(gpu):
+    room = rooms.shoebox((16, 16, 16), seed=1)
+    with Domain(room.dims, "f32") as d:
+        with pytest.raises(L.PfdtdError) as e:
+            d.run(5)
+        assert e.value.status == L.ERR_STATE
+        d.set_voxels(room.bid, room.mat, False)
+        d.set_materials(room.admittance[:2])  # shell uses materials 0..5
+        d.set_params()
+        with pytest.raises(L.PfdtdError) as e:
+            d.run(5)
+        assert e.value.status == L.ERR_MATERIAL
+        with pytest.raises(L.PfdtdError):
+            d.set_scheme(7)
