@@ -95,6 +95,8 @@ int pfdtd_create(int64_t dim_x, int64_t dim_y, int64_t dim_z, int precision, int
 int pfdtd_destroy(pfdtd_domain* d);
 int pfdtd_get_dims(const pfdtd_domain* d, int64_t dims[3]);
 int pfdtd_get_precision(const pfdtd_domain* d, int* precision);
+/* Number unique to this domain among all domains created in the process. */
+int pfdtd_get_serial(const pfdtd_domain* d, int64_t* serial);
 
 /* Reference-behaviour switches, PFDTD_QUIRK_* bits; default 0. */
 int pfdtd_set_quirks(pfdtd_domain* d, int quirks);

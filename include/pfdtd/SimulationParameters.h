@@ -24,23 +24,23 @@ class SimulationParameters {
         bounding_box_min_(nv::Vec3f(0.f, 0.f, 0.f)),
         bounding_box_max_(nv::Vec3f(0.f, 0.f, 0.f)),
         add_padding_to_element_idx_(true),
-        version_(0) {}
+        version_(nextVersion()) {}
   ~SimulationParameters() {}
 
   void readGridIr(std::string ir_fp);
   void setUpdateType(enum UpdateType update_type);
-  void setC(float c) { c_ = c; ++version_; }
-  void setLambda(double lambda) { lambda_ = lambda; ++version_; }
-  void setOctave(unsigned int octave) { octave_ = octave; ++version_; }
-  void setNumSteps(unsigned int num_steps) { num_steps_ = num_steps; ++version_; }
-  void setSpatialFs(unsigned int spatial_fs) { spatial_fs_ = spatial_fs; ++version_; }
+  void setC(float c) { c_ = c; version_ = nextVersion(); }
+  void setLambda(double lambda) { lambda_ = lambda; version_ = nextVersion(); }
+  void setOctave(unsigned int octave) { octave_ = octave; version_ = nextVersion(); }
+  void setNumSteps(unsigned int num_steps) { num_steps_ = num_steps; version_ = nextVersion(); }
+  void setSpatialFs(unsigned int spatial_fs) { spatial_fs_ = spatial_fs; version_ = nextVersion(); }
   void setBoundingBox(nv::Vec3f bounding_box_min, nv::Vec3f bounding_box_max) {
     bounding_box_min_ = bounding_box_min;
     bounding_box_max_ = bounding_box_max;
   }
   void setAddPaddingToElementIdx(bool add_padding_to_element_idx) {
     add_padding_to_element_idx_ = add_padding_to_element_idx;
-    ++version_;
+    version_ = nextVersion();
   }
 
   enum UpdateType getUpdateType() const { return update_type_; }
@@ -54,8 +54,8 @@ class SimulationParameters {
 
   void addSource(float x, float y, float z);
   void addSource(Source src);
-  void addReceiver(float x, float y, float z) { receivers_.push_back(Receiver(x, y, z)); ++version_; }
-  void addReceiver(Receiver rec) { receivers_.push_back(rec); ++version_; }
+  void addReceiver(float x, float y, float z) { receivers_.push_back(Receiver(x, y, z)); version_ = nextVersion(); }
+  void addReceiver(Receiver rec) { receivers_.push_back(rec); version_ = nextVersion(); }
   void addSourceDData(float* d_vector);
   void removeSource(unsigned int i);
   void removeReceiver(unsigned int i);
@@ -64,10 +64,10 @@ class SimulationParameters {
   void resetSourcesAndReceivers();
 
   void addInputData(float* data, unsigned int number_of_samples);
-  void addInputData(std::vector<float> data) { source_input_data_.push_back(data); ++version_; }
+  void addInputData(std::vector<float> data) { source_input_data_.push_back(data); version_ = nextVersion(); }
   void addInputDataDouble(std::vector<double> data) {
     source_input_data_double_.push_back(data);
-    ++version_;
+    version_ = nextVersion();
   }
 
   float getSourceSample(unsigned int source_idx, unsigned int step);
@@ -92,9 +92,10 @@ class SimulationParameters {
   float* getParameterPtr();
   double* getParameterPtrDouble();
 
-  // Counter bumped by every change that can alter source samples or element
-  // coordinates; lets callers cache precomputed sample tables.
+  // Process-wide unique stamp renewed by every change that can alter source
+  // samples or element coordinates; lets callers cache precomputed tables.
   unsigned long long getVersion() const { return version_; }
+  static unsigned long long nextVersion();
 
  private:
   float getRegularSourceSample(unsigned int source_idx, unsigned int step);

@@ -49,6 +49,7 @@ _SIGNATURES = {
     "pfdtd_destroy": (_i32, [_vp]),
     "pfdtd_get_dims": (_i32, [_vp, C.POINTER(_i64)]),
     "pfdtd_get_precision": (_i32, [_vp, C.POINTER(_i32)]),
+    "pfdtd_get_serial": (_i32, [_vp, C.POINTER(_i64)]),
     "pfdtd_set_quirks": (_i32, [_vp, _i32]),
     "pfdtd_set_nodes": (_i32, [_vp, _vp, _vp, _i32]),
     "pfdtd_get_node_ptrs": (_i32, [_vp, C.POINTER(_vp), C.POINTER(_vp)]),

@@ -93,6 +93,7 @@ struct GraphCache {
 // The opaque domain handle.
 struct pfdtd_domain {
   int device = 0;
+  int64_t serial = 0;        // unique per created domain (never reused)
   int sm_count = 152;
   int precision = PFDTD_F32;
   int scheme = PFDTD_SRL_FORWARD;

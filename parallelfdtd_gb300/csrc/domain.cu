@@ -18,6 +18,7 @@ namespace pfdtd {
 
 static thread_local std::string t_error;
 std::atomic<int64_t> g_launches{0};
+static std::atomic<int64_t> g_serial{0};
 
 void set_error(const std::string& msg) { t_error = msg; }
 int fail(int code, const std::string& msg) {
@@ -252,6 +253,7 @@ int pfdtd_create(int64_t dim_x, int64_t dim_y, int64_t dim_z, int precision, int
   DeviceGuard g(device);
   pfdtd_domain* d = new pfdtd_domain();
   d->device = device;
+  d->serial = ++g_serial;
   cudaDeviceGetAttribute(&d->sm_count, cudaDevAttrMultiProcessorCount, device);
   d->precision = precision;
   d->X = dim_x;
@@ -315,6 +317,13 @@ int pfdtd_get_dims(const pfdtd_domain* d, int64_t dims[3]) {
   dims[0] = d->X;
   dims[1] = d->Y;
   dims[2] = d->Z;
+  return PFDTD_OK;
+}
+
+int pfdtd_get_serial(const pfdtd_domain* d, int64_t* serial) {
+  if (int rc = check_domain(d)) return rc;
+  if (!serial) return fail(PFDTD_ERR_ARG, "null serial pointer");
+  *serial = d->serial;
   return PFDTD_OK;
 }
 

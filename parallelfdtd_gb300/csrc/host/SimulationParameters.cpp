@@ -6,7 +6,14 @@
 #include <fstream>
 #include <stdexcept>
 
+#include <atomic>
+
 #include "logger.h"
+
+unsigned long long SimulationParameters::nextVersion() {
+  static std::atomic<unsigned long long> counter{0};
+  return ++counter;
+}
 
 // Whitespace-separated floats; like FileReader::readFloat
 // (src/io/FileReader.cpp:106-127) a value is kept only while the stream
@@ -16,7 +23,7 @@ void SimulationParameters::readGridIr(std::string ir_fp) {
   std::ifstream in(ir_fp.c_str());
   if (!in.good()) {
     c_log_msg(LOG_DEBUG, "SimulationParameters::readGridIr - invalid file %s", ir_fp.c_str());
-    ++version_;
+    version_ = nextVersion();
     return;
   }
   float v;
@@ -25,24 +32,24 @@ void SimulationParameters::readGridIr(std::string ir_fp) {
     if (!in.good()) break;
     grid_ir_.push_back(v);
   }
-  ++version_;
+  version_ = nextVersion();
 }
 
 void SimulationParameters::addSource(float x, float y, float z) {
   sources_.push_back(Source(x, y, z));
-  ++version_;
+  version_ = nextVersion();
 }
 
 void SimulationParameters::addSource(Source src) {
   sources_.push_back(src);
-  ++version_;
+  version_ = nextVersion();
 }
 
 void SimulationParameters::updateSourceAt(unsigned int i, Source src) {
   if (i >= sources_.size())
     c_log_msg(LOG_ERROR, "SimulationParameters::updateSourceAt : index %u out of range", i);
   sources_.at(i) = src;
-  ++version_;
+  version_ = nextVersion();
 }
 
 // The reference checks the index against the source count here
@@ -51,7 +58,7 @@ void SimulationParameters::updateReceiverAt(unsigned int i, Receiver rec) {
   if (i >= sources_.size())
     c_log_msg(LOG_ERROR, "SimulationParameters::updateReceiverAt : index %u out of range", i);
   receivers_.at(i) = rec;
-  ++version_;
+  version_ = nextVersion();
 }
 
 void SimulationParameters::removeSource(unsigned int i) {
@@ -60,7 +67,7 @@ void SimulationParameters::removeSource(unsigned int i) {
     throw std::out_of_range("SimulationParameters::removeSource: idx out of range");
   }
   sources_.erase(sources_.begin() + i);
-  ++version_;
+  version_ = nextVersion();
 }
 
 void SimulationParameters::removeReceiver(unsigned int i) {
@@ -69,13 +76,13 @@ void SimulationParameters::removeReceiver(unsigned int i) {
     throw std::out_of_range("SimulationParameters::removeReceiver: idx out of range");
   }
   receivers_.erase(receivers_.begin() + i);
-  ++version_;
+  version_ = nextVersion();
 }
 
 void SimulationParameters::resetSourcesAndReceivers() {
   receivers_.clear();
   sources_.clear();
-  ++version_;
+  version_ = nextVersion();
 }
 
 void SimulationParameters::addInputData(float* data, unsigned int number_of_samples) {
@@ -84,7 +91,7 @@ void SimulationParameters::addInputData(float* data, unsigned int number_of_samp
   if (data)
     for (unsigned int i = 0; i < number_of_samples; ++i) v[i] = data[i];
   source_input_data_.push_back(v);
-  ++version_;
+  version_ = nextVersion();
 }
 
 void SimulationParameters::addSourceDData(float* d_vector) {
@@ -97,7 +104,7 @@ void SimulationParameters::setUpdateType(enum UpdateType update_type) {
   update_type_ = update_type;
   if (update_type == SRL || update_type == SRL_FORWARD || update_type == SHARED)
     lambda_ = std::sqrt((double)1 / 3);
-  ++version_;
+  version_ = nextVersion();
 }
 
 float SimulationParameters::getSourceSample(unsigned int source_idx, unsigned int step) {

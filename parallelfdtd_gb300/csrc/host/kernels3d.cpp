@@ -23,7 +23,7 @@ void check(int rc, const char* what) {
 }
 
 struct IoCache {
-  pfdtd_domain* d = nullptr;
+  int64_t serial = -1;
   const SimulationParameters* sp = nullptr;
   unsigned long long version = ~0ull;
   bool dbl = false;
@@ -38,7 +38,11 @@ void configure(CudaMesh* m, SimulationParameters* sp, bool dbl) {
     throw(-1);
   }
   check(pfdtd_set_scheme(d, (int)sp->getUpdateType()), "launchFDTD3d - update type");
-  if (t_io.d == d && t_io.sp == sp && t_io.version == sp->getVersion() && t_io.dbl == dbl) return;
+  int64_t serial = -1;
+  pfdtd_get_serial(d, &serial);
+  if (t_io.serial == serial && t_io.sp == sp && t_io.version == sp->getVersion() &&
+      t_io.dbl == dbl)
+    return;
   const unsigned n_src = sp->getNumSources(), steps = sp->getNumSteps();
   std::vector<int64_t> xyz(3 * (size_t)n_src);
   std::vector<int32_t> type(n_src);
@@ -69,7 +73,7 @@ void configure(CudaMesh* m, SimulationParameters* sp, bool dbl) {
     rxyz[3 * i + 2] = p.z;
   }
   check(pfdtd_set_receivers(d, (int)n_rec, rxyz.data()), "launchFDTD3d - receivers");
-  t_io.d = d;
+  t_io.serial = serial;
   t_io.sp = sp;
   t_io.version = sp->getVersion();
   t_io.dbl = dbl;
