@@ -189,6 +189,24 @@ int pfdtd_upload_field(pfdtd_domain* d, int which, const void* host);
 int pfdtd_capture_slice(pfdtd_domain* d, int orientation, int64_t slice, float* p_out,
                         uint8_t* pos_out);
 
+/* Slice capture that allocates no device memory.  No counterpart in the
+ * reference: it is the same capture as pfdtd_capture_slice (same arguments,
+ * same output), for callers that cannot allocate while a simulation runs —
+ * a serving loop that has given the whole HBM budget to resident domains, or
+ * a per-step capture loop that must not stall on cudaFree, which synchronizes
+ * the device.  The slice is gathered into a fixed 5 MiB scratch array
+ * compiled into the library (held on every GPU the library is loaded on
+ * until the process exits), so a slice may hold at most 1,048,576 nodes
+ * (e.g. 1024 x 1024); larger slices return PFDTD_ERR_ARG and write nothing.
+ * The first call on a device looks up the scratch's device address
+ * (cudaGetSymbolAddress); make that first call before any stream capture.
+ * Every call shares the one scratch array: calls that overlap on the GPU
+ * (several host threads, or several domains on one device) race.  Each call
+ * writes every element of its slice, so no earlier call's data leaks into
+ * the result. */
+int pfdtd_capture_slice_noalloc(pfdtd_domain* d, int orientation, int64_t slice, float* p_out,
+                                uint8_t* pos_out);
+
 /* CUDA stream (cudaStream_t) the domain queues its work on. */
 int pfdtd_get_stream(pfdtd_domain* d, void** stream);
 

@@ -73,6 +73,7 @@ _SIGNATURES = {
     "pfdtd_download_field": (_i32, [_vp, _i32, _vp]),
     "pfdtd_upload_field": (_i32, [_vp, _i32, _vp]),
     "pfdtd_capture_slice": (_i32, [_vp, _i32, _i64, _vp, _vp]),
+    "pfdtd_capture_slice_noalloc": (_i32, [_vp, _i32, _i64, _vp, _vp]),
     "pfdtd_get_stream": (_i32, [_vp, C.POINTER(_vp)]),
     "pfdtd_kernel_launches": (_i64, []),
     "pfdtd_encode_nodes": (_i32, [_i32, _vp, _vp, _i64, _i32]),

@@ -209,6 +209,18 @@ class Domain:
         L.call("pfdtd_capture_slice", self.handle, int(orientation), int(slice_idx), _ptr(p), _ptr(q))
         return p, q
 
+    def capture_slice_noalloc(self, orientation: int, slice_idx: int) -> Tuple[np.ndarray, np.ndarray]:
+        """capture_slice without any device allocation: the slice is gathered
+        into the library's fixed scratch (at most 1,048,576 nodes per slice),
+        for callers that must not allocate device memory while running."""
+        X, Y, Z = self.dims
+        w, h = {0: (X, Y), 1: (X, Z), 2: (Y, Z)}[orientation]
+        p = np.empty((h, w), dtype=np.float32)
+        q = np.empty((h, w), dtype=np.uint8)
+        L.call("pfdtd_capture_slice_noalloc", self.handle, int(orientation), int(slice_idx),
+               _ptr(p), _ptr(q))
+        return p, q
+
     def stream_ptr(self) -> int:
         s = C.c_void_p()
         L.call("pfdtd_get_stream", self.handle, C.byref(s))
