@@ -207,6 +207,20 @@ int pfdtd_capture_slice(pfdtd_domain* d, int orientation, int64_t slice, float* 
 int pfdtd_capture_slice_noalloc(pfdtd_domain* d, int orientation, int64_t slice, float* p_out,
                                 uint8_t* pos_out);
 
+/* Update kernel variant: 0 automatic (the TMA-pipelined kernel when the
+ * grid's rows are 16-byte aligned, i.e. X a multiple of 16, FP32/FP64), 1 the
+ * register z-marching kernel, 2 the TMA kernel.  pfdtd_get_kernel reports the
+ * variant the next launch will use (1 or 2). */
+#define PFDTD_KERNEL_AUTO 0
+#define PFDTD_KERNEL_ZMARCH 1
+#define PFDTD_KERNEL_TMA 2
+int pfdtd_set_kernel(pfdtd_domain* d, int variant);
+int pfdtd_get_kernel(pfdtd_domain* d, int* variant);
+
+/* Wait for the domain's queued work and report a kernel pipeline failure
+ * (a bounded wait that expired) as PFDTD_ERR_CUDA. */
+int pfdtd_synchronize(pfdtd_domain* d);
+
 /* CUDA stream (cudaStream_t) the domain queues its work on. */
 int pfdtd_get_stream(pfdtd_domain* d, void** stream);
 

@@ -30,6 +30,7 @@ SRL_FORWARD, SHARED, SRL = 0, 1, 2
 SRC_HARD, SRC_SOFT, SRC_TRANSPARENT = 0, 1, 2
 QUIRK_MATIDX, QUIRK_SOFTSRC = 1, 2
 FIELD_CURRENT, FIELD_PAST = 0, 1
+KERNEL_AUTO, KERNEL_ZMARCH, KERNEL_TMA = 0, 1, 2
 
 INTERRUPT_FN = C.CFUNCTYPE(C.c_int)
 PROGRESS_FN = C.CFUNCTYPE(None, C.c_int, C.c_int, C.c_float)
@@ -75,6 +76,9 @@ _SIGNATURES = {
     "pfdtd_capture_slice": (_i32, [_vp, _i32, _i64, _vp, _vp]),
     "pfdtd_capture_slice_noalloc": (_i32, [_vp, _i32, _i64, _vp, _vp]),
     "pfdtd_get_stream": (_i32, [_vp, C.POINTER(_vp)]),
+    "pfdtd_set_kernel": (_i32, [_vp, _i32]),
+    "pfdtd_get_kernel": (_i32, [_vp, C.POINTER(_i32)]),
+    "pfdtd_synchronize": (_i32, [_vp]),
     "pfdtd_kernel_launches": (_i64, []),
     "pfdtd_encode_nodes": (_i32, [_i32, _vp, _vp, _i64, _i32]),
     "pfdtd_count_boundaries": (_i32, [_vp, _i64, C.c_uint8, C.c_uint8, _i32,

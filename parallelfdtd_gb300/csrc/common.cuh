@@ -1,6 +1,7 @@
 // Internal declarations shared by the CUDA translation units of libpfdtd.
 #pragma once
 
+#include <cuda.h>
 #include <cuda_runtime.h>
 #include <cuda_fp16.h>
 #include <cuda_bf16.h>
@@ -83,6 +84,22 @@ struct ClassTab {
   int n;
 };
 
+// Tensor maps of the TMA update kernel (stencil_tma.cu): each field viewed as
+// X-wide rows with and without the halo box, and the class ids.
+struct TmaState {
+  CUtensorMap halo[2];
+  CUtensorMap tile[2];
+  CUtensorMap cls;
+  int64_t key[4] = {0, 0, 0, 0};
+  bool ready = false;
+  bool attr_set[2][2][2] = {{{false, false}, {false, false}}, {{false, false}, {false, false}}};
+};
+
+// Update kernel variants.
+#define PFDTD_KERNEL_AUTO 0
+#define PFDTD_KERNEL_ZMARCH 1
+#define PFDTD_KERNEL_TMA 2
+
 struct GraphCache {
   cudaGraphExec_t exec = nullptr;
   int64_t key[8] = {0, 0, 0, 0, 0, 0, 0, 0};
@@ -143,6 +160,11 @@ struct pfdtd_domain {
   pfdtd::GraphCache graph;
   int past_step_direction = 1;
 
+  // update kernel selection and the pipeline error flag
+  int kernel_variant = PFDTD_KERNEL_AUTO;
+  int* d_err = nullptr;
+  pfdtd::TmaState tma;
+
   size_t arith_size() const { return precision == PFDTD_F64 ? 8 : 4; }
   void* field(int which) const {
     return (char*)field_base[which] + (size_t)margin * esize;
@@ -157,4 +179,7 @@ int launch_update(pfdtd_domain* d, const void* cur, void* past, cudaStream_t s);
 int launch_io(pfdtd_domain* d, void* cur, void* rec_out, int64_t rec_ld, int64_t inject_end,
               cudaStream_t s);
 int build_classes(pfdtd_domain* d);
+// Implemented in stencil_tma.cu
+bool tma_supported(const pfdtd_domain* d);
+int launch_update_tma(pfdtd_domain* d, const void* cur, void* past, cudaStream_t s);
 }  // namespace pfdtd

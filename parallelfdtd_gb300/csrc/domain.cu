@@ -11,6 +11,7 @@
 #include "common.cuh"
 
 #include <chrono>
+#include <cstdlib>
 #include <cstring>
 #include <mutex>
 
@@ -156,6 +157,18 @@ int get_chunk_graph(pfdtd_domain* d, void* rec_out, int64_t rec_ld, int64_t inje
   return PFDTD_OK;
 }
 
+// Read and clear the pipeline error flag (set by a kernel whose bounded wait
+// expired); the stream must be synchronised.
+int check_pipeline(pfdtd_domain* d) {
+  int e = 0;
+  PFDTD_CK(cudaMemcpy(&e, d->d_err, sizeof(int), cudaMemcpyDeviceToHost));
+  if (e) {
+    PFDTD_CK(cudaMemset(d->d_err, 0, sizeof(int)));
+    return fail(PFDTD_ERR_CUDA, "an update kernel's pipeline wait timed out; results are invalid");
+  }
+  return PFDTD_OK;
+}
+
 int prepare_run(pfdtd_domain* d) {
   if (!d->nodes_set) return fail(PFDTD_ERR_STATE, "node bytes not set");
   if (d->n_mat <= 0) return fail(PFDTD_ERR_STATE, "material table not set");
@@ -182,6 +195,10 @@ int enqueue_run(pfdtd_domain* d, int64_t steps, void* rec_out, F&& between, bool
     if (k >= 2) {
       cudaError_t e = cudaEventSynchronize(ev[k % 2]);
       if (e != cudaSuccess) { rc = cuda_fail(e, "cudaEventSynchronize", __FILE__, __LINE__); break; }
+      int perr = 0;
+      e = cudaMemcpy(&perr, d->d_err, sizeof(int), cudaMemcpyDeviceToHost);
+      if (e != cudaSuccess) { rc = cuda_fail(e, "error flag read", __FILE__, __LINE__); break; }
+      if (perr) { *stopped = true; break; }  // reported by check_pipeline after the sync
       if (between((k - 1) * kChunk)) { *stopped = true; break; }
     }
     cudaGraphExec_t exec = nullptr;
@@ -289,8 +306,14 @@ int pfdtd_create(int64_t dim_x, int64_t dim_y, int64_t dim_z, int precision, int
   }
   cudaMemsetAsync(d->d_pos, 0, (size_t)d->N + 1 + dim_x, d->stream);
   cudaMemsetAsync(d->d_mat, 0, (size_t)d->N + 1 + dim_x, d->stream);
-  if (cudaMalloc((void**)&d->d_step, sizeof(int64_t)) != cudaSuccess)
+  if (cudaMalloc((void**)&d->d_step, sizeof(int64_t)) != cudaSuccess ||
+      cudaMalloc((void**)&d->d_err, sizeof(int)) != cudaSuccess)
     return cleanup(PFDTD_ERR_NOMEM, "step counter allocation failed");
+  cudaMemsetAsync(d->d_err, 0, sizeof(int), d->stream);
+  if (const char* kv = std::getenv("PFDTD_KERNEL")) {
+    if (std::strcmp(kv, "zmarch") == 0) d->kernel_variant = PFDTD_KERNEL_ZMARCH;
+    if (std::strcmp(kv, "tma") == 0) d->kernel_variant = PFDTD_KERNEL_TMA;
+  }
   if (cudaStreamSynchronize(d->stream) != cudaSuccess)
     return cleanup(PFDTD_ERR_CUDA, "domain initialisation failed");
   *out = d;
@@ -304,7 +327,7 @@ int pfdtd_destroy(pfdtd_domain* d) {
   if (d->graph.exec) cudaGraphExecDestroy(d->graph.exec);
   void* ptrs[] = {d->field_base[0], d->field_base[1], d->d_pos, d->d_mat, d->d_cls,
                   d->d_ctab, d->d_src_idx, d->d_src_mode, d->d_src_samples, d->d_rec_idx,
-                  d->d_step, d->d_rec_out};
+                  d->d_step, d->d_rec_out, d->d_err};
   for (void* p : ptrs)
     if (p) cudaFree(p);
   if (d->stream) cudaStreamDestroy(d->stream);
@@ -518,6 +541,7 @@ int pfdtd_run(pfdtd_domain* d, int64_t steps, void* out, pfdtd_interrupt_fn inte
       PFDTD_CK(cudaMemcpyAsync((char*)out + r * row, (char*)d->d_rec_out + r * row, row,
                                cudaMemcpyDeviceToHost, d->stream));
   PFDTD_CK(cudaStreamSynchronize(d->stream));
+  if (int e = check_pipeline(d)) return e;
   const double el = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
   if (progress_cb && !stopped) between(queued);
   if (seconds_per_step) *seconds_per_step = queued > 0 ? el / (double)queued : 0.0;
@@ -566,6 +590,7 @@ int pfdtd_step(pfdtd_domain* d, int64_t step, int step_direction, void* out, int
   if (d->past_step_direction == step_direction) d->cur = 1 - d->cur;
   d->past_step_direction = step_direction;
   PFDTD_CK(cudaStreamSynchronize(s));
+  if (int e = check_pipeline(d)) return e;
   if (out && d->n_rec > 0 && step < num_steps) {
     std::vector<uint8_t> v(d->esize);
     for (int r = 0; r < d->n_rec; ++r) {
@@ -673,6 +698,35 @@ int pfdtd_upload_field(pfdtd_domain* d, int which, const void* host) {
   PFDTD_CK(cudaStreamSynchronize(d->stream));
   PFDTD_CK(cudaMemcpy(p, host, (size_t)d->N * d->esize, cudaMemcpyHostToDevice));
   return PFDTD_OK;
+}
+
+int pfdtd_set_kernel(pfdtd_domain* d, int variant) {
+  if (int rc = check_domain(d)) return rc;
+  if (variant < PFDTD_KERNEL_AUTO || variant > PFDTD_KERNEL_TMA)
+    return fail(PFDTD_ERR_ARG, "unknown kernel variant");
+  if (variant == PFDTD_KERNEL_TMA && d->nodes_set && !d->classes_dirty && !tma_supported(d))
+    return fail(PFDTD_ERR_UNSUPPORTED, "TMA update needs 16-byte aligned rows (X a multiple of 16)");
+  d->kernel_variant = variant;
+  if (d->graph.exec) {
+    cudaGraphExecDestroy(d->graph.exec);
+    d->graph.exec = nullptr;
+  }
+  return PFDTD_OK;
+}
+
+int pfdtd_get_kernel(pfdtd_domain* d, int* variant) {
+  if (int rc = check_domain(d)) return rc;
+  if (!variant) return fail(PFDTD_ERR_ARG, "null output");
+  const bool tma = d->kernel_variant != PFDTD_KERNEL_ZMARCH && tma_supported(d);
+  *variant = tma ? PFDTD_KERNEL_TMA : PFDTD_KERNEL_ZMARCH;
+  return PFDTD_OK;
+}
+
+int pfdtd_synchronize(pfdtd_domain* d) {
+  if (int rc = check_domain(d)) return rc;
+  DeviceGuard g(d->device);
+  PFDTD_CK(cudaStreamSynchronize(d->stream));
+  return check_pipeline(d);
 }
 
 int pfdtd_get_stream(pfdtd_domain* d, void** stream) {

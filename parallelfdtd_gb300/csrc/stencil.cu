@@ -202,6 +202,8 @@ int eval_class_coefs(int precision, int scheme, int quirks, const double* params
                      const std::vector<uint16_t>& keys, std::vector<uint8_t>& out_tab);
 
 int launch_update(pfdtd_domain* d, const void* cur, void* past, cudaStream_t s) {
+  if (d->kernel_variant != PFDTD_KERNEL_ZMARCH && tma_supported(d))
+    return launch_update_tma(d, cur, past, s);
   switch (d->precision) {
     case PFDTD_F32: return launch_update_s<float>(d, cur, past, s);
     case PFDTD_F64: return launch_update_s<double>(d, cur, past, s);

@@ -1,0 +1,432 @@
+// TMA-pipelined z-marching update (sm_103a).
+//
+// Same update rules and rounding as k_update_zmarch (stencil.cu), with the
+// planes staged through shared memory by the Tensor Memory Accelerator:
+//
+//  * one producer warp issues 2-D cp.async.bulk.tensor loads into a ring of
+//    kStages shared-memory stages; stage k holds the P^n plane z0-1+k of the
+//    CTA's tile with a one-row / 16-byte halo, and the P^{n-1} plane and class
+//    ids of plane z0+k-2 (the plane computed once P^n plane z+1 has arrived);
+//  * eight consumer warps compute plane z from stages z-1, z, z+1 and store
+//    P^{n+1} straight to global memory; after a step the stage holding plane
+//    z-1 is released to the producer through an mbarrier;
+//  * the tensor maps view each field as rows of the flat array (X wide,
+//    Y*Z rows), so the row above the last row of a plane is the first row of
+//    the next plane, exactly the flat +-X neighbour the reference reads; the
+//    x-halo outside the grid is zero-filled by the TMA, and the two nodes per
+//    row that need the flat +-1 wrap (x = 0 and x = X-1) read it from global.
+//
+// Every mbarrier wait is bounded: on expiry the kernel raises the domain's
+// error flag, stops issuing loads, waits (bounded) for the loads already in
+// flight and returns.
+#include "common.cuh"
+
+#include <cuda.h>
+
+#include <algorithm>
+#include <cstring>
+
+namespace pfdtd {
+namespace {
+
+constexpr int kTX = 64;             // tile width (nodes along x)
+constexpr int kVec = 4;             // consecutive x nodes per consumer thread
+constexpr int kThreadsPerRow = kTX / kVec;  // 16: two tile rows per warp
+constexpr uint64_t kWaitLimitNs = 2000000000ull;  // 2 s per wait, far above any real wait
+
+template <typename S> struct TmaCfg;
+template <> struct TmaCfg<float> { static constexpr int TY = 16, H = 4, NS = 8; };
+template <> struct TmaCfg<double> { static constexpr int TY = 8, H = 2, NS = 6; };
+
+// Per-class coefficients packed for one 16-byte (float) or 32-byte (double)
+// shared-memory load per node.
+template <typename A> struct alignas(4 * sizeof(A)) PackedCoef { A a, b, c; uint32_t pos; };
+
+__host__ __device__ constexpr int round128(int b) { return (b + 127) / 128 * 128; }
+
+template <typename S, typename C>
+struct Layout {
+  static constexpr int TY = TmaCfg<S>::TY, H = TmaCfg<S>::H, NS = TmaCfg<S>::NS;
+  static constexpr int PW = kTX + 2 * H;                     // plane row width with halo
+  static constexpr int P_BYTES = PW * (TY + 2) * (int)sizeof(S);
+  static constexpr int PP_BYTES = kTX * TY * (int)sizeof(S);
+  static constexpr int CL_BYTES = kTX * TY * (int)sizeof(C);
+  static constexpr int P_OFF = 0;
+  static constexpr int PP_OFF = round128(P_BYTES);
+  static constexpr int CL_OFF = PP_OFF + round128(PP_BYTES);
+  static constexpr int STAGE = CL_OFF + round128(CL_BYTES);
+  static constexpr int BAR_OFF = STAGE * NS;
+  // full + empty barriers + abort flag, plus 128 B to align the dynamic base
+  static constexpr int SMEM = BAR_OFF + 2 * NS * 8 + 16 + 128;
+  static constexpr int CONSUMER_WARPS = TY / 2;               // 16 threads x 4 nodes per row
+  static constexpr int THREADS = (CONSUMER_WARPS + 1) * 32;
+  static_assert((H * (int)sizeof(S)) % 16 == 0 && (PW * (int)sizeof(S)) % 16 == 0, "16-byte rows");
+};
+
+__device__ __forceinline__ uint32_t smem_u32(const void* p) {
+  return (uint32_t)__cvta_generic_to_shared(p);
+}
+
+__device__ __forceinline__ void mbar_init(uint32_t bar, uint32_t count) {
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(bar), "r"(count) : "memory");
+}
+
+__device__ __forceinline__ void mbar_expect_tx(uint32_t bar, uint32_t bytes) {
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(bar), "r"(bytes)
+               : "memory");
+}
+
+__device__ __forceinline__ void mbar_arrive(uint32_t bar) {
+  asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(bar) : "memory");
+}
+
+__device__ __forceinline__ uint64_t global_ns() {
+  uint64_t t;
+  asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+  return t;
+}
+
+// Wait for the phase with the given parity, for at most kWaitLimitNs; false
+// on expiry.
+__device__ __forceinline__ bool mbar_wait(uint32_t bar, uint32_t parity) {
+  uint64_t start = 0;
+  for (uint32_t i = 0;; ++i) {
+    uint32_t done;
+    asm volatile(
+        "{\n\t.reg .pred p;\n\t"
+        "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+        "selp.u32 %0, 1, 0, p;\n\t}"
+        : "=r"(done)
+        : "r"(bar), "r"(parity)
+        : "memory");
+    if (done) return true;
+    if ((i & 255) == 0) {
+      const uint64_t now = global_ns();
+      if (i == 0) start = now;
+      else if (now - start > kWaitLimitNs) return false;
+    }
+  }
+}
+
+__device__ __forceinline__ void tma_load_2d(uint32_t dst, const CUtensorMap* map, int x, int y,
+                                            uint32_t bar) {
+  asm volatile(
+      "cp.async.bulk.tensor.2d.shared::cluster.global.mbarrier::complete_tx::bytes"
+      " [%0], [%1, {%2, %3}], [%4];" ::"r"(dst),
+      "l"((uint64_t)map), "r"(x), "r"(y), "r"(bar)
+      : "memory");
+}
+
+// Four consecutive elements of a 16-byte aligned shared-memory row.
+template <typename S> struct V4 { S v[4]; };
+__device__ __forceinline__ V4<float> lds4(const float* p) {
+  const float4 t = *reinterpret_cast<const float4*>(p);
+  return V4<float>{{t.x, t.y, t.z, t.w}};
+}
+__device__ __forceinline__ V4<double> lds4(const double* p) {
+  const double2 a = reinterpret_cast<const double2*>(p)[0];
+  const double2 b = reinterpret_cast<const double2*>(p)[1];
+  return V4<double>{{a.x, a.y, b.x, b.y}};
+}
+__device__ __forceinline__ void stg4(float* p, const float (&v)[4]) {
+  *reinterpret_cast<float4*>(p) = make_float4(v[0], v[1], v[2], v[3]);
+}
+__device__ __forceinline__ void stg4(double* p, const double (&v)[4]) {
+  reinterpret_cast<double2*>(p)[0] = make_double2(v[0], v[1]);
+  reinterpret_cast<double2*>(p)[1] = make_double2(v[2], v[3]);
+}
+
+template <typename S, typename C, int SCHEME>
+__global__ void __launch_bounds__(Layout<S, C>::THREADS)
+k_update_tma(const __grid_constant__ CUtensorMap map_cur, const __grid_constant__ CUtensorMap map_past,
+             const __grid_constant__ CUtensorMap map_cls, const S* __restrict__ P,
+             S* __restrict__ Pp, ClassTab<typename Store<S>::A> tab, int X, int Y, int64_t XY,
+             int z_last, int zc, typename Store<S>::A l2, int* __restrict__ err) {
+  using A = typename Store<S>::A;
+  using R = Rn<A>;
+  using St = Store<S>;
+  using Lay = Layout<S, C>;
+  constexpr int TY = Lay::TY, H = Lay::H, NS = Lay::NS, PW = Lay::PW;
+  constexpr int kConsumerWarps = Lay::CONSUMER_WARPS, kThreads = Lay::THREADS;
+  constexpr bool kSmemTab = (sizeof(C) == 1);
+  extern __shared__ __align__(128) unsigned char smem_raw[];
+  // TMA destinations: 128-byte aligned stage buffers.
+  unsigned char* smem = (unsigned char*)(((uintptr_t)smem_raw + 127) & ~(uintptr_t)127);
+  __shared__ PackedCoef<A> stab[kSmemTab ? 256 : 1];
+
+  // A launch after one whose pipeline failed does nothing: the run is
+  // already invalid and the host reports it.
+  if (*(volatile int*)err) return;
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int x0 = blockIdx.x * kTX, y0 = blockIdx.y * TY;
+  const int z0 = 1 + blockIdx.z * zc;
+  const int z1 = min(z0 + zc, z_last);
+  const int nplanes = z1 - z0;
+  const uint32_t bar_full = smem_u32(smem + Lay::BAR_OFF);
+  const uint32_t bar_empty = bar_full + NS * 8;
+  volatile int* abort_flag = (volatile int*)(smem + Lay::BAR_OFF + 2 * NS * 8);
+
+  if (threadIdx.x == 0) {
+    for (int s = 0; s < NS; ++s) {
+      mbar_init(bar_full + 8 * s, 1);
+      mbar_init(bar_empty + 8 * s, kConsumerWarps);
+    }
+    *abort_flag = 0;
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+  }
+  if (kSmemTab) {
+    for (int i = threadIdx.x; i < tab.n; i += kThreads)
+      stab[i] = PackedCoef<A>{tab.a[i], tab.b[i], tab.c[i], tab.pos[i]};
+  }
+  __syncthreads();
+  if (nplanes <= 0) return;
+  const int K = nplanes + 2;  // loads: planes z0-1 .. z1 of P^n
+
+  if (warp == kConsumerWarps) {
+    // ---------------- producer ----------------
+    if (lane == 0) {
+      int issued = 0;
+      for (int k = 0; k < K; ++k) {
+        const int slot = k % NS;
+        if (k >= NS) {
+          if (!mbar_wait(bar_empty + 8 * slot, (uint32_t)((k / NS - 1) & 1))) {
+            atomicExch(err, 1);
+            *abort_flag = 1;
+            break;
+          }
+        }
+        if (*abort_flag) break;
+        unsigned char* st = smem + slot * Lay::STAGE;
+        const uint32_t bar = bar_full + 8 * slot;
+        const int zp = z0 - 1 + k;
+        uint32_t bytes = Lay::P_BYTES;
+        if (k >= 2) bytes += Lay::PP_BYTES + Lay::CL_BYTES;
+        mbar_expect_tx(bar, bytes);
+        tma_load_2d(smem_u32(st + Lay::P_OFF), &map_cur, x0 - H, zp * Y + y0 - 1, bar);
+        if (k >= 2) {
+          const int zc_ = z0 + k - 2;
+          tma_load_2d(smem_u32(st + Lay::PP_OFF), &map_past, x0, zc_ * Y + y0, bar);
+          tma_load_2d(smem_u32(st + Lay::CL_OFF), &map_cls, x0, zc_ * Y + y0, bar);
+        }
+        issued = k + 1;
+      }
+      // Wait (bounded) for every load still in flight before the CTA may exit.
+      for (int k = max(0, issued - NS); k < issued; ++k)
+        mbar_wait(bar_full + 8 * (k % NS), (uint32_t)((k / NS) & 1));
+    }
+    return;
+  }
+
+  // ---------------- consumers ----------------
+  // Thread -> 4 consecutive x nodes of one tile row: 16 threads per row, two
+  // rows per warp.
+  const int t = threadIdx.x;
+  const int lx = (t % kThreadsPerRow) * kVec;
+  const int ly = t / kThreadsPerRow;
+  const int x = x0 + lx;
+  const int y = y0 + ly;
+  const bool active = (x < X) && (y < Y);  // X is a multiple of 4: all 4 or none
+  const int si = (ly + 1) * PW + lx + H;   // centre of the thread's first node
+  bool ok = mbar_wait(bar_full, 0) && mbar_wait(bar_full + 8, 0);
+  for (int j = 0; j < nplanes && ok; ++j) {
+    const int sm = j % NS, sc_ = (j + 1) % NS, sp_ = (j + 2) % NS;
+    if (!mbar_wait(bar_full + 8 * sp_, (uint32_t)(((j + 2) / NS) & 1))) {
+      ok = false;
+      break;
+    }
+    if (active) {
+      const S* Pm = (const S*)(smem + sm * Lay::STAGE + Lay::P_OFF);
+      const S* Pc = (const S*)(smem + sc_ * Lay::STAGE + Lay::P_OFF);
+      const S* Pn = (const S*)(smem + sp_ * Lay::STAGE + Lay::P_OFF);
+      const S* Pq = (const S*)(smem + sp_ * Lay::STAGE + Lay::PP_OFF);
+      const C* Cl = (const C*)(smem + sp_ * Lay::STAGE + Lay::CL_OFF);
+      const int z = z0 + j;
+      const int64_t idx = (int64_t)z * XY + (int64_t)y * X + x;
+      const V4<S> vc = lds4(Pc + si);
+      const V4<S> vym = lds4(Pc + si - PW);
+      const V4<S> vyp = lds4(Pc + si + PW);
+      const V4<S> vzm = lds4(Pm + si);
+      const V4<S> vzp = lds4(Pn + si);
+      const V4<S> vpp = lds4(Pq + ly * kTX + lx);
+      A left = St::load(Pc[si - 1]);
+      A right = St::load(Pc[si + kVec]);
+      if (x == 0) left = St::load(P[idx - 1]);
+      if (x + kVec == X) right = St::load(P[idx + kVec]);
+      unsigned cid[kVec];
+      if (sizeof(C) == 1) {
+        const uint32_t w = *reinterpret_cast<const uint32_t*>(Cl + ly * kTX + lx);
+#pragma unroll
+        for (int e = 0; e < kVec; ++e) cid[e] = (w >> (8 * e)) & 0xFFu;
+      } else {
+        const uint2 w = *reinterpret_cast<const uint2*>(Cl + ly * kTX + lx);
+        cid[0] = w.x & 0xFFFFu; cid[1] = w.x >> 16; cid[2] = w.y & 0xFFFFu; cid[3] = w.y >> 16;
+      }
+      S res[kVec];
+#pragma unroll
+      for (int e = 0; e < kVec; ++e) {
+        const A pc = St::load(vc.v[e]);
+        const A xm = e == 0 ? left : St::load(vc.v[e - 1]);
+        const A xp = e == kVec - 1 ? right : St::load(vc.v[e + 1]);
+        const A ym = St::load(vym.v[e]), yp = St::load(vyp.v[e]);
+        const A pm = St::load(vzm.v[e]), pn = St::load(vzp.v[e]);
+        const A pp = St::load(vpp.v[e]);
+        PackedCoef<A> k;
+        if (kSmemTab) {
+          k = stab[cid[e]];
+        } else {
+          k = PackedCoef<A>{__ldg(tab.a + cid[e]), __ldg(tab.b + cid[e]), __ldg(tab.c + cid[e]),
+                            __ldg(tab.pos + cid[e])};
+        }
+        A out;
+        if (SCHEME == 0) {
+          const A s6 = R::add(R::add(R::add(R::add(R::add(pn, pm), yp), ym), xp), xm);
+          out = R::mul(k.a, R::sub(R::add(R::mul(k.b, pc), R::mul(l2, s6)), R::mul(k.c, pp)));
+        } else {
+          const uint32_t cp = k.pos;
+          const A dx = (A)(cp & 1u), dy = (A)((cp >> 1) & 1u), dz = (A)((cp >> 2) & 1u);
+          const A bx = (cp & 0x10u) ? xp : xm;
+          const A by = (cp & 0x20u) ? yp : ym;
+          const A bz = (cp & 0x40u) ? pm : pn;
+          const A sb6 = R::add(R::add(R::mul(bx, dx), R::mul(by, dy)), R::mul(bz, dz));
+          const A s7 = R::add(R::add(R::add(R::add(R::add(R::add(xm, xp), ym), yp), pn), pm), sb6);
+          out = R::mul(k.a, R::add(R::sub(R::mul(s7, l2), R::mul(k.b, pc)), R::mul(k.c, pp)));
+        }
+        res[e] = St::store(out);
+      }
+      stg4(Pp + idx, res);
+    }
+    __syncwarp();
+    if (lane == 0) mbar_arrive(bar_empty + 8 * sm);
+  }
+  if (!ok) {
+    atomicExch(err, 1);
+    *abort_flag = 1;
+  }
+}
+
+typedef CUresult (*EncodeTiledFn)(CUtensorMap*, CUtensorMapDataType, cuuint32_t, void*,
+                                  const cuuint64_t*, const cuuint64_t*, const cuuint32_t*,
+                                  const cuuint32_t*, CUtensorMapInterleave, CUtensorMapSwizzle,
+                                  CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
+
+EncodeTiledFn encode_fn() {
+  static EncodeTiledFn fn = nullptr;
+  static bool tried = false;
+  if (!tried) {
+    tried = true;
+    void* p = nullptr;
+    cudaDriverEntryPointQueryResult q;
+    if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault,
+                                         &q) == cudaSuccess &&
+        q == cudaDriverEntryPointSuccess)
+      fn = (EncodeTiledFn)p;
+    else
+      cudaGetLastError();
+  }
+  return fn;
+}
+
+// 2-D map over the flat array viewed as X-wide rows (Y*Z rows).
+bool make_map(CUtensorMap* m, CUtensorMapDataType dt, size_t esize, void* base, int64_t X,
+              int64_t rows, int box_x, int box_y) {
+  EncodeTiledFn fn = encode_fn();
+  if (!fn) return false;
+  cuuint64_t dims[2] = {(cuuint64_t)X, (cuuint64_t)rows};
+  cuuint64_t strides[1] = {(cuuint64_t)(X * (int64_t)esize)};
+  cuuint32_t box[2] = {(cuuint32_t)box_x, (cuuint32_t)box_y};
+  cuuint32_t es[2] = {1, 1};
+  return fn(m, dt, 2, base, dims, strides, box, es, CU_TENSOR_MAP_INTERLEAVE_NONE,
+            CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
+            CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
+}
+
+template <typename S, typename C, int SCHEME>
+int launch_tma_t(pfdtd_domain* d, const void* cur, void* past, cudaStream_t s) {
+  using A = typename Store<S>::A;
+  using Lay = Layout<S, C>;
+  const int64_t nz = d->Z - 2;
+  if (nz <= 0) return PFDTD_OK;
+  TmaState& ts = d->tma;
+  const int cur_i = (cur == d->field(0)) ? 0 : 1;
+  const int64_t key[4] = {(int64_t)(intptr_t)d->d_cls, d->cls_bytes, d->precision, 1};
+  if (!ts.ready || std::memcmp(key, ts.key, sizeof(key)) != 0) {
+    const CUtensorMapDataType dt =
+        sizeof(S) == 8 ? CU_TENSOR_MAP_DATA_TYPE_FLOAT64 : CU_TENSOR_MAP_DATA_TYPE_FLOAT32;
+    const CUtensorMapDataType ct =
+        sizeof(C) == 1 ? CU_TENSOR_MAP_DATA_TYPE_UINT8 : CU_TENSOR_MAP_DATA_TYPE_UINT16;
+    const int64_t rows = d->Y * d->Z;
+    bool ok = true;
+    for (int f = 0; f < 2; ++f) {
+      ok = ok && make_map(&ts.halo[f], dt, sizeof(S), d->field(f), d->X, rows, Lay::PW, Lay::TY + 2);
+      ok = ok && make_map(&ts.tile[f], dt, sizeof(S), d->field(f), d->X, rows, kTX, Lay::TY);
+    }
+    ok = ok && make_map(&ts.cls, ct, sizeof(C), d->d_cls, d->X, rows, kTX, Lay::TY);
+    if (!ok) return fail(PFDTD_ERR_UNSUPPORTED, "tensor map encoding failed");
+    std::memcpy(ts.key, key, sizeof(key));
+    ts.ready = true;
+  }
+  if (!ts.attr_set[sizeof(S) == 8][sizeof(C) == 2][SCHEME]) {
+    PFDTD_CK(cudaFuncSetAttribute(k_update_tma<S, C, SCHEME>,
+                                  cudaFuncAttributeMaxDynamicSharedMemorySize, Lay::SMEM));
+    ts.attr_set[sizeof(S) == 8][sizeof(C) == 2][SCHEME] = true;
+  }
+  const int gx = (int)((d->X + kTX - 1) / kTX);
+  const int gy = (int)((d->Y + Lay::TY - 1) / Lay::TY);
+  // z-chunks: several per tile so that the grid fills the machine in whole
+  // waves of (SMs x resident CTAs), each chunk at least 16 planes long.
+  const int64_t resident = (int64_t)d->sm_count * (sizeof(S) == 4 ? 2 : 1);
+  const int64_t tiles = (int64_t)gx * gy;
+  int64_t best_c = 1;
+  double best = 1e30;
+  for (int64_t c = 1; c <= std::max<int64_t>(1, nz / 16); ++c) {
+    const int64_t ctas = tiles * c;
+    const int64_t waves = (ctas + resident - 1) / resident;
+    const double eff = (double)ctas / (double)(waves * resident);  // wave fill
+    const double zlen = (double)nz / (double)c;
+    const double cost = 1.0 / eff * (1.0 + 2.0 / zlen);
+    if (cost < best - 1e-9) { best = cost; best_c = c; }
+  }
+  const int64_t zc = (nz + best_c - 1) / best_c;
+  const int gz = (int)((nz + zc - 1) / zc);
+  const size_t as = sizeof(A);
+  const char* tb = (const char*)d->d_ctab;
+  ClassTab<A> tab{(const A*)tb, (const A*)(tb + as * d->n_classes),
+                  (const A*)(tb + 2 * as * d->n_classes),
+                  (const uint32_t*)(tb + 3 * as * d->n_classes), d->n_classes};
+  k_update_tma<S, C, SCHEME><<<dim3(gx, gy, gz), Lay::THREADS, Lay::SMEM, s>>>(
+      ts.halo[cur_i], ts.tile[1 - cur_i], ts.cls, (const S*)cur, (S*)past, tab, (int)d->X,
+      (int)d->Y, d->XY, (int)(d->Z - 1), (int)zc, (A)d->params[1], d->d_err);
+  count_launch();
+  PFDTD_CK(cudaGetLastError());
+  return PFDTD_OK;
+}
+
+template <typename S>
+int launch_tma_s(pfdtd_domain* d, const void* cur, void* past, cudaStream_t s) {
+  const bool centred = (d->class_scheme == PFDTD_SRL);
+  if (d->cls_bytes == 1)
+    return centred ? launch_tma_t<S, uint8_t, 1>(d, cur, past, s)
+                   : launch_tma_t<S, uint8_t, 0>(d, cur, past, s);
+  return centred ? launch_tma_t<S, uint16_t, 1>(d, cur, past, s)
+                 : launch_tma_t<S, uint16_t, 0>(d, cur, past, s);
+}
+
+}  // namespace
+
+// The TMA path needs 16-byte aligned rows for the fields and class ids.
+bool tma_supported(const pfdtd_domain* d) {
+  if (d->precision != PFDTD_F32 && d->precision != PFDTD_F64) return false;
+  if ((d->X * (int64_t)d->esize) % 16 != 0) return false;
+  if ((d->X * (int64_t)d->cls_bytes) % 16 != 0) return false;
+  if (d->Y * d->Z >= ((int64_t)1 << 31)) return false;
+  return encode_fn() != nullptr;
+}
+
+int launch_update_tma(pfdtd_domain* d, const void* cur, void* past, cudaStream_t s) {
+  if (d->precision == PFDTD_F32) return launch_tma_s<float>(d, cur, past, s);
+  if (d->precision == PFDTD_F64) return launch_tma_s<double>(d, cur, past, s);
+  return fail(PFDTD_ERR_UNSUPPORTED, "TMA update needs FP32 or FP64 fields");
+}
+
+}  // namespace pfdtd

@@ -221,6 +221,18 @@ class Domain:
                _ptr(p), _ptr(q))
         return p, q
 
+    def set_kernel(self, variant) -> None:
+        v = {"auto": L.KERNEL_AUTO, "zmarch": L.KERNEL_ZMARCH, "tma": L.KERNEL_TMA}.get(variant, variant)
+        L.call("pfdtd_set_kernel", self.handle, int(v))
+
+    def kernel(self) -> str:
+        v = C.c_int()
+        L.call("pfdtd_get_kernel", self.handle, C.byref(v))
+        return {L.KERNEL_ZMARCH: "zmarch", L.KERNEL_TMA: "tma"}[v.value]
+
+    def synchronize(self) -> None:
+        L.call("pfdtd_synchronize", self.handle)
+
     def stream_ptr(self) -> int:
         s = C.c_void_p()
         L.call("pfdtd_get_stream", self.handle, C.byref(s))

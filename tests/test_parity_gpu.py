@@ -336,3 +336,66 @@ def test_errors_are_status_codes(gpu):
         assert e.value.status == L.ERR_MATERIAL
         with pytest.raises(L.PfdtdError):
             d.set_scheme(7)
+
+
+@pytest.mark.parametrize("variant", ["zmarch", "tma"])
+@pytest.mark.parametrize("prec,centred", [("f32", False), ("f32", True), ("f64", False), ("f64", True)])
+def test_kernel_variants_bit_identical(gpu, O, variant, prec, centred):
+    """Both update kernels (register z-marching and TMA-pipelined) against the
+    oracle, on a room whose x extent is not a multiple of the TMA tile and
+    whose y extent is not a multiple of the tile height."""
+    room = rooms.boxes_room((208, 52, 40), n_boxes=6, edge=(5, 16), n_materials=9, seed=13)
+    steps = 120
+    srcs = [(p, 1) for p in room.random_air_nodes(2, seed=3)]
+    rec = room.random_air_nodes(5, seed=4)
+    pulse = rooms.gaussian_pulse(steps, 3.0)
+    params = default_params()
+    with Domain(room.dims, prec) as d:
+        d.set_voxels(room.bid, room.mat, centred=centred)
+        d.set_materials(room.admittance)
+        d.set_params(params)
+        d.set_scheme("centred" if centred else "forward")
+        d.set_kernel(variant)
+        d.set_sources([s[0] for s in srcs], [1, 1], np.stack([pulse, 0.3 * pulse]))
+        d.set_receivers(rec)
+        g, _, _ = d.run(steps)
+        assert d.kernel() == variant
+        P = d.download_field(L.FIELD_CURRENT)
+    pos, mat = O.encode_nodes(room.bid, room.mat, centred)
+    r, rP, _ = O.run(pos, mat, room.dims, room.admittance, params, [room.flat(*s[0]) for s in srcs],
+                     [1, 1], np.stack([pulse, 0.3 * pulse]), [room.flat(*x) for x in rec], steps,
+                     scheme=2 if centred else 0, double=(prec == "f64"))
+    assert_parity(g, r, prec)
+    assert np.array_equal(P, rP)
+
+
+def test_tma_wrap_neighbours_on_outer_faces(gpu, O):
+    """Inside nodes on the outer x/y faces read the flat-index wrapped
+    neighbour, as the reference kernel does; both variants match the oracle."""
+    X, Y, Z = 64, 20, 12
+    rng = np.random.default_rng(5)
+    pos = np.full(X * Y * Z, 0x86, np.uint8)      # every node inside, K = 6
+    pos[rng.random(pos.size) < 0.1] = 0x84          # some K = 4 boundary nodes
+    mat = rng.integers(0, 3, pos.size).astype(np.uint8)
+    table = np.repeat(np.array([[0.1], [0.3], [0.6]]), 20, axis=1)
+    steps = 30
+    pulse = rooms.gaussian_pulse(steps, 2.0, t0=5.0)
+    out = {}
+    for variant in ("zmarch", "tma"):
+        with Domain((X, Y, Z), "f32") as d:
+            d.set_nodes(pos, mat)
+            d.set_materials(table)
+            d.set_params()
+            d.set_kernel(variant)
+            d.set_sources([(0, 0, 6), (X - 1, Y - 1, 5)], [1, 1], np.stack([pulse, -pulse]))
+            d.set_receivers([(0, 5, 6), (X - 1, 7, 4), (31, 0, 3)])
+            g, _, _ = d.run(steps)
+            out[variant] = (g, d.download_field(L.FIELD_CURRENT))
+    X_, Y_ = X, Y
+    r, rP, _ = O.run(pos, mat, (X, Y, Z), table, default_params(),
+                     [6 * X_ * Y_, 5 * X_ * Y_ + (Y - 1) * X + X - 1], [1, 1],
+                     np.stack([pulse, -pulse]),
+                     [6 * X * Y + 5 * X, 4 * X * Y + 7 * X + X - 1, 3 * X * Y + 31], steps)
+    for variant, (g, P) in out.items():
+        assert np.array_equal(g, r), variant
+        assert np.array_equal(P, rP), variant
