@@ -215,6 +215,11 @@ int pfdtd_capture_slice_noalloc(pfdtd_domain* d, int orientation, int64_t slice,
 #define PFDTD_KERNEL_ZMARCH 1
 #define PFDTD_KERNEL_TMA 2
 int pfdtd_set_kernel(pfdtd_domain* d, int variant);
+/* Tile shape of the TMA kernel for FP32 fields: 0 64x16, 1 128x8, 2 32x32,
+ * 3 128x16, 4 128x4 (x halo in the TMA box); 5 128x8, 6 256x4, 7 256x8,
+ * 8 256x2 (x halo read from global); -1 (default) picks the widest of
+ * 256/128/64 that divides X.  FP64 always uses 64x8. */
+int pfdtd_set_tile(pfdtd_domain* d, int tile);
 int pfdtd_get_kernel(pfdtd_domain* d, int* variant);
 
 /* Wait for the domain's queued work and report a kernel pipeline failure

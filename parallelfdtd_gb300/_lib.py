@@ -77,6 +77,7 @@ _SIGNATURES = {
     "pfdtd_capture_slice_noalloc": (_i32, [_vp, _i32, _i64, _vp, _vp]),
     "pfdtd_get_stream": (_i32, [_vp, C.POINTER(_vp)]),
     "pfdtd_set_kernel": (_i32, [_vp, _i32]),
+    "pfdtd_set_tile": (_i32, [_vp, _i32]),
     "pfdtd_get_kernel": (_i32, [_vp, C.POINTER(_i32)]),
     "pfdtd_synchronize": (_i32, [_vp]),
     "pfdtd_kernel_launches": (_i64, []),

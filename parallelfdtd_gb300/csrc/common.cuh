@@ -162,6 +162,7 @@ struct pfdtd_domain {
 
   // update kernel selection and the pipeline error flag
   int kernel_variant = PFDTD_KERNEL_AUTO;
+  int tma_tile = -1;         // tile shape of the TMA kernel, -1 automatic (stencil_tma.cu)
   int* d_err = nullptr;
   pfdtd::TmaState tma;
 
@@ -181,5 +182,6 @@ int launch_io(pfdtd_domain* d, void* cur, void* rec_out, int64_t rec_ld, int64_t
 int build_classes(pfdtd_domain* d);
 // Implemented in stencil_tma.cu
 bool tma_supported(const pfdtd_domain* d);
+int tma_tile_count();
 int launch_update_tma(pfdtd_domain* d, const void* cur, void* past, cudaStream_t s);
 }  // namespace pfdtd

@@ -310,6 +310,7 @@ int pfdtd_create(int64_t dim_x, int64_t dim_y, int64_t dim_z, int precision, int
       cudaMalloc((void**)&d->d_err, sizeof(int)) != cudaSuccess)
     return cleanup(PFDTD_ERR_NOMEM, "step counter allocation failed");
   cudaMemsetAsync(d->d_err, 0, sizeof(int), d->stream);
+  if (const char* tv = std::getenv("PFDTD_TMA_TILE")) d->tma_tile = std::atoi(tv);
   if (const char* kv = std::getenv("PFDTD_KERNEL")) {
     if (std::strcmp(kv, "zmarch") == 0) d->kernel_variant = PFDTD_KERNEL_ZMARCH;
     if (std::strcmp(kv, "tma") == 0) d->kernel_variant = PFDTD_KERNEL_TMA;
@@ -707,6 +708,17 @@ int pfdtd_set_kernel(pfdtd_domain* d, int variant) {
   if (variant == PFDTD_KERNEL_TMA && d->nodes_set && !d->classes_dirty && !tma_supported(d))
     return fail(PFDTD_ERR_UNSUPPORTED, "TMA update needs 16-byte aligned rows (X a multiple of 16)");
   d->kernel_variant = variant;
+  if (d->graph.exec) {
+    cudaGraphExecDestroy(d->graph.exec);
+    d->graph.exec = nullptr;
+  }
+  return PFDTD_OK;
+}
+
+int pfdtd_set_tile(pfdtd_domain* d, int tile) {
+  if (int rc = check_domain(d)) return rc;
+  if (tile < -1 || tile >= tma_tile_count()) return fail(PFDTD_ERR_ARG, "unknown tile shape");
+  d->tma_tile = tile;
   if (d->graph.exec) {
     cudaGraphExecDestroy(d->graph.exec);
     d->graph.exec = nullptr;

@@ -29,14 +29,9 @@
 namespace pfdtd {
 namespace {
 
-constexpr int kTX = 64;             // tile width (nodes along x)
 constexpr int kVec = 4;             // consecutive x nodes per consumer thread
-constexpr int kThreadsPerRow = kTX / kVec;  // 16: two tile rows per warp
 constexpr uint64_t kWaitLimitNs = 2000000000ull;  // 2 s per wait, far above any real wait
 
-template <typename S> struct TmaCfg;
-template <> struct TmaCfg<float> { static constexpr int TY = 16, H = 4, NS = 8; };
-template <> struct TmaCfg<double> { static constexpr int TY = 8, H = 2, NS = 6; };
 
 // Per-class coefficients packed for one 16-byte (float) or 32-byte (double)
 // shared-memory load per node.
@@ -44,13 +39,21 @@ template <typename A> struct alignas(4 * sizeof(A)) PackedCoef { A a, b, c; uint
 
 __host__ __device__ constexpr int round128(int b) { return (b + 127) / 128 * 128; }
 
-template <typename S, typename C>
+// Tile shape: TX nodes along x (box inner extent TX + 2H <= 256), TY rows,
+// NS pipeline stages.
+template <typename S, typename C, int TX_, int TY_, int NS_, bool XHALO_ = true>
 struct Layout {
-  static constexpr int TY = TmaCfg<S>::TY, H = TmaCfg<S>::H, NS = TmaCfg<S>::NS;
-  static constexpr int PW = kTX + 2 * H;                     // plane row width with halo
+  static constexpr int TX = TX_, TY = TY_, NS = NS_;
+  // With XHALO the box carries a 16-byte x halo on both sides; without it the
+  // box is exactly TX wide (up to 256) and the threads at the tile's x edges
+  // read their outside neighbour from global memory (an L2 hit: the
+  // neighbouring tile loads it).
+  static constexpr bool XHALO = XHALO_;
+  static constexpr int H = XHALO ? 16 / (int)sizeof(S) : 0;
+  static constexpr int PW = TX + 2 * H;                      // plane row width with halo
   static constexpr int P_BYTES = PW * (TY + 2) * (int)sizeof(S);
-  static constexpr int PP_BYTES = kTX * TY * (int)sizeof(S);
-  static constexpr int CL_BYTES = kTX * TY * (int)sizeof(C);
+  static constexpr int PP_BYTES = TX * TY * (int)sizeof(S);
+  static constexpr int CL_BYTES = TX * TY * (int)sizeof(C);
   static constexpr int P_OFF = 0;
   static constexpr int PP_OFF = round128(P_BYTES);
   static constexpr int CL_OFF = PP_OFF + round128(PP_BYTES);
@@ -58,9 +61,11 @@ struct Layout {
   static constexpr int BAR_OFF = STAGE * NS;
   // full + empty barriers + abort flag, plus 128 B to align the dynamic base
   static constexpr int SMEM = BAR_OFF + 2 * NS * 8 + 16 + 128;
-  static constexpr int CONSUMER_WARPS = TY / 2;               // 16 threads x 4 nodes per row
+  static constexpr int ROW_THREADS = TX / kVec;                // threads per tile row
+  static constexpr int CONSUMER_WARPS = TX * TY / kVec / 32;
   static constexpr int THREADS = (CONSUMER_WARPS + 1) * 32;
-  static_assert((H * (int)sizeof(S)) % 16 == 0 && (PW * (int)sizeof(S)) % 16 == 0, "16-byte rows");
+  static_assert(CONSUMER_WARPS * 32 * kVec == TX * TY, "consumer mapping");
+  static_assert(PW <= 256 && (PW * (int)sizeof(S)) % 16 == 0, "TMA box row");
 };
 
 __device__ __forceinline__ uint32_t smem_u32(const void* p) {
@@ -136,8 +141,8 @@ __device__ __forceinline__ void stg4(double* p, const double (&v)[4]) {
   reinterpret_cast<double2*>(p)[1] = make_double2(v[2], v[3]);
 }
 
-template <typename S, typename C, int SCHEME>
-__global__ void __launch_bounds__(Layout<S, C>::THREADS)
+template <typename S, typename C, int SCHEME, typename Lay>
+__global__ void __launch_bounds__(Lay::THREADS)
 k_update_tma(const __grid_constant__ CUtensorMap map_cur, const __grid_constant__ CUtensorMap map_past,
              const __grid_constant__ CUtensorMap map_cls, const S* __restrict__ P,
              S* __restrict__ Pp, ClassTab<typename Store<S>::A> tab, int X, int Y, int64_t XY,
@@ -145,8 +150,8 @@ k_update_tma(const __grid_constant__ CUtensorMap map_cur, const __grid_constant_
   using A = typename Store<S>::A;
   using R = Rn<A>;
   using St = Store<S>;
-  using Lay = Layout<S, C>;
-  constexpr int TY = Lay::TY, H = Lay::H, NS = Lay::NS, PW = Lay::PW;
+  constexpr int kTX = Lay::TX, TY = Lay::TY, H = Lay::H, NS = Lay::NS, PW = Lay::PW;
+  constexpr int kThreadsPerRow = Lay::ROW_THREADS;
   constexpr int kConsumerWarps = Lay::CONSUMER_WARPS, kThreads = Lay::THREADS;
   constexpr bool kSmemTab = (sizeof(C) == 1);
   extern __shared__ __align__(128) unsigned char smem_raw[];
@@ -249,10 +254,11 @@ k_update_tma(const __grid_constant__ CUtensorMap map_cur, const __grid_constant_
       const V4<S> vzm = lds4(Pm + si);
       const V4<S> vzp = lds4(Pn + si);
       const V4<S> vpp = lds4(Pq + ly * kTX + lx);
-      A left = St::load(Pc[si - 1]);
-      A right = St::load(Pc[si + kVec]);
-      if (x == 0) left = St::load(P[idx - 1]);
-      if (x + kVec == X) right = St::load(P[idx + kVec]);
+      A left, right;
+      if (x == 0 || (!Lay::XHALO && lx == 0)) left = St::load(P[idx - 1]);
+      else left = St::load(Pc[si - 1]);
+      if (x + kVec == X || (!Lay::XHALO && lx + kVec == kTX)) right = St::load(P[idx + kVec]);
+      else right = St::load(Pc[si + kVec]);
       unsigned cid[kVec];
       if (sizeof(C) == 1) {
         const uint32_t w = *reinterpret_cast<const uint32_t*>(Cl + ly * kTX + lx);
@@ -341,15 +347,16 @@ bool make_map(CUtensorMap* m, CUtensorMapDataType dt, size_t esize, void* base, 
             CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
 }
 
-template <typename S, typename C, int SCHEME>
+template <typename S, typename C, int SCHEME, typename Lay>
 int launch_tma_t(pfdtd_domain* d, const void* cur, void* past, cudaStream_t s) {
   using A = typename Store<S>::A;
-  using Lay = Layout<S, C>;
+  constexpr int kTX = Lay::TX;
   const int64_t nz = d->Z - 2;
   if (nz <= 0) return PFDTD_OK;
   TmaState& ts = d->tma;
   const int cur_i = (cur == d->field(0)) ? 0 : 1;
-  const int64_t key[4] = {(int64_t)(intptr_t)d->d_cls, d->cls_bytes, d->precision, 1};
+  const int64_t key[4] = {(int64_t)(intptr_t)d->d_cls, d->cls_bytes, d->precision,
+                          (int64_t)Lay::TX * 10000 + Lay::TY * 10 + (Lay::XHALO ? 1 : 0)};
   if (!ts.ready || std::memcmp(key, ts.key, sizeof(key)) != 0) {
     const CUtensorMapDataType dt =
         sizeof(S) == 8 ? CU_TENSOR_MAP_DATA_TYPE_FLOAT64 : CU_TENSOR_MAP_DATA_TYPE_FLOAT32;
@@ -366,16 +373,18 @@ int launch_tma_t(pfdtd_domain* d, const void* cur, void* past, cudaStream_t s) {
     std::memcpy(ts.key, key, sizeof(key));
     ts.ready = true;
   }
-  if (!ts.attr_set[sizeof(S) == 8][sizeof(C) == 2][SCHEME]) {
-    PFDTD_CK(cudaFuncSetAttribute(k_update_tma<S, C, SCHEME>,
+  static bool attr_done = false;  // one instantiation, one attribute (per process)
+  if (!attr_done) {
+    PFDTD_CK(cudaFuncSetAttribute(k_update_tma<S, C, SCHEME, Lay>,
                                   cudaFuncAttributeMaxDynamicSharedMemorySize, Lay::SMEM));
-    ts.attr_set[sizeof(S) == 8][sizeof(C) == 2][SCHEME] = true;
+    attr_done = true;
   }
   const int gx = (int)((d->X + kTX - 1) / kTX);
   const int gy = (int)((d->Y + Lay::TY - 1) / Lay::TY);
   // z-chunks: several per tile so that the grid fills the machine in whole
   // waves of (SMs x resident CTAs), each chunk at least 16 planes long.
-  const int64_t resident = (int64_t)d->sm_count * (sizeof(S) == 4 ? 2 : 1);
+  const int64_t per_sm = std::max<int64_t>(1, (228 * 1024) / (Lay::SMEM + 1024 + 8192));
+  const int64_t resident = (int64_t)d->sm_count * per_sm;
   const int64_t tiles = (int64_t)gx * gy;
   int64_t best_c = 1;
   double best = 1e30;
@@ -394,7 +403,7 @@ int launch_tma_t(pfdtd_domain* d, const void* cur, void* past, cudaStream_t s) {
   ClassTab<A> tab{(const A*)tb, (const A*)(tb + as * d->n_classes),
                   (const A*)(tb + 2 * as * d->n_classes),
                   (const uint32_t*)(tb + 3 * as * d->n_classes), d->n_classes};
-  k_update_tma<S, C, SCHEME><<<dim3(gx, gy, gz), Lay::THREADS, Lay::SMEM, s>>>(
+  k_update_tma<S, C, SCHEME, Lay><<<dim3(gx, gy, gz), Lay::THREADS, Lay::SMEM, s>>>(
       ts.halo[cur_i], ts.tile[1 - cur_i], ts.cls, (const S*)cur, (S*)past, tab, (int)d->X,
       (int)d->Y, d->XY, (int)(d->Z - 1), (int)zc, (A)d->params[1], d->d_err);
   count_launch();
@@ -402,19 +411,60 @@ int launch_tma_t(pfdtd_domain* d, const void* cur, void* past, cudaStream_t s) {
   return PFDTD_OK;
 }
 
-template <typename S>
-int launch_tma_s(pfdtd_domain* d, const void* cur, void* past, cudaStream_t s) {
+template <typename S, typename Lay8, typename Lay16>
+int launch_tma_l(pfdtd_domain* d, const void* cur, void* past, cudaStream_t s) {
   const bool centred = (d->class_scheme == PFDTD_SRL);
   if (d->cls_bytes == 1)
-    return centred ? launch_tma_t<S, uint8_t, 1>(d, cur, past, s)
-                   : launch_tma_t<S, uint8_t, 0>(d, cur, past, s);
-  return centred ? launch_tma_t<S, uint16_t, 1>(d, cur, past, s)
-                 : launch_tma_t<S, uint16_t, 0>(d, cur, past, s);
+    return centred ? launch_tma_t<S, uint8_t, 1, Lay8>(d, cur, past, s)
+                   : launch_tma_t<S, uint8_t, 0, Lay8>(d, cur, past, s);
+  return centred ? launch_tma_t<S, uint16_t, 1, Lay16>(d, cur, past, s)
+                 : launch_tma_t<S, uint16_t, 0, Lay16>(d, cur, past, s);
+}
+
+// Tile shapes built for FP32 (index = tile id): TX x TY nodes, stages, x halo
+// in the TMA box or read from global at the tile's x edges.
+#define PFDTD_F32_TILES(X)                                                             \
+  X(0, 64, 16, 8, true) X(1, 128, 8, 8, true) X(2, 32, 32, 8, true) X(3, 128, 16, 6, true)   \
+  X(4, 128, 4, 12, true) X(5, 128, 8, 8, false) X(6, 256, 4, 8, false)                        \
+  X(7, 256, 8, 6, false) X(8, 256, 2, 16, false)
+
+template <typename S>
+int launch_tma_s(pfdtd_domain* d, const void* cur, void* past, cudaStream_t s);
+
+// Automatic tile: the widest x extent (256, 128 or 64 nodes) that divides X,
+// so that no CTA holds a partly empty tile and TMA rows are as long as
+// possible (measured on the 512 x 384 x 256 room: 256 x 4 streams at 98% of
+// the copy bandwidth, 64 x 16 with an in-box halo at 74%).
+int auto_tile(const pfdtd_domain* d) {
+  if (d->X % 256 == 0) return 6;
+  if (d->X % 128 == 0) return 5;
+  return 0;
+}
+
+template <>
+int launch_tma_s<float>(pfdtd_domain* d, const void* cur, void* past, cudaStream_t s) {
+  switch (d->tma_tile < 0 ? auto_tile(d) : d->tma_tile) {
+#define PFDTD_CASE(id, tx, ty, ns, xh)                                                    \
+  case id:                                                                                \
+    return launch_tma_l<float, Layout<float, uint8_t, tx, ty, ns, xh>,                     \
+                        Layout<float, uint16_t, tx, ty, ns, xh>>(d, cur, past, s);
+    PFDTD_F32_TILES(PFDTD_CASE)
+#undef PFDTD_CASE
+  }
+  return fail(PFDTD_ERR_ARG, "unknown TMA tile shape");
+}
+
+template <>
+int launch_tma_s<double>(pfdtd_domain* d, const void* cur, void* past, cudaStream_t s) {
+  return launch_tma_l<double, Layout<double, uint8_t, 64, 8, 6>, Layout<double, uint16_t, 64, 8, 6>>(
+      d, cur, past, s);
 }
 
 }  // namespace
 
 // The TMA path needs 16-byte aligned rows for the fields and class ids.
+int tma_tile_count() { return 9; }
+
 bool tma_supported(const pfdtd_domain* d) {
   if (d->precision != PFDTD_F32 && d->precision != PFDTD_F64) return false;
   if ((d->X * (int64_t)d->esize) % 16 != 0) return false;

@@ -399,3 +399,29 @@ def test_tma_wrap_neighbours_on_outer_faces(gpu, O):
     for variant, (g, P) in out.items():
         assert np.array_equal(g, r), variant
         assert np.array_equal(P, rP), variant
+
+
+@pytest.mark.parametrize("tile", list(range(9)))
+@pytest.mark.parametrize("centred", [False, True])
+def test_tma_tile_shapes_bit_identical(gpu, O, tile, centred):
+    room = rooms.boxes_room((208, 52, 40), n_boxes=6, edge=(5, 16), n_materials=9, seed=14)
+    steps = 60
+    src = room.random_air_nodes(1, seed=3)
+    rec = room.random_air_nodes(4, seed=4)
+    pulse = rooms.gaussian_pulse(steps, 3.0)
+    with Domain(room.dims, "f32") as d:
+        d.set_voxels(room.bid, room.mat, centred=centred)
+        d.set_materials(room.admittance)
+        d.set_params()
+        d.set_scheme("centred" if centred else "forward")
+        d.set_kernel("tma")
+        L.call("pfdtd_set_tile", d.handle, tile)
+        d.set_sources(src, [1], pulse[None])
+        d.set_receivers(rec)
+        g, _, _ = d.run(steps)
+        P = d.download_field(L.FIELD_CURRENT)
+    pos, mat = O.encode_nodes(room.bid, room.mat, centred)
+    r, rP, _ = O.run(pos, mat, room.dims, room.admittance, default_params(), [room.flat(*src[0])],
+                     [1], pulse[None], [room.flat(*x) for x in rec], steps, scheme=2 if centred else 0)
+    assert_parity(g, r, "f32")
+    assert np.array_equal(P, rP)
