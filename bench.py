@@ -53,7 +53,7 @@ def parse():
     p.add_argument("--steps", type=int, default=3)
     p.add_argument("--warmup", type=int, default=3)
     p.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    p.add_argument("--precision", default="f32", choices=["f32", "f64"])
+    p.add_argument("--precision", default="f32", choices=["f32", "f64", "f16", "bf16"])
     p.add_argument("--fdtd-steps", type=int, default=FDTD_STEPS)
     p.add_argument("--dims", type=str, default=None, help="X,Y,Z override (testing)")
     p.add_argument("--no-cpu-baseline", action="store_true")
@@ -242,6 +242,7 @@ def main():
     updates_per_run = X * Y * (Z - 2) * S
     prec = a.precision
     samples = rooms.impulse(S)[None].astype(np.float64 if prec == "f64" else np.float32)
+    esize = {"f32": 4, "f64": 8, "f16": 2, "bf16": 2}[prec]
     d = Domain(dims, prec, device=local)
     d.set_voxels(room.bid, room.mat, centred=False)
     pos_host, mat_host = d.get_nodes()
@@ -250,7 +251,6 @@ def main():
     d.set_scheme("forward")
     d.set_sources([src], [1], samples)
     d.set_receivers(rec)
-    esize = 8 if prec == "f64" else 4
     stream = torch.cuda.ExternalStream(d.stream_ptr())
     d_out = torch.zeros(N_REC * S, dtype=torch.float64 if prec == "f64" else torch.float32,
                         device=f"cuda:{local}")
@@ -327,7 +327,7 @@ def main():
         e2e_s = float(t.item())
     e2e = {"value": updates_per_run * world / e2e_s, "unit": METRIC,
            "h2d_bytes_per_step": int(2 * room.n_nodes + samples.nbytes),
-           "d2h_bytes_per_step": int(N_REC * S * esize)}
+           "d2h_bytes_per_step": int(N_REC * S * (8 if prec == "f64" else 4))}
 
     if rank == 0:
         base = None
@@ -343,11 +343,12 @@ def main():
                                    f"leapfrog steps, SRL forward, {prec}",
                        "fdtd_steps_per_step": S, "nodes": X * Y * Z,
                        "parallelism": f"replicas x{world}",
-                       "l2": "inputs larger than L2 (fields 2 x 201 MB + 50 MB classes)"},
+                       "l2": f"inputs larger than L2 (fields 2 x {X * Y * Z * esize / 1e6:.0f} MB "
+                             f"+ {X * Y * Z / 1e6:.0f} MB class ids)"},
             "e2e": e2e,
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                          "frac": achieved / peak, "traffic": traffic,
-                         "kernel": "k_update_zmarch", "kernel_ms": kms,
+                         "kernel": "k_update_" + d.kernel(), "kernel_ms": kms,
                          "algorithmic_bytes_per_launch": algo_bytes,
                          "peak_kind": f"of {peak_kind}"},
             "clocks": clk.summary(),

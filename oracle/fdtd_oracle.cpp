@@ -101,6 +101,36 @@ bool material_index(unsigned m, T octave, bool quirk_mat, unsigned n_entries,
   return true;
 }
 
+// Field storage types.  FP16 uses the compiler's IEEE binary16 type (round to
+// nearest even on conversion); BF16 keeps the top 16 bits of a float, rounded
+// to nearest even.  Arithmetic happens in float for both.
+struct BF16 {
+  uint16_t v;
+};
+inline float to_float(float x) { return x; }
+inline double to_float(double x) { return x; }
+inline float to_float(_Float16 x) { return (float)x; }
+inline float to_float(BF16 x) {
+  uint32_t u = (uint32_t)x.v << 16;
+  float f;
+  std::memcpy(&f, &u, 4);
+  return f;
+}
+template <typename S> inline S from_float(float f);
+template <> inline float from_float<float>(float f) { return f; }
+template <> inline _Float16 from_float<_Float16>(float f) { return (_Float16)f; }
+template <> inline BF16 from_float<BF16>(float f) {
+  uint32_t u;
+  std::memcpy(&u, &f, 4);
+  if ((u & 0x7F800000u) == 0x7F800000u && (u & 0x7FFFFFu)) return BF16{(uint16_t)((u >> 16) | 0x40)};
+  u += 0x7FFFu + ((u >> 16) & 1u);
+  return BF16{(uint16_t)(u >> 16)};
+}
+template <typename S> struct Arith { typedef float type; };
+template <> struct Arith<double> { typedef double type; };
+template <typename S> inline S from_arith(typename Arith<S>::type v) { return from_float<S>(v); }
+template <> inline double from_arith<double>(double v) { return v; }
+
 struct RunDesc {
   int scheme;   // 0 forward (Bilbao), 1 centred (Kowalczyk)
   int quirks;   // bit0: forward material index m*20*octave; bit1: soft source overwrites
@@ -122,8 +152,8 @@ struct RunDesc {
 
 // One leapfrog update over z in [1, Z-2] writing into Pp.
 // Forward rule: kernels3d.cu:485-529.  Centred rule: kernels3d.cu:608-665.
-template <typename T>
-int update(const RunDesc& d, const T* P, T* Pp, const std::vector<T>& beta_tab,
+template <typename T, typename St>
+int update(const RunDesc& d, const St* P, St* Pp, const std::vector<T>& beta_tab,
            const std::vector<uint8_t>& valid) {
   const T* prm = (const T*)d.params;
   const T l = prm[0], l2 = prm[1];
@@ -135,13 +165,14 @@ int update(const RunDesc& d, const T* P, T* Pp, const std::vector<T>& beta_tab,
       const unsigned pos = d.pos[c];
       const unsigned key = (pos << 8) | d.mat[c];
       const T beta = beta_tab[key];
-      const T p = P[c];
-      const T pp = Pp[c];
+      const T p = to_float(P[c]);
+      const T pp = to_float(Pp[c]);
       T ret;
       if (d.scheme == 0) {
         const T position = (T)(pos & kForwardMask);
         const T sw = (T)(pos >> kInsideSwitch);
-        const T S = P[c + XY] + P[c - XY] + P[c + X] + P[c - X] + P[c + 1] + P[c - 1];
+        const T S = (T)to_float(P[c + XY]) + (T)to_float(P[c - XY]) + (T)to_float(P[c + X]) +
+                    (T)to_float(P[c - X]) + (T)to_float(P[c + 1]) + (T)to_float(P[c - 1]);
         ret = sw * ((T)1 / ((T)1 + beta)) *
               (((T)2 - position * l2) * p + l2 * S - ((T)1 - beta) * pp);
       } else {
@@ -149,12 +180,12 @@ int update(const RunDesc& d, const T* P, T* Pp, const std::vector<T>& beta_tab,
         const T dx = (T)(pos & kDirX), dy = (T)((pos & kDirY) >> 1),
                 dz = (T)((pos & kDirZ) >> 2);
         T pz[2], py[2], px[2];
-        pz[1] = P[c - XY];
-        pz[0] = P[c + XY];
-        py[0] = P[c - X];
-        py[1] = P[c + X];
-        px[0] = P[c - 1];
-        px[1] = P[c + 1];
+        pz[1] = to_float(P[c - XY]);
+        pz[0] = to_float(P[c + XY]);
+        py[0] = to_float(P[c - X]);
+        py[1] = to_float(P[c + X]);
+        px[0] = to_float(P[c - 1]);
+        px[1] = to_float(P[c + 1]);
         const int sx = (pos & kSignX) >> 4, sy = (pos & kSignY) >> 5,
                   sz = (pos & kSignZ) >> 6;
         const T Sb = px[sx] * dx + py[sy] * dy + pz[sz] * dz;
@@ -162,7 +193,7 @@ int update(const RunDesc& d, const T* P, T* Pp, const std::vector<T>& beta_tab,
         ret = (S - ((T)2 - (T)6 * l2) * p + (beta - (T)1) * pp) * sw *
               ((T)1 / ((T)1 + beta));
       }
-      Pp[c] = ret;
+      Pp[c] = from_arith<St>(ret);
     }
   }
   return 0;
@@ -205,8 +236,8 @@ int beta_table(const RunDesc& d, std::vector<T>& beta, std::vector<uint8_t>& val
 // Step loop of launchFDTD3d / launchFDTD3dDouble (kernels3d.cu:83-181):
 // inject sources into P (:93-104), update (:109-153), swap (:160),
 // record receivers from the new P (:164-173).
-template <typename T>
-int run(const RunDesc& d, T* P, T* Pp, T* out) {
+template <typename T, typename S>
+int run(const RunDesc& d, S* P, S* Pp, T* out) {
   if (d.X < 1 || d.Y < 1 || d.Z < 3) return -1;
   std::vector<T> beta;
   std::vector<uint8_t> valid;
@@ -220,24 +251,24 @@ int run(const RunDesc& d, T* P, T* Pp, T* out) {
       if (idx < 0 || idx >= N) continue;
       const T v = samples[(int64_t)i * d.steps + step];
       if (d.src_type[i] == 0 || (d.quirks & 2))
-        P[idx] = v;      // setSample, cudaMesh.h:322-338 (and Q4 addSample)
+        P[idx] = from_arith<S>(v);  // setSample, cudaMesh.h:322-338 (and Q4 addSample)
       else
-        P[idx] = P[idx] + v;  // intended addSample, cudaMesh.h:349-369
+        P[idx] = from_arith<S>((T)to_float(P[idx]) + v);  // addSample, cudaMesh.h:349-369
     }
-    update<T>(d, P, Pp, beta, valid);
-    T* t = P; P = Pp; Pp = t;
+    update<T, S>(d, P, Pp, beta, valid);
+    S* t = P; P = Pp; Pp = t;
     for (int r = 0; r < d.n_rec; ++r) {
       const int64_t idx = d.rec_idx[r];
       if (idx < 0 || idx >= N) continue;
-      out[(int64_t)r * d.steps + step] = P[idx];
+      out[(int64_t)r * d.steps + step] = to_float(P[idx]);
     }
   }
   // Leave the caller's first buffer holding the current field: after an odd
   // number of swaps the roles of the two buffers are exchanged.
   if ((d.steps & 1) != 0) {
-    std::vector<T> cur_copy(P, P + N);      // P is the caller's second buffer
-    std::memcpy(P, Pp, sizeof(T) * N);
-    std::memcpy(Pp, cur_copy.data(), sizeof(T) * N);
+    std::vector<S> cur_copy(P, P + N);      // P is the caller's second buffer
+    std::memcpy(P, Pp, sizeof(S) * N);
+    std::memcpy(Pp, cur_copy.data(), sizeof(S) * N);
   }
   return 0;
 }
@@ -387,7 +418,8 @@ double oracle_source_sample_f64(int src_type, int input_type, uint32_t step, uin
   return sample;
 }
 
-// Full run (kernels3d.cu:31-203 float, :205-374 double).  P and Pp hold the
+// Full run (kernels3d.cu:31-203 float, :205-374 double; precision 2 and 3
+// store the fields in FP16 / BF16 with float arithmetic).  P and Pp hold the
 // initial (current, past) fields and receive the final ones; out receives
 // [n_rec * steps] receiver samples, row per receiver (kernels3d.cu:183-191).
 // Returns 0, or -1 bad dims, -3 material index out of the table.
@@ -399,9 +431,12 @@ int oracle_run(int precision, int scheme, int quirks, int64_t X, int64_t Y, int6
                int threads) {
   RunDesc d{scheme, quirks, X, Y, Z, pos, mat, table, n_mat, params, n_src, src_idx,
             src_type, src_samples, n_rec, rec_idx, steps, threads > 0 ? threads : 1};
-  if (precision == 1)
-    return run<double>(d, (double*)P, (double*)Pp, (double*)out);
-  return run<float>(d, (float*)P, (float*)Pp, (float*)out);
+  switch (precision) {
+    case 1: return run<double, double>(d, (double*)P, (double*)Pp, (double*)out);
+    case 2: return run<float, _Float16>(d, (_Float16*)P, (_Float16*)Pp, (float*)out);
+    case 3: return run<float, BF16>(d, (BF16*)P, (BF16*)Pp, (float*)out);
+  }
+  return run<float, float>(d, (float*)P, (float*)Pp, (float*)out);
 }
 
 int oracle_max_threads(void) {

@@ -100,10 +100,15 @@ def run(pos: np.ndarray, mat: np.ndarray, dims: Sequence[int], table: np.ndarray
         params: Sequence[float], src_idx: Sequence[int], src_type: Sequence[int],
         samples: np.ndarray, rec_idx: Sequence[int], steps: int, scheme: int = 0,
         quirks: int = 0, double: bool = False, threads: int = 0,
-        P0: Optional[np.ndarray] = None, Pp0: Optional[np.ndarray] = None):
-    """Oracle step loop.  Returns (receivers [n_rec, steps], P, P_past)."""
+        P0: Optional[np.ndarray] = None, Pp0: Optional[np.ndarray] = None,
+        storage: Optional[str] = None):
+    """Oracle step loop.  Returns (receivers [n_rec, steps], P, P_past).
+    storage: None (FP32, or FP64 with double=True), "f16" or "bf16" (16-bit
+    fields with float arithmetic; fields returned as float16 / uint16)."""
     lib = load()
     dt = np.float64 if double else np.float32
+    prec = 1 if double else {None: 0, "f32": 0, "f16": 2, "bf16": 3}[storage]
+    st_dt = {0: np.float32, 1: np.float64, 2: np.float16, 3: np.uint16}[prec]
     X, Y, Z = (int(v) for v in dims)
     N = X * Y * Z
     pos = np.ascontiguousarray(pos, dtype=np.uint8).reshape(-1)
@@ -115,12 +120,12 @@ def run(pos: np.ndarray, mat: np.ndarray, dims: Sequence[int], table: np.ndarray
     st = np.ascontiguousarray(src_type, dtype=np.int32).reshape(-1)
     sm = np.ascontiguousarray(samples, dtype=dt).reshape(si.size, -1) if si.size else np.zeros((0, steps), dt)
     ri = np.ascontiguousarray(rec_idx, dtype=np.int64).reshape(-1)
-    P = np.zeros(N, dtype=dt) if P0 is None else np.array(P0, dtype=dt, copy=True)
-    Pp = np.zeros(N, dtype=dt) if Pp0 is None else np.array(Pp0, dtype=dt, copy=True)
+    P = np.zeros(N, dtype=st_dt) if P0 is None else np.array(P0, dtype=st_dt, copy=True)
+    Pp = np.zeros(N, dtype=st_dt) if Pp0 is None else np.array(Pp0, dtype=st_dt, copy=True)
     out = np.zeros((ri.size, steps), dtype=dt)
     if threads <= 0:
         threads = lib.oracle_max_threads()
-    rc = lib.oracle_run(1 if double else 0, scheme, quirks, X, Y, Z, _p(pos), _p(mat), _p(tab),
+    rc = lib.oracle_run(prec, scheme, quirks, X, Y, Z, _p(pos), _p(mat), _p(tab),
                         n_mat, _p(prm), si.size, _p(si), _p(st), _p(sm), ri.size, _p(ri),
                         steps, _p(P), _p(Pp), _p(out), threads)
     if rc != 0:

@@ -133,6 +133,26 @@ __device__ __forceinline__ V4<double> lds4(const double* p) {
   const double2 b = reinterpret_cast<const double2*>(p)[1];
   return V4<double>{{a.x, a.y, b.x, b.y}};
 }
+template <typename H2, typename S>
+__device__ __forceinline__ V4<S> lds4_16(const S* p) {
+  const uint2 t = *reinterpret_cast<const uint2*>(p);
+  H2 a, b;
+  memcpy(&a, &t.x, 4);
+  memcpy(&b, &t.y, 4);
+  return V4<S>{{a.x, a.y, b.x, b.y}};
+}
+__device__ __forceinline__ V4<__half> lds4(const __half* p) { return lds4_16<__half2>(p); }
+__device__ __forceinline__ V4<__nv_bfloat16> lds4(const __nv_bfloat16* p) {
+  return lds4_16<__nv_bfloat162>(p);
+}
+template <typename S>
+__device__ __forceinline__ void stg4_16(S* p, const S (&v)[4]) {
+  uint16_t u[4];
+  memcpy(u, v, 8);
+  *reinterpret_cast<uint2*>(p) = make_uint2(u[0] | ((uint32_t)u[1] << 16), u[2] | ((uint32_t)u[3] << 16));
+}
+__device__ __forceinline__ void stg4(__half* p, const __half (&v)[4]) { stg4_16(p, v); }
+__device__ __forceinline__ void stg4(__nv_bfloat16* p, const __nv_bfloat16 (&v)[4]) { stg4_16(p, v); }
 __device__ __forceinline__ void stg4(float* p, const float (&v)[4]) {
   *reinterpret_cast<float4*>(p) = make_float4(v[0], v[1], v[2], v[3]);
 }
@@ -311,6 +331,12 @@ k_update_tma(const __grid_constant__ CUtensorMap map_cur, const __grid_constant_
   }
 }
 
+template <typename S> struct TmaType;
+template <> struct TmaType<float> { static constexpr CUtensorMapDataType value = CU_TENSOR_MAP_DATA_TYPE_FLOAT32; };
+template <> struct TmaType<double> { static constexpr CUtensorMapDataType value = CU_TENSOR_MAP_DATA_TYPE_FLOAT64; };
+template <> struct TmaType<__half> { static constexpr CUtensorMapDataType value = CU_TENSOR_MAP_DATA_TYPE_FLOAT16; };
+template <> struct TmaType<__nv_bfloat16> { static constexpr CUtensorMapDataType value = CU_TENSOR_MAP_DATA_TYPE_BFLOAT16; };
+
 typedef CUresult (*EncodeTiledFn)(CUtensorMap*, CUtensorMapDataType, cuuint32_t, void*,
                                   const cuuint64_t*, const cuuint64_t*, const cuuint32_t*,
                                   const cuuint32_t*, CUtensorMapInterleave, CUtensorMapSwizzle,
@@ -358,8 +384,7 @@ int launch_tma_t(pfdtd_domain* d, const void* cur, void* past, cudaStream_t s) {
   const int64_t key[4] = {(int64_t)(intptr_t)d->d_cls, d->cls_bytes, d->precision,
                           (int64_t)Lay::TX * 10000 + Lay::TY * 10 + (Lay::XHALO ? 1 : 0)};
   if (!ts.ready || std::memcmp(key, ts.key, sizeof(key)) != 0) {
-    const CUtensorMapDataType dt =
-        sizeof(S) == 8 ? CU_TENSOR_MAP_DATA_TYPE_FLOAT64 : CU_TENSOR_MAP_DATA_TYPE_FLOAT32;
+    const CUtensorMapDataType dt = TmaType<S>::value;
     const CUtensorMapDataType ct =
         sizeof(C) == 1 ? CU_TENSOR_MAP_DATA_TYPE_UINT8 : CU_TENSOR_MAP_DATA_TYPE_UINT16;
     const int64_t rows = d->Y * d->Z;
@@ -454,6 +479,39 @@ int launch_tma_s<float>(pfdtd_domain* d, const void* cur, void* past, cudaStream
   return fail(PFDTD_ERR_ARG, "unknown TMA tile shape");
 }
 
+// 16-bit storage tiles: 0 64x16 (halo in box), 1 128x8, 2 256x8, 3 256x4.
+#define PFDTD_F16_TILES(X) \
+  X(0, 64, 16, 8, true) X(1, 128, 8, 8, false) X(2, 256, 8, 8, false) X(3, 256, 4, 8, false)
+
+int auto_tile16(const pfdtd_domain* d) {
+  if (d->X % 256 == 0) return 2;
+  if (d->X % 128 == 0) return 1;
+  return 0;
+}
+
+template <typename S>
+int launch_tma_16(pfdtd_domain* d, const void* cur, void* past, cudaStream_t s) {
+  switch (d->tma_tile < 0 ? auto_tile16(d) : d->tma_tile) {
+#define PFDTD_CASE16(id, tx, ty, ns, xh)                                                  \
+  case id:                                                                                \
+    return launch_tma_l<S, Layout<S, uint8_t, tx, ty, ns, xh>,                             \
+                        Layout<S, uint16_t, tx, ty, ns, xh>>(d, cur, past, s);
+    PFDTD_F16_TILES(PFDTD_CASE16)
+#undef PFDTD_CASE16
+  }
+  return fail(PFDTD_ERR_ARG, "unknown TMA tile shape for 16-bit fields (0..3)");
+}
+
+template <>
+int launch_tma_s<__half>(pfdtd_domain* d, const void* cur, void* past, cudaStream_t s) {
+  return launch_tma_16<__half>(d, cur, past, s);
+}
+
+template <>
+int launch_tma_s<__nv_bfloat16>(pfdtd_domain* d, const void* cur, void* past, cudaStream_t s) {
+  return launch_tma_16<__nv_bfloat16>(d, cur, past, s);
+}
+
 template <>
 int launch_tma_s<double>(pfdtd_domain* d, const void* cur, void* past, cudaStream_t s) {
   return launch_tma_l<double, Layout<double, uint8_t, 64, 8, 6>, Layout<double, uint16_t, 64, 8, 6>>(
@@ -466,7 +524,6 @@ int launch_tma_s<double>(pfdtd_domain* d, const void* cur, void* past, cudaStrea
 int tma_tile_count() { return 9; }
 
 bool tma_supported(const pfdtd_domain* d) {
-  if (d->precision != PFDTD_F32 && d->precision != PFDTD_F64) return false;
   if ((d->X * (int64_t)d->esize) % 16 != 0) return false;
   if ((d->X * (int64_t)d->cls_bytes) % 16 != 0) return false;
   if (d->Y * d->Z >= ((int64_t)1 << 31)) return false;
@@ -474,9 +531,13 @@ bool tma_supported(const pfdtd_domain* d) {
 }
 
 int launch_update_tma(pfdtd_domain* d, const void* cur, void* past, cudaStream_t s) {
-  if (d->precision == PFDTD_F32) return launch_tma_s<float>(d, cur, past, s);
-  if (d->precision == PFDTD_F64) return launch_tma_s<double>(d, cur, past, s);
-  return fail(PFDTD_ERR_UNSUPPORTED, "TMA update needs FP32 or FP64 fields");
+  switch (d->precision) {
+    case PFDTD_F32: return launch_tma_s<float>(d, cur, past, s);
+    case PFDTD_F64: return launch_tma_s<double>(d, cur, past, s);
+    case PFDTD_F16: return launch_tma_s<__half>(d, cur, past, s);
+    case PFDTD_BF16: return launch_tma_s<__nv_bfloat16>(d, cur, past, s);
+  }
+  return fail(PFDTD_ERR_UNSUPPORTED, "unknown precision");
 }
 
 }  // namespace pfdtd

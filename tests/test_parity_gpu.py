@@ -425,3 +425,37 @@ def test_tma_tile_shapes_bit_identical(gpu, O, tile, centred):
                      [1], pulse[None], [room.flat(*x) for x in rec], steps, scheme=2 if centred else 0)
     assert_parity(g, r, "f32")
     assert np.array_equal(P, rP)
+
+
+@pytest.mark.parametrize("variant", ["zmarch", "tma"])
+@pytest.mark.parametrize("prec", ["f16", "bf16"])
+@pytest.mark.parametrize("centred", [False, True])
+def test_16bit_storage_bit_identical(gpu, O, variant, prec, centred):
+    """FP16 / BF16 field storage with FP32 arithmetic: bit-identical to the
+    oracle that rounds its stored fields the same way; the error against the
+    FP64 oracle is bounded (FP16 <= 1e-2, BF16 <= 1e-1 relative L2 here)."""
+    room = rooms.boxes_room((256, 48, 40), n_boxes=6, edge=(5, 16), n_materials=9, seed=15)
+    steps = 150
+    src = room.random_air_nodes(1, seed=3)
+    rec = room.random_air_nodes(4, seed=4)
+    pulse = rooms.gaussian_pulse(steps, 4.0)
+    with Domain(room.dims, prec) as d:
+        d.set_voxels(room.bid, room.mat, centred=centred)
+        d.set_materials(room.admittance)
+        d.set_params()
+        d.set_scheme("centred" if centred else "forward")
+        d.set_kernel(variant)
+        d.set_sources(src, [1], pulse[None])
+        d.set_receivers(rec)
+        g, _, _ = d.run(steps)
+        assert d.kernel() == variant
+        P = d.download_field(L.FIELD_CURRENT)
+    pos, mat = O.encode_nodes(room.bid, room.mat, centred)
+    args = (pos, mat, room.dims, room.admittance, default_params(), [room.flat(*src[0])], [1],
+            pulse[None], [room.flat(*x) for x in rec], steps)
+    r, rP, _ = O.run(*args, scheme=2 if centred else 0, storage=prec)
+    assert np.array_equal(g, r)
+    assert np.array_equal(P.view(np.uint16), rP.view(np.uint16))
+    d64, _, _ = O.run(*args, scheme=2 if centred else 0, double=True)
+    err = rel_l2(g, d64)
+    assert err < (1e-2 if prec == "f16" else 1e-1), err
