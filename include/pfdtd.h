@@ -56,6 +56,11 @@ extern "C" {
 #define PFDTD_SRL_FORWARD 0
 #define PFDTD_SHARED 1
 #define PFDTD_SRL 2
+/* IWB 27-point compact scheme at lambda = 1, (a, b) = (1/4, 1/16); no
+ * counterpart in the reference.  Uses the centred node encoding; boundary
+ * nodes reflect their outward neighbours and lose beta = lambda * Y * (number
+ * of boundary axes).  Needs the parameter vector [1, 1, 1/3, octave]. */
+#define PFDTD_IWB 3
 
 /* Source types (src/base/SrcRec.h:33). */
 #define PFDTD_SRC_HARD 0
@@ -136,7 +141,7 @@ int pfdtd_set_sources(pfdtd_domain* d, int n, const int64_t* xyz, const int32_t*
  * (kernels3d.cu:66-78, :164-173). */
 int pfdtd_set_receivers(pfdtd_domain* d, int n, const int64_t* xyz);
 
-/* Update scheme used by the next run/step (PFDTD_SRL_FORWARD, _SHARED, _SRL). */
+/* Update scheme used by the next run/step (PFDTD_SRL_FORWARD, _SHARED, _SRL, _IWB). */
 int pfdtd_set_scheme(pfdtd_domain* d, int scheme);
 
 /* Run `steps` leapfrog steps from step index 0 (launchFDTD3d,

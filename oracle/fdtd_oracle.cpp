@@ -132,7 +132,7 @@ template <typename S> inline S from_arith(typename Arith<S>::type v) { return fr
 template <> inline double from_arith<double>(double v) { return v; }
 
 struct RunDesc {
-  int scheme;   // 0 forward (Bilbao), 1 centred (Kowalczyk)
+  int scheme;   // 0 forward (Bilbao), 1 centred (Kowalczyk), 3 IWB (centred encoding)
   int quirks;   // bit0: forward material index m*20*octave; bit1: soft source overwrites
   int64_t X, Y, Z;
   const uint8_t* pos;
@@ -149,6 +149,50 @@ struct RunDesc {
   int64_t steps;
   int threads;
 };
+
+// IWB 27-point compact scheme (no counterpart in the reference; the
+// reference's UpdateType has SRL schemes only, SimulationParameters.h:39).
+//
+// Interior: p+ = d1*S1 + d2*S2 + d3*S3 + d4*p - p-, with S1/S2/S3 the sums of
+// the 6 face, 12 edge and 8 corner neighbours and (lambda, a, b) = (1, 1/4,
+// 1/16): d1 = 1/4, d2 = 1/8, d3 = 1/16, d4 = -3/2 (Kowalczyk & van Walstijn,
+// IEEE TASLP 19(1), 2011).
+// Boundary (centred node encoding, cudaMesh.h:35-44): along each boundary
+// axis the neighbour offsets that point out of the room (toward the missing
+// side: -1 when SIGN is set, +1 otherwise) are reflected to the opposite
+// side, and the locally reacting admittance Y adds the loss term
+// beta = lambda * Y * (number of boundary axes):
+//   p+ = s * (d1*S1' + d2*S2' + d3*S3' + d4*p - (1 - beta)*p-) / (1 + beta).
+// Canonical evaluation order (shared with the CUDA kernel): offsets visited
+// for dz, dy, dx in -1, 0, 1 (skipping the centre), each added to its class
+// sum in that order; then ((S1*d1 + S2*d2) + S3*d3 + d4*p) - c*p-, times a.
+template <typename T, typename St>
+T iwb_node(const St* P, int64_t N, int64_t c, int64_t X, int64_t XY, unsigned pos, T pp, T a,
+           T cc) {
+  const int dirx = pos & 0x01, diry = (pos >> 1) & 1, dirz = (pos >> 2) & 1;
+  const int ox = (pos & 0x10) ? -1 : 1, oy = (pos & 0x20) ? -1 : 1, oz = (pos & 0x40) ? -1 : 1;
+  T s1 = 0, s2 = 0, s3 = 0;
+  bool f1 = true, f2 = true, f3 = true;
+  for (int dz = -1; dz <= 1; ++dz)
+    for (int dy = -1; dy <= 1; ++dy)
+      for (int dx = -1; dx <= 1; ++dx) {
+        const int n = (dx != 0) + (dy != 0) + (dz != 0);
+        if (n == 0) continue;
+        const int mx = (dirx && dx == ox) ? -dx : dx;
+        const int my = (diry && dy == oy) ? -dy : dy;
+        const int mz = (dirz && dz == oz) ? -dz : dz;
+        // Flat neighbours outside the grid read 0, as the zeroed margins
+        // around the device fields do.
+        const int64_t i = c + mz * XY + my * X + mx;
+        const T v = (i >= 0 && i < N) ? (T)to_float(P[i]) : (T)0;
+        if (n == 1) { s1 = f1 ? v : s1 + v; f1 = false; }
+        else if (n == 2) { s2 = f2 ? v : s2 + v; f2 = false; }
+        else { s3 = f3 ? v : s3 + v; f3 = false; }
+      }
+  const T p = (T)to_float(P[c]);
+  const T sw = s1 * (T)0.25 + s2 * (T)0.125 + s3 * (T)0.0625;
+  return a * ((sw + (T)(-1.5) * p) - cc * pp);
+}
 
 // One leapfrog update over z in [1, Z-2] writing into Pp.
 // Forward rule: kernels3d.cu:485-529.  Centred rule: kernels3d.cu:608-665.
@@ -168,7 +212,11 @@ int update(const RunDesc& d, const St* P, St* Pp, const std::vector<T>& beta_tab
       const T p = to_float(P[c]);
       const T pp = to_float(Pp[c]);
       T ret;
-      if (d.scheme == 0) {
+      if (d.scheme == 3) {
+        const T sw = (T)(pos >> kInsideSwitch);
+        ret = iwb_node<T, St>(P, XY * Z, c, X, XY, pos, pp, sw * ((T)1 / ((T)1 + beta)),
+                              (T)1 - beta);
+      } else if (d.scheme == 0) {
         const T position = (T)(pos & kForwardMask);
         const T sw = (T)(pos >> kInsideSwitch);
         const T S = (T)to_float(P[c + XY]) + (T)to_float(P[c - XY]) + (T)to_float(P[c + X]) +
@@ -223,6 +271,9 @@ int beta_table(const RunDesc& d, std::vector<T>& beta, std::vector<uint8_t>& val
     if (d.scheme == 0) {
       const T position = (T)(pos & kForwardMask);
       beta[key] = (T)0.5 * (Y * ((T)6 - position) * prm[0]);
+    } else if (d.scheme == 3) {
+      const T ndirs = (T)((pos & 1u) + ((pos >> 1) & 1u) + ((pos >> 2) & 1u));
+      beta[key] = Y * prm[0] * ndirs;
     } else {
       const T dx = (T)(pos & kDirX), dy = (T)((pos & kDirY) >> 1),
               dz = (T)((pos & kDirZ) >> 2);

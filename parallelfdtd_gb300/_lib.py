@@ -26,7 +26,7 @@ ERR_STATE = -5
 ERR_UNSUPPORTED = -6
 
 F32, F64, F16, BF16 = 0, 1, 2, 3
-SRL_FORWARD, SHARED, SRL = 0, 1, 2
+SRL_FORWARD, SHARED, SRL, IWB = 0, 1, 2, 3
 SRC_HARD, SRC_SOFT, SRC_TRANSPARENT = 0, 1, 2
 QUIRK_MATIDX, QUIRK_SOFTSRC = 1, 2
 FIELD_CURRENT, FIELD_PAST = 0, 1

@@ -35,7 +35,7 @@ int eval(int scheme, int quirks, const double* params, const std::vector<double>
     // (kernels3d.cu:513, reproduced under PFDTD_QUIRK_MATIDX), otherwise
     // m*20 + octave as the centred kernel computes it (kernels3d.cu:639).
     unsigned mi;
-    if (scheme != PFDTD_SRL && (quirks & PFDTD_QUIRK_MATIDX))
+    if (scheme == PFDTD_SRL_FORWARD && (quirks & PFDTD_QUIRK_MATIDX))
       mi = (unsigned)((A)(m * 20u) * octave);
     else
       mi = (unsigned)((A)(m * 20u) + octave);
@@ -47,7 +47,14 @@ int eval(int scheme, int quirks, const double* params, const std::vector<double>
                       " entries");
     const A Y = (A)materials[mi];
     const A sw = (A)(pos >> 7);
-    if (scheme != PFDTD_SRL) {
+    if (scheme == PFDTD_IWB) {
+      // IWB boundary update (see the kernel): beta = lambda * Y * (boundary axes)
+      const A ndirs = (A)((pos & 0x01u) + ((pos >> 1) & 1u) + ((pos >> 2) & 1u));
+      const A beta = Y * l * ndirs;
+      ca[i] = sw * ((A)1 / ((A)1 + beta));
+      cb[i] = (A)(-1.5);
+      cc[i] = (A)1 - beta;
+    } else if (scheme != PFDTD_SRL) {
       // kernels3d.cu:509-526
       const A position = (A)(pos & 0x7Fu);
       const A beta = (A)0.5 * (Y * ((A)6 - position) * l);

@@ -380,10 +380,12 @@ int pfdtd_set_quirks(pfdtd_domain* d, int quirks) {
 
 int pfdtd_set_scheme(pfdtd_domain* d, int scheme) {
   if (int rc = check_domain(d)) return rc;
-  if (scheme != PFDTD_SRL_FORWARD && scheme != PFDTD_SHARED && scheme != PFDTD_SRL)
+  if (scheme != PFDTD_SRL_FORWARD && scheme != PFDTD_SHARED && scheme != PFDTD_SRL &&
+      scheme != PFDTD_IWB)
     return fail(PFDTD_ERR_UNSUPPORTED, "unknown update scheme");
-  const int eff_old = d->scheme == PFDTD_SRL ? PFDTD_SRL : PFDTD_SRL_FORWARD;
-  const int eff_new = scheme == PFDTD_SRL ? PFDTD_SRL : PFDTD_SRL_FORWARD;
+  auto eff = [](int sc) { return sc == PFDTD_SHARED ? PFDTD_SRL_FORWARD : sc; };
+  const int eff_old = eff(d->scheme);
+  const int eff_new = eff(scheme);
   if (eff_old != eff_new) d->classes_dirty = true;
   d->scheme = scheme;
   return PFDTD_OK;

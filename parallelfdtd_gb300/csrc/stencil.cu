@@ -93,6 +93,108 @@ k_update_zmarch(const C* __restrict__ cls, const S* __restrict__ P, S* __restric
   }
 }
 
+// IWB 27-point update (no counterpart in the reference).  One thread per
+// (x, y) column marching z; the 3 x 3 neighbourhood of planes z-1, z and z+1
+// stays in registers and each step reads the 3 x 3 block of plane z+1 through
+// the read-only cache.  Boundary nodes (DIR bits) replace the outward
+// column/row/plane of their neighbourhood by the inward one, one axis after
+// the other (x, y, z), which reflects every outward offset.  Sums follow the
+// canonical order of the oracle: offsets for dz, dy, dx in -1, 0, 1 into the
+// face, edge and corner sums.
+template <typename S, typename C>
+__global__ void __launch_bounds__(kBX * kBY)
+k_update_iwb(const C* __restrict__ cls, const S* __restrict__ P, S* __restrict__ Pp,
+             ClassTab<typename Store<S>::A> tab, int X, int Y, int64_t XY, int z_last, int zc) {
+  using A = typename Store<S>::A;
+  using R = Rn<A>;
+  using St = Store<S>;
+  const int x = blockIdx.x * kBX + threadIdx.x;
+  const int y = blockIdx.y * kBY + threadIdx.y;
+  const int z0 = 1 + blockIdx.z * zc;
+  const int z1 = min(z0 + zc, z_last);
+  if (x >= X || y >= Y || z0 >= z1) return;
+  // v[plane][dy+1][dx+1]: plane 0 = z-1, 1 = z, 2 = z+1
+  A v[3][3][3];
+  auto load_plane = [&](int slot, int64_t base) {
+#pragma unroll
+    for (int dy = -1; dy <= 1; ++dy)
+#pragma unroll
+      for (int dx = -1; dx <= 1; ++dx)
+        v[slot][dy + 1][dx + 1] = St::load(__ldg(P + base + (int64_t)dy * X + dx));
+  };
+  int64_t idx = (int64_t)z0 * XY + (int64_t)y * X + x;
+  load_plane(0, idx - XY);
+  load_plane(1, idx);
+  for (int z = z0; z < z1; ++z, idx += XY) {
+    load_plane(2, idx + XY);
+    const unsigned c = cls[idx];
+    const A pp = St::load(Pp[idx]);
+    const A ca = __ldg(tab.a + c), cb = __ldg(tab.b + c), cc = __ldg(tab.c + c);
+    const uint32_t cp = __ldg(tab.pos + c);
+    A m[3][3][3];
+#pragma unroll
+    for (int a = 0; a < 3; ++a)
+#pragma unroll
+      for (int b = 0; b < 3; ++b)
+#pragma unroll
+        for (int e = 0; e < 3; ++e) m[a][b][e] = v[a][b][e];
+    if (cp & 0x07u) {
+      if (cp & 0x01u) {  // x: outward is -1 with SIGN_X, +1 without
+        const bool neg = cp & 0x10u;
+#pragma unroll
+        for (int a = 0; a < 3; ++a)
+#pragma unroll
+          for (int b = 0; b < 3; ++b) {
+            if (neg) m[a][b][0] = m[a][b][2]; else m[a][b][2] = m[a][b][0];
+          }
+      }
+      if (cp & 0x02u) {
+        const bool neg = cp & 0x20u;
+#pragma unroll
+        for (int a = 0; a < 3; ++a)
+#pragma unroll
+          for (int e = 0; e < 3; ++e) {
+            if (neg) m[a][0][e] = m[a][2][e]; else m[a][2][e] = m[a][0][e];
+          }
+      }
+      if (cp & 0x04u) {
+        const bool neg = cp & 0x40u;
+#pragma unroll
+        for (int b = 0; b < 3; ++b)
+#pragma unroll
+          for (int e = 0; e < 3; ++e) {
+            if (neg) m[0][b][e] = m[2][b][e]; else m[2][b][e] = m[0][b][e];
+          }
+      }
+    }
+    A s1 = (A)0, s2 = (A)0, s3 = (A)0;
+    bool f1 = true, f2 = true, f3 = true;
+#pragma unroll
+    for (int a = 0; a < 3; ++a)
+#pragma unroll
+      for (int b = 0; b < 3; ++b)
+#pragma unroll
+        for (int e = 0; e < 3; ++e) {
+          const int n = (a != 1) + (b != 1) + (e != 1);
+          if (n == 0) continue;
+          const A w = m[a][b][e];
+          if (n == 1) { s1 = f1 ? w : R::add(s1, w); f1 = false; }
+          else if (n == 2) { s2 = f2 ? w : R::add(s2, w); f2 = false; }
+          else { s3 = f3 ? w : R::add(s3, w); f3 = false; }
+        }
+    const A sw = R::add(R::add(R::mul(s1, (A)0.25), R::mul(s2, (A)0.125)), R::mul(s3, (A)0.0625));
+    const A out = R::mul(ca, R::sub(R::add(sw, R::mul(cb, v[1][1][1])), R::mul(cc, pp)));
+    Pp[idx] = St::store(out);
+#pragma unroll
+    for (int b = 0; b < 3; ++b)
+#pragma unroll
+      for (int e = 0; e < 3; ++e) {
+        v[0][b][e] = v[1][b][e];
+        v[1][b][e] = v[2][b][e];
+      }
+  }
+}
+
 // Between two updates: record receivers from the current field for the step
 // just finished (kernels3d.cu:164-173), then inject this step's source
 // samples into the current field in source order (kernels3d.cu:93-104).
@@ -171,8 +273,35 @@ int launch_update_t(pfdtd_domain* d, const void* cur, void* past, cudaStream_t s
   return PFDTD_OK;
 }
 
+template <typename S, typename C>
+int launch_iwb_t(pfdtd_domain* d, const void* cur, void* past, cudaStream_t s) {
+  using A = typename Store<S>::A;
+  const int64_t nz = d->Z - 2;
+  if (nz <= 0) return PFDTD_OK;
+  const int gx = (int)((d->X + kBX - 1) / kBX);
+  const int gy = (int)((d->Y + kBY - 1) / kBY);
+  const int64_t target = (int64_t)d->sm_count * 8 * 4;
+  int64_t zc = std::max<int64_t>(8, (nz * (int64_t)gx * gy + target - 1) / target);
+  zc = std::min<int64_t>(zc, nz);
+  const int gz = (int)((nz + zc - 1) / zc);
+  const size_t as = sizeof(A);
+  const char* tb = (const char*)d->d_ctab;
+  ClassTab<A> tab{(const A*)tb, (const A*)(tb + as * d->n_classes),
+                  (const A*)(tb + 2 * as * d->n_classes),
+                  (const uint32_t*)(tb + 3 * as * d->n_classes), d->n_classes};
+  k_update_iwb<S, C><<<dim3(gx, gy, gz), dim3(kBX, kBY), 0, s>>>(
+      (const C*)d->d_cls, (const S*)cur, (S*)past, tab, (int)d->X, (int)d->Y, d->XY,
+      (int)(d->Z - 1), (int)zc);
+  count_launch();
+  PFDTD_CK(cudaGetLastError());
+  return PFDTD_OK;
+}
+
 template <typename S>
 int launch_update_s(pfdtd_domain* d, const void* cur, void* past, cudaStream_t s) {
+  if (d->class_scheme == PFDTD_IWB)
+    return d->cls_bytes == 1 ? launch_iwb_t<S, uint8_t>(d, cur, past, s)
+                             : launch_iwb_t<S, uint16_t>(d, cur, past, s);
   const bool centred = (d->class_scheme == PFDTD_SRL);
   if (d->cls_bytes == 1)
     return centred ? launch_update_t<S, uint8_t, 1>(d, cur, past, s)
@@ -202,7 +331,8 @@ int eval_class_coefs(int precision, int scheme, int quirks, const double* params
                      const std::vector<uint16_t>& keys, std::vector<uint8_t>& out_tab);
 
 int launch_update(pfdtd_domain* d, const void* cur, void* past, cudaStream_t s) {
-  if (d->kernel_variant != PFDTD_KERNEL_ZMARCH && tma_supported(d))
+  if (d->kernel_variant != PFDTD_KERNEL_ZMARCH && d->class_scheme != PFDTD_IWB &&
+      tma_supported(d))
     return launch_update_tma(d, cur, past, s);
   switch (d->precision) {
     case PFDTD_F32: return launch_update_s<float>(d, cur, past, s);
@@ -227,7 +357,8 @@ int launch_io(pfdtd_domain* d, void* cur, void* rec_out, int64_t rec_ld, int64_t
 // Build the class ids and the coefficient table for the domain's current
 // scheme, quirks, parameters and materials.
 int build_classes(pfdtd_domain* d) {
-  const int scheme = (d->scheme == PFDTD_SRL) ? PFDTD_SRL : PFDTD_SRL_FORWARD;
+  const int scheme = (d->scheme == PFDTD_SRL || d->scheme == PFDTD_IWB) ? d->scheme
+                                                                       : PFDTD_SRL_FORWARD;
   if (!d->classes_dirty && d->class_scheme == scheme) return PFDTD_OK;
   if (!d->nodes_set) return fail(PFDTD_ERR_STATE, "node bytes not set");
   if (d->n_mat <= 0) return fail(PFDTD_ERR_STATE, "material table not set");

@@ -15,7 +15,7 @@ from . import _lib as L
 
 _PREC = {"f32": L.F32, "f64": L.F64, "f16": L.F16, "bf16": L.BF16}
 _SCHEME = {"forward": L.SRL_FORWARD, "srl_forward": L.SRL_FORWARD, "shared": L.SHARED,
-           "centred": L.SRL, "centered": L.SRL, "srl": L.SRL}
+           "centred": L.SRL, "centered": L.SRL, "srl": L.SRL, "iwb": L.IWB}
 _STORE_DTYPE = {L.F32: np.float32, L.F64: np.float64, L.F16: np.float16, L.BF16: np.uint16}
 
 
@@ -32,10 +32,11 @@ def arith_dtype(precision: int):
     return np.float64 if precision == L.F64 else np.float32
 
 
-def default_params(octave: int = 0) -> np.ndarray:
+def default_params(octave: int = 0, scheme="forward") -> np.ndarray:
     """[lambda, lambda^2, 1/3, octave] at lambda = 1/sqrt(3), as the reference's
-    SimulationParameters::getParameterPtrDouble (SimulationParameters.cpp:389-396)."""
-    lam = 1.0 / math.sqrt(3.0)
+    SimulationParameters::getParameterPtrDouble (SimulationParameters.cpp:389-396);
+    lambda = 1 for the IWB scheme."""
+    lam = 1.0 if scheme_code(scheme) == L.IWB else 1.0 / math.sqrt(3.0)
     return np.array([lam, lam * lam, 1.0 / 3.0, float(octave)], dtype=np.float64)
 
 

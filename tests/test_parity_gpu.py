@@ -459,3 +459,34 @@ def test_16bit_storage_bit_identical(gpu, O, variant, prec, centred):
     d64, _, _ = O.run(*args, scheme=2 if centred else 0, double=True)
     err = rel_l2(g, d64)
     assert err < (1e-2 if prec == "f16" else 1e-1), err
+
+
+@pytest.mark.parametrize("prec", ["f32", "f64", "f16"])
+def test_iwb_bit_identical(gpu, O, prec):
+    """IWB 27-point scheme (specification in the oracle): the CUDA path equals
+    the oracle bit for bit on a room with boxes (faces, edges, corners)."""
+    room = rooms.boxes_room((96, 64, 48), n_boxes=8, edge=(6, 20), n_materials=12, seed=4)
+    steps = 200
+    srcs = room.random_air_nodes(2, seed=1)
+    rec = room.random_air_nodes(4, seed=2)
+    pulse = rooms.gaussian_pulse(steps, 3.0)
+    params = default_params(scheme="iwb")
+    with Domain(room.dims, prec) as d:
+        d.set_voxels(room.bid, room.mat, centred=True)
+        d.set_materials(room.admittance)
+        d.set_params(params)
+        d.set_scheme("iwb")
+        d.set_sources(srcs, [1, 1], np.stack([pulse, -0.5 * pulse]))
+        d.set_receivers(rec)
+        g, _, _ = d.run(steps)
+        P = d.download_field(L.FIELD_CURRENT)
+    pos, mat = O.encode_nodes(room.bid, room.mat, True)
+    r, rP, _ = O.run(pos, mat, room.dims, room.admittance, params, [room.flat(*s) for s in srcs],
+                     [1, 1], np.stack([pulse, -0.5 * pulse]), [room.flat(*x) for x in rec], steps,
+                     scheme=3, double=(prec == "f64"), storage=(prec if prec == "f16" else None))
+    assert np.abs(r).max() > 1e-4
+    if prec == "f16":
+        assert np.array_equal(g, r) and np.array_equal(P.view(np.uint16), rP.view(np.uint16))
+    else:
+        assert_parity(g, r, prec)
+        assert np.array_equal(P, rP)
