@@ -124,6 +124,21 @@ int pfdtd_nodes_changed(pfdtd_domain* d);
  * PFDTD_F64) exactly as the reference would hold them. */
 int pfdtd_set_materials(pfdtd_domain* d, const double* table, int n_mat, int n_coef);
 
+/* Frequency-dependent boundary admittance (no counterpart in the reference,
+ * which only reserves fields for it, src/kernels/cudaMesh.h:88, :122-123).
+ * flags[m] != 0 gives material m the filter
+ *   Y(z) = (b0 + b1 z^-1 + b2 z^-2 + b3 z^-3) / (1 + a1 z^-1 + a2 z^-2 + a3 z^-3),
+ * coefs [n_mat * 7] = b0, b1, b2, b3, a1, a2, a3 per material (orders below 3
+ * pad with zeros).  Inside boundary nodes of such materials replace the
+ * frequency-independent loss by the filter: with G the node's geometric
+ * factor (forward: 0.5 (6-K) lambda; centred and IWB: lambda * axes) and
+ * x = (p+ - p-)/2, the loss term 2 G Y x becomes 2 G (b0 x + s1), the filter
+ * state (transposed direct form II) kept per node.  n_mat = 0 removes all
+ * filters.  States persist across runs and are zeroed by pfdtd_reset_fields. */
+int pfdtd_set_dif_filters(pfdtd_domain* d, int n_mat, const int32_t* flags, const double* coefs);
+/* Number of frequency-dependent boundary nodes (builds the tables if needed). */
+int pfdtd_get_dif_count(pfdtd_domain* d, int64_t* n);
+
 /* Parameter vector [lambda, lambda^2, 1/3, octave] as
  * SimulationParameters::getParameterPtr(Double) (SimulationParameters.cpp:379-396). */
 int pfdtd_set_params(pfdtd_domain* d, const double params[4]);

@@ -148,7 +148,21 @@ struct RunDesc {
   const int64_t* rec_idx;
   int64_t steps;
   int threads;
+  // Frequency-dependent boundaries: per material a flag and the filter
+  // b0..b3, a1..a3 (order <= 3, unused coefficients 0).
+  const int32_t* dif_flag;   // [n_mat] or null
+  const void* dif_coef;      // [n_mat * 7] of T
 };
+
+// Geometric factor G of a boundary node: the loss term of the FI update is
+// beta (p+ - p-) = 2 G Y x with x = (p+ - p-)/2 (forward: beta = 0.5 Y (6-K)
+// lambda, kernels3d.cu:514; centred and IWB: beta = lambda Y axes).
+template <typename T>
+T geometric_factor(int scheme, unsigned pos, T lambda) {
+  if (scheme == 0) return (T)0.5 * (((T)6 - (T)(pos & kForwardMask)) * lambda);
+  const T ndirs = (T)((pos & 1u) + ((pos >> 1) & 1u) + ((pos >> 2) & 1u));
+  return lambda * ndirs;
+}
 
 // IWB 27-point compact scheme (no counterpart in the reference; the
 // reference's UpdateType has SRL schemes only, SimulationParameters.h:39).
@@ -196,26 +210,64 @@ T iwb_node(const St* P, int64_t N, int64_t c, int64_t X, int64_t XY, unsigned po
 
 // One leapfrog update over z in [1, Z-2] writing into Pp.
 // Forward rule: kernels3d.cu:485-529.  Centred rule: kernels3d.cu:608-665.
+// A frequency-dependent boundary node (material with a filter, inside,
+// G > 0) replaces the FI loss by the filter output y = b0 x + s1
+// (transposed direct form II, x = (p+ - p-)/2):
+//   p+ = s/(1+G b0) * ((L - (1 - G b0) p-) - 2 G s1)      forward, IWB
+//   p+ = s/(1+G b0) * ((L + (G b0 - 1) p-) - 2 G s1)      centred SRL
+// with L the lossless part of the scheme's update, then
+//   s1 = (b1 x - a1 y) + s2,  s2 = (b2 x - a2 y) + s3,  s3 = b3 x - a3 y.
+template <typename T>
+struct DifState {
+  std::vector<int64_t> slot;  // per node: state slot or -1
+  std::vector<T> s;           // [n_slots * 3]
+};
+
 template <typename T, typename St>
 int update(const RunDesc& d, const St* P, St* Pp, const std::vector<T>& beta_tab,
-           const std::vector<uint8_t>& valid) {
+           const std::vector<uint8_t>& valid, DifState<T>* dif = nullptr) {
   const T* prm = (const T*)d.params;
   const T l = prm[0], l2 = prm[1];
   const int64_t X = d.X, XY = d.X * d.Y, Z = d.Z;
+  const T* dcoef = (const T*)d.dif_coef;
   (void)l;
 #pragma omp parallel for schedule(static) num_threads(d.threads)
   for (int64_t z = 1; z < Z - 1; ++z) {
     for (int64_t c = z * XY; c < (z + 1) * XY; ++c) {
       const unsigned pos = d.pos[c];
       const unsigned key = (pos << 8) | d.mat[c];
-      const T beta = beta_tab[key];
+      T beta = beta_tab[key];
       const T p = to_float(P[c]);
       const T pp = to_float(Pp[c]);
+      const int64_t slot = dif ? dif->slot[c] : -1;
+      T g2 = 0, s1 = 0;
+      const T* f = nullptr;
+      if (slot >= 0) {
+        // DIF boundary node: beta from b0, explicit filter state.
+        const unsigned mi_f = d.mat[c];
+        f = dcoef + 7 * mi_f;
+        const T G = geometric_factor<T>(d.scheme, pos, l);
+        beta = G * f[0];
+        g2 = (T)2 * G;
+        s1 = dif->s[3 * slot];
+      }
       T ret;
       if (d.scheme == 3) {
         const T sw = (T)(pos >> kInsideSwitch);
-        ret = iwb_node<T, St>(P, XY * Z, c, X, XY, pos, pp, sw * ((T)1 / ((T)1 + beta)),
-                              (T)1 - beta);
+        if (slot >= 0) {
+          const T lossless = iwb_node<T, St>(P, XY * Z, c, X, XY, pos, (T)0, (T)1, (T)0);
+          ret = sw * ((T)1 / ((T)1 + beta)) * ((lossless - ((T)1 - beta) * pp) - g2 * s1);
+        } else {
+          ret = iwb_node<T, St>(P, XY * Z, c, X, XY, pos, pp, sw * ((T)1 / ((T)1 + beta)),
+                                (T)1 - beta);
+        }
+      } else if (d.scheme == 0 && slot >= 0) {
+        const T position = (T)(pos & kForwardMask);
+        const T sw = (T)(pos >> kInsideSwitch);
+        const T S = (T)to_float(P[c + XY]) + (T)to_float(P[c - XY]) + (T)to_float(P[c + X]) +
+                    (T)to_float(P[c - X]) + (T)to_float(P[c + 1]) + (T)to_float(P[c - 1]);
+        ret = sw * ((T)1 / ((T)1 + beta)) *
+              ((((T)2 - position * l2) * p + l2 * S - ((T)1 - beta) * pp) - g2 * s1);
       } else if (d.scheme == 0) {
         const T position = (T)(pos & kForwardMask);
         const T sw = (T)(pos >> kInsideSwitch);
@@ -238,8 +290,20 @@ int update(const RunDesc& d, const St* P, St* Pp, const std::vector<T>& beta_tab
                   sz = (pos & kSignZ) >> 6;
         const T Sb = px[sx] * dx + py[sy] * dy + pz[sz] * dz;
         const T S = (px[0] + px[1] + py[0] + py[1] + pz[0] + pz[1] + Sb) * l2;
-        ret = (S - ((T)2 - (T)6 * l2) * p + (beta - (T)1) * pp) * sw *
-              ((T)1 / ((T)1 + beta));
+        if (slot >= 0)
+          ret = sw * ((T)1 / ((T)1 + beta)) *
+                (((S - ((T)2 - (T)6 * l2) * p) + (beta - (T)1) * pp) - g2 * s1);
+        else
+          ret = (S - ((T)2 - (T)6 * l2) * p + (beta - (T)1) * pp) * sw *
+                ((T)1 / ((T)1 + beta));
+      }
+      if (slot >= 0) {
+        T* st = &dif->s[3 * slot];
+        const T x = (ret - pp) * (T)0.5;
+        const T y = f[0] * x + st[0];
+        st[0] = (f[1] * x - f[4] * y) + st[1];
+        st[1] = (f[2] * x - f[5] * y) + st[2];
+        st[2] = f[3] * x - f[6] * y;
       }
       Pp[c] = from_arith<St>(ret);
     }
@@ -296,6 +360,21 @@ int run(const RunDesc& d, S* P, S* Pp, T* out) {
   if (rc) return rc;
   const T* samples = (const T*)d.src_samples;
   const int64_t N = d.X * d.Y * d.Z;
+  DifState<T> dif;
+  bool any_dif = false;
+  if (d.dif_flag) {
+    const T l = ((const T*)d.params)[0];
+    dif.slot.assign(N, -1);
+    int64_t n_slots = 0;
+    for (int64_t i = d.X * d.Y; i < N - d.X * d.Y; ++i) {
+      const unsigned pos = d.pos[i];
+      if (!(pos >> kInsideSwitch) || d.mat[i] >= (unsigned)d.n_mat || !d.dif_flag[d.mat[i]]) continue;
+      if (geometric_factor<T>(d.scheme, pos, l) <= (T)0) continue;
+      dif.slot[i] = n_slots++;
+    }
+    dif.s.assign(3 * n_slots, (T)0);
+    any_dif = n_slots > 0;
+  }
   for (int64_t step = 0; step < d.steps; ++step) {
     for (int i = 0; i < d.n_src; ++i) {
       const int64_t idx = d.src_idx[i];
@@ -306,7 +385,7 @@ int run(const RunDesc& d, S* P, S* Pp, T* out) {
       else
         P[idx] = from_arith<S>((T)to_float(P[idx]) + v);  // addSample, cudaMesh.h:349-369
     }
-    update<T, S>(d, P, Pp, beta, valid);
+    update<T, S>(d, P, Pp, beta, valid, any_dif ? &dif : nullptr);
     S* t = P; P = Pp; Pp = t;
     for (int r = 0; r < d.n_rec; ++r) {
       const int64_t idx = d.rec_idx[r];
@@ -470,6 +549,8 @@ double oracle_source_sample_f64(int src_type, int input_type, uint32_t step, uin
 }
 
 // Full run (kernels3d.cu:31-203 float, :205-374 double; precision 2 and 3
+// store the fields in FP16 / BF16 with float arithmetic; dif_flag/dif_coef
+// optionally give materials frequency-dependent admittance filters).
 // store the fields in FP16 / BF16 with float arithmetic).  P and Pp hold the
 // initial (current, past) fields and receive the final ones; out receives
 // [n_rec * steps] receiver samples, row per receiver (kernels3d.cu:183-191).
@@ -479,9 +560,10 @@ int oracle_run(int precision, int scheme, int quirks, int64_t X, int64_t Y, int6
                const void* params, int n_src, const int64_t* src_idx,
                const int32_t* src_type, const void* src_samples, int n_rec,
                const int64_t* rec_idx, int64_t steps, void* P, void* Pp, void* out,
-               int threads) {
+               int threads, const int32_t* dif_flag, const void* dif_coef) {
   RunDesc d{scheme, quirks, X, Y, Z, pos, mat, table, n_mat, params, n_src, src_idx,
-            src_type, src_samples, n_rec, rec_idx, steps, threads > 0 ? threads : 1};
+            src_type, src_samples, n_rec, rec_idx, steps, threads > 0 ? threads : 1,
+            dif_flag, dif_coef};
   switch (precision) {
     case 1: return run<double, double>(d, (double*)P, (double*)Pp, (double*)out);
     case 2: return run<float, _Float16>(d, (_Float16*)P, (_Float16*)Pp, (float*)out);

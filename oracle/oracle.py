@@ -45,7 +45,7 @@ def load(build_if_missing: bool = True) -> C.CDLL:
                                              vp, C.c_uint32]
     lib.oracle_source_sample_f64.restype = C.c_double
     lib.oracle_run.argtypes = [i32, i32, i32, i64, i64, i64, vp, vp, vp, i32, vp, i32, vp, vp,
-                               vp, i32, vp, i64, vp, vp, vp, i32]
+                               vp, i32, vp, i64, vp, vp, vp, i32, vp, vp]
     lib.oracle_run.restype = i32
     lib.oracle_max_threads.argtypes = []
     lib.oracle_max_threads.restype = i32
@@ -101,10 +101,12 @@ def run(pos: np.ndarray, mat: np.ndarray, dims: Sequence[int], table: np.ndarray
         samples: np.ndarray, rec_idx: Sequence[int], steps: int, scheme: int = 0,
         quirks: int = 0, double: bool = False, threads: int = 0,
         P0: Optional[np.ndarray] = None, Pp0: Optional[np.ndarray] = None,
-        storage: Optional[str] = None):
+        storage: Optional[str] = None, dif: Optional[Tuple[np.ndarray, np.ndarray]] = None):
     """Oracle step loop.  Returns (receivers [n_rec, steps], P, P_past).
     storage: None (FP32, or FP64 with double=True), "f16" or "bf16" (16-bit
-    fields with float arithmetic; fields returned as float16 / uint16)."""
+    fields with float arithmetic; fields returned as float16 / uint16).
+    dif: (flags [n_mat] int, coefs [n_mat, 7] b0..b3, a1..a3) for materials
+    with frequency-dependent admittance."""
     lib = load()
     dt = np.float64 if double else np.float32
     prec = 1 if double else {None: 0, "f32": 0, "f16": 2, "bf16": 3}[storage]
@@ -125,9 +127,15 @@ def run(pos: np.ndarray, mat: np.ndarray, dims: Sequence[int], table: np.ndarray
     out = np.zeros((ri.size, steps), dtype=dt)
     if threads <= 0:
         threads = lib.oracle_max_threads()
+    dflag = dcoef = None
+    if dif is not None:
+        dflag = np.ascontiguousarray(dif[0], dtype=np.int32).reshape(-1)
+        dcoef = np.ascontiguousarray(dif[1], dtype=dt).reshape(-1, 7)
+        if dflag.size != n_mat or dcoef.shape[0] != n_mat:
+            raise ValueError("dif tables must have one row per material")
     rc = lib.oracle_run(prec, scheme, quirks, X, Y, Z, _p(pos), _p(mat), _p(tab),
                         n_mat, _p(prm), si.size, _p(si), _p(st), _p(sm), ri.size, _p(ri),
-                        steps, _p(P), _p(Pp), _p(out), threads)
+                        steps, _p(P), _p(Pp), _p(out), threads, _p(dflag), _p(dcoef))
     if rc != 0:
         raise RuntimeError(f"oracle_run failed with {rc}")
     return out, P, Pp

@@ -58,6 +58,8 @@ _SIGNATURES = {
     "pfdtd_get_nodes": (_i32, [_vp, _vp, _vp]),
     "pfdtd_set_materials": (_i32, [_vp, C.POINTER(C.c_double), _i32, _i32]),
     "pfdtd_set_params": (_i32, [_vp, C.POINTER(C.c_double)]),
+    "pfdtd_set_dif_filters": (_i32, [_vp, _i32, C.POINTER(C.c_int32), C.POINTER(C.c_double)]),
+    "pfdtd_get_dif_count": (_i32, [_vp, C.POINTER(_i64)]),
     "pfdtd_set_sources": (_i32, [_vp, _i32, C.POINTER(_i64), C.POINTER(C.c_int32), _vp, _i64]),
     "pfdtd_set_receivers": (_i32, [_vp, _i32, C.POINTER(_i64)]),
     "pfdtd_set_scheme": (_i32, [_vp, _i32]),

@@ -160,6 +160,14 @@ struct pfdtd_domain {
   pfdtd::GraphCache graph;
   int past_step_direction = 1;
 
+  // frequency-dependent boundaries (dif.cu)
+  std::vector<int32_t> dif_flags;   // per material: has a filter
+  std::vector<double> dif_coefs;    // per material: b0..b3, a1..a3
+  int64_t n_dif = 0;
+  int64_t* d_dif_list = nullptr;    // ordered flat indices of DIF nodes
+  void* d_dif_tab = nullptr;        // per class: a, b, c, 2G, filter (11 values)
+  void* d_dif_state = nullptr;      // per DIF node: s1, s2, s3, previous p
+
   // update kernel selection and the pipeline error flag
   int kernel_variant = PFDTD_KERNEL_AUTO;
   int tma_tile = -1;         // tile shape of the TMA kernel, -1 automatic (stencil_tma.cu)
@@ -182,6 +190,11 @@ int launch_io(pfdtd_domain* d, void* cur, void* rec_out, int64_t rec_ld, int64_t
 int build_classes(pfdtd_domain* d);
 // Implemented in stencil_tma.cu
 bool tma_supported(const pfdtd_domain* d);
+// Implemented in dif.cu
+int build_dif(pfdtd_domain* d, const std::vector<uint16_t>& keys,
+              const std::vector<uint8_t>& main_tab);
+int launch_dif(pfdtd_domain* d, const void* cur, void* past, cudaStream_t s);
+int launch_dif_init(pfdtd_domain* d, cudaStream_t s);
 int tma_tile_count();
 int launch_update_tma(pfdtd_domain* d, const void* cur, void* past, cudaStream_t s);
 }  // namespace pfdtd

@@ -1,0 +1,324 @@
+// Frequency-dependent (IIR admittance) boundary nodes.
+//
+// The reference only reserves room for digital impedance filters
+// (src/kernels/cudaMesh.h:88, :122-123).  Here a material may carry
+// Y(z) = (b0 + b1 z^-1 + b2 z^-2 + b3 z^-3) / (1 + a1 z^-1 + a2 z^-2 + a3 z^-3).
+// At such a boundary node the loss term of the frequency-independent update,
+// beta (p+ - p-) = 2 G Y x with x = (p+ - p-)/2 and G the node's geometric
+// factor, becomes 2 G y with y = b0 x + s1 the filter output (transposed
+// direct form II): the b0 part stays implicit (beta = G b0) and the state s1
+// enters explicitly.
+//
+// The main update kernels treat every node with the FI rule; afterwards
+// k_dif_update recomputes the DIF nodes (a sparse, ordered list) from the same
+// P^n and overwrites them.  Because the main kernel has by then overwritten
+// P^{n-1} at those nodes, each DIF node keeps its own previous value in its
+// state (re-read from the past field at the start of every run or step).
+#include "common.cuh"
+
+#include <algorithm>
+#include <vector>
+
+namespace pfdtd {
+namespace {
+
+constexpr int kChunkNodes = 4096;  // nodes per block when listing DIF nodes
+constexpr int kListThreads = 256;
+
+// Per DIF class: a, b, c, g2 and the filter b0..b3, a1..a3 (11 values).
+constexpr int kDifClassVals = 11;
+
+__global__ void k_dif_count(const void* __restrict__ cls, int cls_bytes,
+                            const uint8_t* __restrict__ is_dif, int64_t begin, int64_t end,
+                            int* __restrict__ counts) {
+  const int64_t start = begin + (int64_t)blockIdx.x * kChunkNodes;
+  int n = 0;
+  for (int i = threadIdx.x; i < kChunkNodes; i += blockDim.x) {
+    const int64_t j = start + i;
+    if (j >= end) break;
+    const unsigned c = cls_bytes == 1 ? ((const uint8_t*)cls)[j] : ((const uint16_t*)cls)[j];
+    n += is_dif[c];
+  }
+  for (int o = 16; o > 0; o >>= 1) n += __shfl_down_sync(0xffffffffu, n, o);
+  __shared__ int sn[kListThreads / 32];
+  if ((threadIdx.x & 31) == 0) sn[threadIdx.x >> 5] = n;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    int t = 0;
+    for (int w = 0; w < kListThreads / 32; ++w) t += sn[w];
+    counts[blockIdx.x] = t;
+  }
+}
+
+// Ordered write: thread t owns nodes [start + 16 t, start + 16 t + 16).
+__global__ void k_dif_list(const void* __restrict__ cls, int cls_bytes,
+                           const uint8_t* __restrict__ is_dif, int64_t begin, int64_t end,
+                           const int* __restrict__ offsets, int64_t* __restrict__ list) {
+  constexpr int per = kChunkNodes / kListThreads;
+  const int64_t start = begin + (int64_t)blockIdx.x * kChunkNodes + (int64_t)threadIdx.x * per;
+  int n = 0;
+  for (int i = 0; i < per; ++i) {
+    const int64_t j = start + i;
+    if (j >= end) break;
+    const unsigned c = cls_bytes == 1 ? ((const uint8_t*)cls)[j] : ((const uint16_t*)cls)[j];
+    n += is_dif[c];
+  }
+  __shared__ int scan[kListThreads];
+  scan[threadIdx.x] = n;
+  __syncthreads();
+  for (int o = 1; o < kListThreads; o <<= 1) {
+    const int v = threadIdx.x >= o ? scan[threadIdx.x - o] : 0;
+    __syncthreads();
+    scan[threadIdx.x] += v;
+    __syncthreads();
+  }
+  int k = offsets[blockIdx.x] + scan[threadIdx.x] - n;
+  for (int i = 0; i < per; ++i) {
+    const int64_t j = start + i;
+    if (j >= end) break;
+    const unsigned c = cls_bytes == 1 ? ((const uint8_t*)cls)[j] : ((const uint16_t*)cls)[j];
+    if (is_dif[c]) list[k++] = j;
+  }
+}
+
+// prev <- P^{n-1} at each DIF node (start of a run or step).
+template <typename S>
+__global__ void k_dif_init_prev(const int64_t* __restrict__ list, int64_t n,
+                                const S* __restrict__ past, typename Store<S>::A* __restrict__ st) {
+  for (int64_t k = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; k < n;
+       k += (int64_t)gridDim.x * blockDim.x)
+    st[4 * k + 3] = Store<S>::load(past[list[k]]);
+}
+
+template <typename S, int SCHEME>
+__global__ void k_dif_update(const int64_t* __restrict__ list, int64_t n,
+                             const void* __restrict__ cls, int cls_bytes,
+                             const typename Store<S>::A* __restrict__ dtab, const S* __restrict__ P,
+                             S* __restrict__ Pp, typename Store<S>::A* __restrict__ st, int64_t X,
+                             int64_t XY, typename Store<S>::A l2, const uint32_t* __restrict__ cpos) {
+  using A = typename Store<S>::A;
+  using R = Rn<A>;
+  using Sto = Store<S>;
+  for (int64_t k = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; k < n;
+       k += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t i = list[k];
+    const unsigned c = cls_bytes == 1 ? ((const uint8_t*)cls)[i] : ((const uint16_t*)cls)[i];
+    const A* t = dtab + (int64_t)kDifClassVals * c;
+    const A a = t[0], b = t[1], cc = t[2], g2 = t[3];
+    A* s = st + 4 * k;
+    const A pp = s[3];
+    const A s1 = s[0];
+    const A p = Sto::load(P[i]);
+    A num;
+    if (SCHEME == 0) {
+      const A s6 = R::add(R::add(R::add(R::add(R::add(Sto::load(P[i + XY]), Sto::load(P[i - XY])),
+                                                  Sto::load(P[i + X])), Sto::load(P[i - X])),
+                                  Sto::load(P[i + 1])), Sto::load(P[i - 1]));
+      num = R::sub(R::sub(R::add(R::mul(b, p), R::mul(l2, s6)), R::mul(cc, pp)), R::mul(g2, s1));
+    } else if (SCHEME == 1) {
+      const uint32_t cp = cpos[c];
+      const A xm = Sto::load(P[i - 1]), xp = Sto::load(P[i + 1]);
+      const A ym = Sto::load(P[i - X]), yp = Sto::load(P[i + X]);
+      const A zm = Sto::load(P[i - XY]), zp = Sto::load(P[i + XY]);
+      const A dx = (A)(cp & 1u), dy = (A)((cp >> 1) & 1u), dz = (A)((cp >> 2) & 1u);
+      const A bx = (cp & 0x10u) ? xp : xm;
+      const A by = (cp & 0x20u) ? yp : ym;
+      const A bz = (cp & 0x40u) ? zm : zp;
+      const A sb6 = R::add(R::add(R::mul(bx, dx), R::mul(by, dy)), R::mul(bz, dz));
+      const A s7 = R::add(R::add(R::add(R::add(R::add(R::add(xm, xp), ym), yp), zp), zm), sb6);
+      num = R::sub(R::add(R::sub(R::mul(s7, l2), R::mul(b, p)), R::mul(cc, pp)), R::mul(g2, s1));
+    } else {
+      const uint32_t cp = cpos[c];
+      const int ox = (cp & 0x10u) ? -1 : 1, oy = (cp & 0x20u) ? -1 : 1, oz = (cp & 0x40u) ? -1 : 1;
+      A f1 = (A)0, f2 = (A)0, f3 = (A)0;
+      bool n1 = true, n2 = true, n3 = true;
+      for (int dz = -1; dz <= 1; ++dz)
+        for (int dy = -1; dy <= 1; ++dy)
+          for (int dx = -1; dx <= 1; ++dx) {
+            const int nn = (dx != 0) + (dy != 0) + (dz != 0);
+            if (nn == 0) continue;
+            const int mx = ((cp & 1u) && dx == ox) ? -dx : dx;
+            const int my = ((cp & 2u) && dy == oy) ? -dy : dy;
+            const int mz = ((cp & 4u) && dz == oz) ? -dz : dz;
+            const A v = Sto::load(P[i + mz * XY + my * X + mx]);
+            if (nn == 1) { f1 = n1 ? v : R::add(f1, v); n1 = false; }
+            else if (nn == 2) { f2 = n2 ? v : R::add(f2, v); n2 = false; }
+            else { f3 = n3 ? v : R::add(f3, v); n3 = false; }
+          }
+      const A sw = R::add(R::add(R::mul(f1, (A)0.25), R::mul(f2, (A)0.125)), R::mul(f3, (A)0.0625));
+      num = R::sub(R::sub(R::add(sw, R::mul(b, p)), R::mul(cc, pp)), R::mul(g2, s1));
+    }
+    const A out = R::mul(a, num);
+    // Filter state update (transposed direct form II).
+    const A x = R::mul(R::sub(out, pp), (A)0.5);
+    const A y = R::add(R::mul(t[4], x), s1);
+    s[0] = R::add(R::sub(R::mul(t[5], x), R::mul(t[8], y)), s[1]);
+    s[1] = R::add(R::sub(R::mul(t[6], x), R::mul(t[9], y)), s[2]);
+    s[2] = R::sub(R::mul(t[7], x), R::mul(t[10], y));
+    s[3] = p;
+    Pp[i] = Sto::store(out);
+  }
+}
+
+int grid_for(int64_t n) {
+  return (int)std::max<int64_t>(1, std::min<int64_t>((n + 255) / 256, 152 * 16));
+}
+
+template <typename A>
+void eval_dif_classes(const pfdtd_domain* d, int scheme, const std::vector<uint16_t>& keys,
+                      const std::vector<uint8_t>& main_tab, std::vector<uint8_t>& is_dif,
+                      std::vector<A>& dtab) {
+  const size_t n = keys.size();
+  const A* mb = (const A*)(main_tab.data() + n * sizeof(A));  // b coefficients
+  const A l = (A)d->params[0];
+  is_dif.assign(n, 0);
+  dtab.assign(n * kDifClassVals, (A)0);
+  for (size_t i = 0; i < n; ++i) {
+    const unsigned pos = keys[i] >> 8, m = keys[i] & 0xFFu;
+    if (!(pos >> 7) || m >= d->dif_flags.size() || !d->dif_flags[m]) continue;
+    A G;
+    if (scheme == PFDTD_SRL_FORWARD)
+      G = (A)0.5 * (((A)6 - (A)(pos & 0x7Fu)) * l);
+    else
+      G = l * (A)((pos & 1u) + ((pos >> 1) & 1u) + ((pos >> 2) & 1u));
+    if (!(G > (A)0)) continue;
+    const double* f = &d->dif_coefs[7 * m];
+    const A b0 = (A)f[0];
+    const A beta = G * b0;
+    A* t = &dtab[i * kDifClassVals];
+    t[0] = (A)1 * ((A)1 / ((A)1 + beta));  // inside switch is 1 for DIF nodes
+    t[1] = mb[i];
+    t[2] = (scheme == PFDTD_SRL) ? beta - (A)1 : (A)1 - beta;
+    t[3] = (A)2 * G;
+    for (int j = 0; j < 7; ++j) t[4 + j] = (A)f[j];
+    is_dif[i] = 1;
+  }
+}
+
+template <typename S>
+int launch_dif_t(pfdtd_domain* d, const void* cur, void* past, cudaStream_t s) {
+  using A = typename Store<S>::A;
+  const size_t as = sizeof(A);
+  const uint32_t* cpos = (const uint32_t*)((const char*)d->d_ctab + 3 * as * d->n_classes);
+  const A l2 = (A)d->params[1];
+  const int g = grid_for(d->n_dif);
+  switch (d->class_scheme) {
+    case PFDTD_SRL:
+      k_dif_update<S, 1><<<g, 256, 0, s>>>(d->d_dif_list, d->n_dif, d->d_cls, d->cls_bytes,
+                                           (const A*)d->d_dif_tab, (const S*)cur, (S*)past,
+                                           (A*)d->d_dif_state, d->X, d->XY, l2, cpos);
+      break;
+    case PFDTD_IWB:
+      k_dif_update<S, 2><<<g, 256, 0, s>>>(d->d_dif_list, d->n_dif, d->d_cls, d->cls_bytes,
+                                           (const A*)d->d_dif_tab, (const S*)cur, (S*)past,
+                                           (A*)d->d_dif_state, d->X, d->XY, l2, cpos);
+      break;
+    default:
+      k_dif_update<S, 0><<<g, 256, 0, s>>>(d->d_dif_list, d->n_dif, d->d_cls, d->cls_bytes,
+                                           (const A*)d->d_dif_tab, (const S*)cur, (S*)past,
+                                           (A*)d->d_dif_state, d->X, d->XY, l2, cpos);
+  }
+  count_launch();
+  PFDTD_CK(cudaGetLastError());
+  return PFDTD_OK;
+}
+
+template <typename S>
+int launch_init_t(pfdtd_domain* d, cudaStream_t s) {
+  using A = typename Store<S>::A;
+  k_dif_init_prev<S><<<grid_for(d->n_dif), 256, 0, s>>>(d->d_dif_list, d->n_dif,
+                                                        (const S*)d->past_field(),
+                                                        (A*)d->d_dif_state);
+  count_launch();
+  PFDTD_CK(cudaGetLastError());
+  return PFDTD_OK;
+}
+
+}  // namespace
+
+// Build the DIF class table and the ordered DIF node list after the classes
+// were (re)built.  keys/main_tab: the class keys and coefficient table.
+int build_dif(pfdtd_domain* d, const std::vector<uint16_t>& keys,
+              const std::vector<uint8_t>& main_tab) {
+  for (void** p : {(void**)&d->d_dif_list, &d->d_dif_tab, &d->d_dif_state})
+    if (*p) {
+      PFDTD_CK(cudaFree(*p));
+      *p = nullptr;
+    }
+  d->n_dif = 0;
+  if (d->dif_flags.empty()) return PFDTD_OK;
+  std::vector<uint8_t> is_dif;
+  std::vector<uint8_t> tab_bytes;
+  if (d->precision == PFDTD_F64) {
+    std::vector<double> t;
+    eval_dif_classes<double>(d, d->class_scheme, keys, main_tab, is_dif, t);
+    tab_bytes.assign((uint8_t*)t.data(), (uint8_t*)(t.data() + t.size()));
+  } else {
+    std::vector<float> t;
+    eval_dif_classes<float>(d, d->class_scheme, keys, main_tab, is_dif, t);
+    tab_bytes.assign((uint8_t*)t.data(), (uint8_t*)(t.data() + t.size()));
+  }
+  if (std::find(is_dif.begin(), is_dif.end(), 1) == is_dif.end()) return PFDTD_OK;
+  cudaStream_t s = d->stream;
+  const int64_t begin = d->XY, end = d->N - d->XY;
+  const int64_t blocks = (end - begin + kChunkNodes - 1) / kChunkNodes;
+  uint8_t* d_is = nullptr;
+  int* d_counts = nullptr;
+  PFDTD_CK(cudaMalloc((void**)&d_is, is_dif.size()));
+  PFDTD_CK(cudaMalloc((void**)&d_counts, sizeof(int) * (blocks + 1)));
+  PFDTD_CK(cudaMemcpyAsync(d_is, is_dif.data(), is_dif.size(), cudaMemcpyHostToDevice, s));
+  k_dif_count<<<(int)blocks, kListThreads, 0, s>>>(d->d_cls, d->cls_bytes, d_is, begin, end, d_counts);
+  count_launch();
+  std::vector<int> counts(blocks);
+  PFDTD_CK(cudaMemcpyAsync(counts.data(), d_counts, sizeof(int) * blocks, cudaMemcpyDeviceToHost, s));
+  PFDTD_CK(cudaStreamSynchronize(s));
+  std::vector<int> offsets(blocks);
+  int64_t total = 0;
+  for (int64_t b = 0; b < blocks; ++b) {
+    offsets[b] = (int)total;
+    total += counts[b];
+  }
+  if (total > 0) {
+    PFDTD_CK(cudaMemcpyAsync(d_counts, offsets.data(), sizeof(int) * blocks, cudaMemcpyHostToDevice, s));
+    PFDTD_CK(cudaMalloc((void**)&d->d_dif_list, sizeof(int64_t) * total));
+    k_dif_list<<<(int)blocks, kListThreads, 0, s>>>(d->d_cls, d->cls_bytes, d_is, begin, end,
+                                                   d_counts, d->d_dif_list);
+    count_launch();
+    PFDTD_CK(cudaGetLastError());
+    PFDTD_CK(cudaMalloc(&d->d_dif_tab, tab_bytes.size()));
+    PFDTD_CK(cudaMemcpyAsync(d->d_dif_tab, tab_bytes.data(), tab_bytes.size(),
+                             cudaMemcpyHostToDevice, s));
+    const size_t sbytes = (size_t)total * 4 * d->arith_size();
+    PFDTD_CK(cudaMalloc(&d->d_dif_state, sbytes));
+    PFDTD_CK(cudaMemsetAsync(d->d_dif_state, 0, sbytes, s));
+  }
+  PFDTD_CK(cudaStreamSynchronize(s));
+  cudaFree(d_is);
+  cudaFree(d_counts);
+  d->n_dif = total;
+  return PFDTD_OK;
+}
+
+int launch_dif(pfdtd_domain* d, const void* cur, void* past, cudaStream_t s) {
+  if (d->n_dif <= 0) return PFDTD_OK;
+  switch (d->precision) {
+    case PFDTD_F32: return launch_dif_t<float>(d, cur, past, s);
+    case PFDTD_F64: return launch_dif_t<double>(d, cur, past, s);
+    case PFDTD_F16: return launch_dif_t<__half>(d, cur, past, s);
+    case PFDTD_BF16: return launch_dif_t<__nv_bfloat16>(d, cur, past, s);
+  }
+  return fail(PFDTD_ERR_UNSUPPORTED, "unknown precision");
+}
+
+int launch_dif_init(pfdtd_domain* d, cudaStream_t s) {
+  if (d->n_dif <= 0) return PFDTD_OK;
+  switch (d->precision) {
+    case PFDTD_F32: return launch_init_t<float>(d, s);
+    case PFDTD_F64: return launch_init_t<double>(d, s);
+    case PFDTD_F16: return launch_init_t<__half>(d, s);
+    case PFDTD_BF16: return launch_init_t<__nv_bfloat16>(d, s);
+  }
+  return fail(PFDTD_ERR_UNSUPPORTED, "unknown precision");
+}
+
+}  // namespace pfdtd

@@ -115,6 +115,8 @@ int enqueue_step(pfdtd_domain* d, void* rec_out, int64_t rec_ld, int64_t inject_
   if (rc) return rc;
   rc = launch_update(d, d->cur_field(), d->past_field(), s);
   if (rc) return rc;
+  rc = launch_dif(d, d->cur_field(), d->past_field(), s);
+  if (rc) return rc;
   d->cur = 1 - d->cur;
   return PFDTD_OK;
 }
@@ -183,6 +185,7 @@ int enqueue_run(pfdtd_domain* d, int64_t steps, void* rec_out, F&& between, bool
                 int64_t* steps_queued) {
   cudaStream_t s = d->stream;
   PFDTD_CK(cudaMemsetAsync(d->d_step, 0, sizeof(int64_t), s));
+  if (int rc0 = launch_dif_init(d, s)) return rc0;
   const int64_t chunks = steps / kChunk;
   const int64_t rem = steps - chunks * kChunk;
   cudaEvent_t ev[2] = {nullptr, nullptr};
@@ -328,7 +331,8 @@ int pfdtd_destroy(pfdtd_domain* d) {
   if (d->graph.exec) cudaGraphExecDestroy(d->graph.exec);
   void* ptrs[] = {d->field_base[0], d->field_base[1], d->d_pos, d->d_mat, d->d_cls,
                   d->d_ctab, d->d_src_idx, d->d_src_mode, d->d_src_samples, d->d_rec_idx,
-                  d->d_step, d->d_rec_out, d->d_err};
+                  d->d_step, d->d_rec_out, d->d_err, d->d_dif_list, d->d_dif_tab,
+                  d->d_dif_state};
   for (void* p : ptrs)
     if (p) cudaFree(p);
   if (d->stream) cudaStreamDestroy(d->stream);
@@ -587,7 +591,11 @@ int pfdtd_step(pfdtd_domain* d, int64_t step, int step_direction, void* out, int
   PFDTD_CK(cudaMemcpyAsync(d->d_step, &step, sizeof(int64_t), cudaMemcpyHostToDevice, s));
   rc = launch_io(d, d->cur_field(), nullptr, 0, INT64_MAX, s);
   if (rc) return rc;
+  rc = launch_dif_init(d, s);
+  if (rc) return rc;
   rc = launch_update(d, d->cur_field(), d->past_field(), s);
+  if (rc) return rc;
+  rc = launch_dif(d, d->cur_field(), d->past_field(), s);
   if (rc) return rc;
   // kernels3d.cu:462-465: swap only while the direction is unchanged.
   if (d->past_step_direction == step_direction) d->cur = 1 - d->cur;
@@ -672,7 +680,35 @@ int pfdtd_reset_fields(pfdtd_domain* d) {
   DeviceGuard g(d->device);
   const size_t fbytes = (size_t)(d->N + 2 * d->margin) * d->esize;
   for (int i = 0; i < 2; ++i) PFDTD_CK(cudaMemsetAsync(d->field_base[i], 0, fbytes, d->stream));
+  if (d->n_dif > 0)
+    PFDTD_CK(cudaMemsetAsync(d->d_dif_state, 0, (size_t)d->n_dif * 4 * d->arith_size(), d->stream));
   PFDTD_CK(cudaStreamSynchronize(d->stream));
+  return PFDTD_OK;
+}
+
+int pfdtd_set_dif_filters(pfdtd_domain* d, int n_mat, const int32_t* flags, const double* coefs) {
+  if (int rc = check_domain(d)) return rc;
+  if (n_mat < 0 || (n_mat > 0 && (!flags || !coefs)))
+    return fail(PFDTD_ERR_ARG, "invalid filter tables");
+  d->dif_flags.assign(flags, flags + n_mat);
+  d->dif_coefs.assign(coefs, coefs + (size_t)n_mat * 7);
+  for (int m = 0; m < n_mat; ++m) {
+    if (!flags[m]) continue;
+    const double* f = coefs + 7 * m;
+    for (int j = 0; j < 7; ++j)
+      if (!(f[j] == f[j])) return fail(PFDTD_ERR_ARG, "filter coefficient is NaN");
+  }
+  d->classes_dirty = true;
+  return PFDTD_OK;
+}
+
+int pfdtd_get_dif_count(pfdtd_domain* d, int64_t* n) {
+  if (int rc = check_domain(d)) return rc;
+  if (!n) return fail(PFDTD_ERR_ARG, "null output");
+  DeviceGuard g(d->device);
+  int rc = prepare_run(d);
+  if (rc) return rc;
+  *n = d->n_dif;
   return PFDTD_OK;
 }
 

@@ -418,6 +418,8 @@ int build_classes(pfdtd_domain* d) {
   PFDTD_CK(cudaStreamSynchronize(s));
   d->n_classes = n_classes;
   d->class_scheme = scheme;
+  rc = build_dif(d, keys, tab);
+  if (rc != PFDTD_OK) return rc;
   d->classes_dirty = false;
   d->class_version++;
   return PFDTD_OK;

@@ -131,6 +131,19 @@ class Domain:
         L.call("pfdtd_set_materials", self.handle,
                t.ctypes.data_as(C.POINTER(C.c_double)), t.shape[0], t.shape[1])
 
+    def set_dif_filters(self, flags: Sequence[int], coefs: np.ndarray) -> None:
+        """Per-material frequency-dependent admittance filters: flags [n_mat],
+        coefs [n_mat, 7] = b0..b3, a1..a3 (see materials.dif_table)."""
+        f = np.ascontiguousarray(flags, dtype=np.int32).reshape(-1)
+        c = np.ascontiguousarray(coefs, dtype=np.float64).reshape(-1, 7)
+        L.call("pfdtd_set_dif_filters", self.handle, f.size,
+               f.ctypes.data_as(C.POINTER(C.c_int32)), c.ctypes.data_as(C.POINTER(C.c_double)))
+
+    def dif_count(self) -> int:
+        n = C.c_int64()
+        L.call("pfdtd_get_dif_count", self.handle, C.byref(n))
+        return int(n.value)
+
     def set_params(self, params: Optional[Sequence[float]] = None) -> None:
         p = np.ascontiguousarray(default_params() if params is None else params, dtype=np.float64)
         L.call("pfdtd_set_params", self.handle, p.ctypes.data_as(C.POINTER(C.c_double)))

@@ -490,3 +490,45 @@ def test_iwb_bit_identical(gpu, O, prec):
     else:
         assert_parity(g, r, prec)
         assert np.array_equal(P, rP)
+
+
+@pytest.mark.parametrize("prec", ["f32", "f64"])
+@pytest.mark.parametrize("scheme", ["forward", "centred", "iwb"])
+def test_dif_boundaries_bit_identical(gpu, O, prec, scheme):
+    """Frequency-dependent boundaries (3rd-order passive IIR admittances on
+    half of the materials): the CUDA path equals the oracle bit for bit."""
+    from parallelfdtd_gb300 import materials
+    room = rooms.boxes_room((128, 64, 48), n_boxes=8, edge=(6, 20), n_materials=10, seed=6)
+    steps = 300
+    srcs = room.random_air_nodes(2, seed=1)
+    rec = room.random_air_nodes(4, seed=2)
+    pulse = rooms.gaussian_pulse(steps, 3.0)
+    code = {"forward": 0, "centred": 2, "iwb": 3}[scheme]
+    params = default_params(scheme=scheme)
+    flags = np.array([m % 2 for m in range(10)], np.int32)
+    table = materials.dif_table(materials.positive_real_filters(10, 3, seed=12), 3)
+    with Domain(room.dims, prec) as d:
+        d.set_voxels(room.bid, room.mat, centred=(scheme != "forward"))
+        d.set_materials(room.admittance)
+        d.set_params(params)
+        d.set_scheme(scheme)
+        d.set_dif_filters(flags, table)
+        d.set_sources(srcs, [1, 1], np.stack([pulse, -0.5 * pulse]))
+        d.set_receivers(rec)
+        n_dif = d.dif_count()
+        g, _, _ = d.run(steps)
+        P = d.download_field(L.FIELD_CURRENT)
+    pos, mat = O.encode_nodes(room.bid, room.mat, scheme != "forward")
+    r, rP, _ = O.run(pos, mat, room.dims, room.admittance, params, [room.flat(*s) for s in srcs],
+                     [1, 1], np.stack([pulse, -0.5 * pulse]), [room.flat(*x) for x in rec], steps,
+                     scheme=code, double=(prec == "f64"), dif=(flags, table))
+    X, Y, Z = room.dims
+    inside = (pos.reshape(Z, Y, X)[1:-1] >> 7) == 1
+    flagged = flags[mat.reshape(Z, Y, X)[1:-1]] == 1
+    if scheme == "forward":
+        boundary = (pos.reshape(Z, Y, X)[1:-1] & 0x7F) < 6
+    else:
+        boundary = (pos.reshape(Z, Y, X)[1:-1] & 0x07) != 0
+    assert n_dif == int(np.count_nonzero(inside & flagged & boundary)) > 0
+    assert_parity(g, r, prec)
+    assert np.array_equal(P, rP)
