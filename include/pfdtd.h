@@ -97,6 +97,16 @@ int pfdtd_device_count(int* count);
  * domain.  dim_z >= 3. */
 int pfdtd_create(int64_t dim_x, int64_t dim_y, int64_t dim_z, int precision, int device,
                  pfdtd_domain** out);
+/* Batched domain: `fields` (a power of two, 1..64) independent pressure
+ * fields per node sharing the node bytes, materials and parameters — e.g. one
+ * field per source position of a multi-source study.  Fields are interleaved
+ * node-major (element = node * fields + field), so one class byte is read per
+ * `fields` node-updates.  pfdtd_create is pfdtd_create_batched with 1 field.
+ * Single-node access, slices and the unbatched source/receiver calls use
+ * field 0. */
+int pfdtd_create_batched(int64_t dim_x, int64_t dim_y, int64_t dim_z, int fields, int precision,
+                         int device, pfdtd_domain** out);
+int pfdtd_get_fields(const pfdtd_domain* d, int* fields);
 int pfdtd_destroy(pfdtd_domain* d);
 int pfdtd_get_dims(const pfdtd_domain* d, int64_t dims[3]);
 int pfdtd_get_precision(const pfdtd_domain* d, int* precision);
@@ -151,10 +161,17 @@ int pfdtd_set_params(pfdtd_domain* d, const double params[4]);
 int pfdtd_set_sources(pfdtd_domain* d, int n, const int64_t* xyz, const int32_t* type,
                       const void* samples, int64_t n_samples);
 
+/* Sources of a batched domain: field[i] is the field source i drives. */
+int pfdtd_set_sources_batched(pfdtd_domain* d, int n, const int64_t* xyz, const int32_t* field,
+                              const int32_t* type, const void* samples, int64_t n_samples);
+
 /* Receivers: n positions (x,y,z triples).  A receiver whose z lies outside
  * the grid is skipped and its output row left untouched
  * (kernels3d.cu:66-78, :164-173). */
 int pfdtd_set_receivers(pfdtd_domain* d, int n, const int64_t* xyz);
+
+/* Receivers of a batched domain: field[i] is the field receiver i records. */
+int pfdtd_set_receivers_batched(pfdtd_domain* d, int n, const int64_t* xyz, const int32_t* field);
 
 /* Update scheme used by the next run/step (PFDTD_SRL_FORWARD, _SHARED, _SRL, _IWB). */
 int pfdtd_set_scheme(pfdtd_domain* d, int scheme);
@@ -196,7 +213,7 @@ int pfdtd_flip(pfdtd_domain* d);
 int pfdtd_reset_fields(pfdtd_domain* d);
 /* Device pointer of a field (PFDTD_FIELD_*); element 0 is node (0,0,0). */
 int pfdtd_get_field_ptr(pfdtd_domain* d, int which, void** d_ptr);
-/* Copy a whole field to / from the host (N elements of the storage type). */
+/* Copy a whole field to / from the host (N * fields elements of the storage type). */
 int pfdtd_download_field(pfdtd_domain* d, int which, void* host);
 int pfdtd_upload_field(pfdtd_domain* d, int which, const void* host);
 

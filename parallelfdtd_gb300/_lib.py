@@ -48,6 +48,11 @@ _SIGNATURES = {
     "pfdtd_device_count": (_i32, [C.POINTER(_i32)]),
     "pfdtd_create": (_i32, [_i64, _i64, _i64, _i32, _i32, C.POINTER(_vp)]),
     "pfdtd_destroy": (_i32, [_vp]),
+    "pfdtd_create_batched": (_i32, [_i64, _i64, _i64, _i32, _i32, _i32, C.POINTER(_vp)]),
+    "pfdtd_get_fields": (_i32, [_vp, C.POINTER(_i32)]),
+    "pfdtd_set_sources_batched": (_i32, [_vp, _i32, C.POINTER(_i64), C.POINTER(C.c_int32),
+                                         C.POINTER(C.c_int32), _vp, _i64]),
+    "pfdtd_set_receivers_batched": (_i32, [_vp, _i32, C.POINTER(_i64), C.POINTER(C.c_int32)]),
     "pfdtd_get_dims": (_i32, [_vp, C.POINTER(_i64)]),
     "pfdtd_get_precision": (_i32, [_vp, C.POINTER(_i32)]),
     "pfdtd_get_serial": (_i32, [_vp, C.POINTER(_i64)]),

@@ -116,6 +116,10 @@ struct pfdtd_domain {
   int scheme = PFDTD_SRL_FORWARD;
   int quirks = 0;
   int64_t X = 0, Y = 0, Z = 0, XY = 0, N = 0;
+  // Batched fields: K independent fields per node sharing the geometry,
+  // interleaved node-major (element = node * K + field); K a power of two.
+  int K = 1, kshift = 0;
+  int64_t NE = 0;            // field elements, N * K
   size_t esize = 4;          // storage bytes per field element
   int64_t margin = 0;        // elements before node 0 / after node N-1
   void* field_base[2] = {nullptr, nullptr};

@@ -82,16 +82,20 @@ __global__ void k_dif_list(const void* __restrict__ cls, int cls_bytes,
 }
 
 // prev <- P^{n-1} at each DIF node (start of a run or step).
+// (n counts DIF nodes times fields; entry k is field k & (K-1) of DIF node
+// k >> kshift.)
 template <typename S>
-__global__ void k_dif_init_prev(const int64_t* __restrict__ list, int64_t n,
+__global__ void k_dif_init_prev(const int64_t* __restrict__ list, int64_t n, int kshift,
                                 const S* __restrict__ past, typename Store<S>::A* __restrict__ st) {
   for (int64_t k = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; k < n;
-       k += (int64_t)gridDim.x * blockDim.x)
-    st[4 * k + 3] = Store<S>::load(past[list[k]]);
+       k += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t e = (list[k >> kshift] << kshift) + (k & ((1 << kshift) - 1));
+    st[4 * k + 3] = Store<S>::load(past[e]);
+  }
 }
 
 template <typename S, int SCHEME>
-__global__ void k_dif_update(const int64_t* __restrict__ list, int64_t n,
+__global__ void k_dif_update(const int64_t* __restrict__ list, int64_t n, int kshift,
                              const void* __restrict__ cls, int cls_bytes,
                              const typename Store<S>::A* __restrict__ dtab, const S* __restrict__ P,
                              S* __restrict__ Pp, typename Store<S>::A* __restrict__ st, int64_t X,
@@ -99,10 +103,13 @@ __global__ void k_dif_update(const int64_t* __restrict__ list, int64_t n,
   using A = typename Store<S>::A;
   using R = Rn<A>;
   using Sto = Store<S>;
+  // X, XY count field elements; the x neighbour is K elements away.
+  const int64_t ks = (int64_t)1 << kshift;
   for (int64_t k = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; k < n;
        k += (int64_t)gridDim.x * blockDim.x) {
-    const int64_t i = list[k];
-    const unsigned c = cls_bytes == 1 ? ((const uint8_t*)cls)[i] : ((const uint16_t*)cls)[i];
+    const int64_t node = list[k >> kshift];
+    const int64_t i = (node << kshift) + (k & (ks - 1));
+    const unsigned c = cls_bytes == 1 ? ((const uint8_t*)cls)[node] : ((const uint16_t*)cls)[node];
     const A* t = dtab + (int64_t)kDifClassVals * c;
     const A a = t[0], b = t[1], cc = t[2], g2 = t[3];
     A* s = st + 4 * k;
@@ -113,11 +120,11 @@ __global__ void k_dif_update(const int64_t* __restrict__ list, int64_t n,
     if (SCHEME == 0) {
       const A s6 = R::add(R::add(R::add(R::add(R::add(Sto::load(P[i + XY]), Sto::load(P[i - XY])),
                                                   Sto::load(P[i + X])), Sto::load(P[i - X])),
-                                  Sto::load(P[i + 1])), Sto::load(P[i - 1]));
+                                  Sto::load(P[i + ks])), Sto::load(P[i - ks]));
       num = R::sub(R::sub(R::add(R::mul(b, p), R::mul(l2, s6)), R::mul(cc, pp)), R::mul(g2, s1));
     } else if (SCHEME == 1) {
       const uint32_t cp = cpos[c];
-      const A xm = Sto::load(P[i - 1]), xp = Sto::load(P[i + 1]);
+      const A xm = Sto::load(P[i - ks]), xp = Sto::load(P[i + ks]);
       const A ym = Sto::load(P[i - X]), yp = Sto::load(P[i + X]);
       const A zm = Sto::load(P[i - XY]), zp = Sto::load(P[i + XY]);
       const A dx = (A)(cp & 1u), dy = (A)((cp >> 1) & 1u), dz = (A)((cp >> 2) & 1u);
@@ -140,7 +147,7 @@ __global__ void k_dif_update(const int64_t* __restrict__ list, int64_t n,
             const int mx = ((cp & 1u) && dx == ox) ? -dx : dx;
             const int my = ((cp & 2u) && dy == oy) ? -dy : dy;
             const int mz = ((cp & 4u) && dz == oz) ? -dz : dz;
-            const A v = Sto::load(P[i + mz * XY + my * X + mx]);
+            const A v = Sto::load(P[i + mz * XY + my * X + mx * ks]);
             if (nn == 1) { f1 = n1 ? v : R::add(f1, v); n1 = false; }
             else if (nn == 2) { f2 = n2 ? v : R::add(f2, v); n2 = false; }
             else { f3 = n3 ? v : R::add(f3, v); n3 = false; }
@@ -201,22 +208,24 @@ int launch_dif_t(pfdtd_domain* d, const void* cur, void* past, cudaStream_t s) {
   const size_t as = sizeof(A);
   const uint32_t* cpos = (const uint32_t*)((const char*)d->d_ctab + 3 * as * d->n_classes);
   const A l2 = (A)d->params[1];
-  const int g = grid_for(d->n_dif);
+  const int64_t n = d->n_dif * d->K;
+  const int64_t XE = d->X * d->K, XYE = d->XY * d->K;
+  const int g = grid_for(n);
   switch (d->class_scheme) {
     case PFDTD_SRL:
-      k_dif_update<S, 1><<<g, 256, 0, s>>>(d->d_dif_list, d->n_dif, d->d_cls, d->cls_bytes,
+      k_dif_update<S, 1><<<g, 256, 0, s>>>(d->d_dif_list, n, d->kshift, d->d_cls, d->cls_bytes,
                                            (const A*)d->d_dif_tab, (const S*)cur, (S*)past,
-                                           (A*)d->d_dif_state, d->X, d->XY, l2, cpos);
+                                           (A*)d->d_dif_state, XE, XYE, l2, cpos);
       break;
     case PFDTD_IWB:
-      k_dif_update<S, 2><<<g, 256, 0, s>>>(d->d_dif_list, d->n_dif, d->d_cls, d->cls_bytes,
+      k_dif_update<S, 2><<<g, 256, 0, s>>>(d->d_dif_list, n, d->kshift, d->d_cls, d->cls_bytes,
                                            (const A*)d->d_dif_tab, (const S*)cur, (S*)past,
-                                           (A*)d->d_dif_state, d->X, d->XY, l2, cpos);
+                                           (A*)d->d_dif_state, XE, XYE, l2, cpos);
       break;
     default:
-      k_dif_update<S, 0><<<g, 256, 0, s>>>(d->d_dif_list, d->n_dif, d->d_cls, d->cls_bytes,
+      k_dif_update<S, 0><<<g, 256, 0, s>>>(d->d_dif_list, n, d->kshift, d->d_cls, d->cls_bytes,
                                            (const A*)d->d_dif_tab, (const S*)cur, (S*)past,
-                                           (A*)d->d_dif_state, d->X, d->XY, l2, cpos);
+                                           (A*)d->d_dif_state, XE, XYE, l2, cpos);
   }
   count_launch();
   PFDTD_CK(cudaGetLastError());
@@ -226,9 +235,9 @@ int launch_dif_t(pfdtd_domain* d, const void* cur, void* past, cudaStream_t s) {
 template <typename S>
 int launch_init_t(pfdtd_domain* d, cudaStream_t s) {
   using A = typename Store<S>::A;
-  k_dif_init_prev<S><<<grid_for(d->n_dif), 256, 0, s>>>(d->d_dif_list, d->n_dif,
-                                                        (const S*)d->past_field(),
-                                                        (A*)d->d_dif_state);
+  const int64_t n = d->n_dif * d->K;
+  k_dif_init_prev<S><<<grid_for(n), 256, 0, s>>>(d->d_dif_list, n, d->kshift,
+                                                 (const S*)d->past_field(), (A*)d->d_dif_state);
   count_launch();
   PFDTD_CK(cudaGetLastError());
   return PFDTD_OK;
@@ -288,7 +297,7 @@ int build_dif(pfdtd_domain* d, const std::vector<uint16_t>& keys,
     PFDTD_CK(cudaMalloc(&d->d_dif_tab, tab_bytes.size()));
     PFDTD_CK(cudaMemcpyAsync(d->d_dif_tab, tab_bytes.data(), tab_bytes.size(),
                              cudaMemcpyHostToDevice, s));
-    const size_t sbytes = (size_t)total * 4 * d->arith_size();
+    const size_t sbytes = (size_t)total * d->K * 4 * d->arith_size();
     PFDTD_CK(cudaMalloc(&d->d_dif_state, sbytes));
     PFDTD_CK(cudaMemsetAsync(d->d_dif_state, 0, sbytes, s));
   }

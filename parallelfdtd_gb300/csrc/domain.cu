@@ -57,6 +57,13 @@ int64_t flat_index(const pfdtd_domain* d, int64_t x, int64_t y, int64_t z) {
   return i;
 }
 
+// Field element of node (x, y, z) and field f, or -1 (see flat_index).
+int64_t element_index(const pfdtd_domain* d, int64_t x, int64_t y, int64_t z, int64_t f) {
+  if (f < 0 || f >= d->K) return -1;
+  const int64_t i = flat_index(d, x, y, z);
+  return i < 0 ? -1 : i * d->K + f;
+}
+
 int check_domain(const pfdtd_domain* d) {
   if (!d) return fail(PFDTD_ERR_ARG, "null domain");
   return PFDTD_OK;
@@ -255,8 +262,15 @@ int pfdtd_device_count(int* count) {
 
 int pfdtd_create(int64_t dim_x, int64_t dim_y, int64_t dim_z, int precision, int device,
                  pfdtd_domain** out) {
+  return pfdtd_create_batched(dim_x, dim_y, dim_z, 1, precision, device, out);
+}
+
+int pfdtd_create_batched(int64_t dim_x, int64_t dim_y, int64_t dim_z, int fields, int precision,
+                         int device, pfdtd_domain** out) {
   if (!out) return fail(PFDTD_ERR_ARG, "null output handle");
   *out = nullptr;
+  if (fields < 1 || fields > 64 || (fields & (fields - 1)) != 0)
+    return fail(PFDTD_ERR_ARG, "fields per node must be a power of two in 1..64");
   if (dim_x < 1 || dim_y < 1 || dim_z < 3)
     return fail(PFDTD_ERR_ARG, "grid must be at least 1 x 1 x 3 nodes");
   if (dim_x > (1 << 30) || dim_y > (1 << 30) || dim_z > (1 << 30) ||
@@ -281,13 +295,17 @@ int pfdtd_create(int64_t dim_x, int64_t dim_y, int64_t dim_z, int precision, int
   d->Z = dim_z;
   d->XY = dim_x * dim_y;
   d->N = d->XY * dim_z;
+  d->K = fields;
+  d->kshift = 0;
+  while ((1 << d->kshift) < fields) ++d->kshift;
+  d->NE = d->N * fields;
   d->esize = es;
   // Margins of one row plus a 256-byte-aligned pad on both sides of each
   // field keep every row-wise access of a tile with halo inside the
   // allocation; the reference allocates N + 1 + X (cudaMesh.h:717-718).
   const int64_t align = 256 / (int64_t)es;
-  d->margin = ((dim_x + 64 + align - 1) / align) * align;
-  const size_t fbytes = (size_t)(d->N + 2 * d->margin) * es;
+  d->margin = (((dim_x + 64) * fields + align - 1) / align) * align;
+  const size_t fbytes = (size_t)(d->NE + 2 * d->margin) * es;
   auto cleanup = [&](int code, const char* msg) {
     pfdtd_destroy(d);
     return fail(code, msg);
@@ -337,6 +355,13 @@ int pfdtd_destroy(pfdtd_domain* d) {
     if (p) cudaFree(p);
   if (d->stream) cudaStreamDestroy(d->stream);
   delete d;
+  return PFDTD_OK;
+}
+
+int pfdtd_get_fields(const pfdtd_domain* d, int* fields) {
+  if (int rc = check_domain(d)) return rc;
+  if (!fields) return fail(PFDTD_ERR_ARG, "null output");
+  *fields = d->K;
   return PFDTD_OK;
 }
 
@@ -451,6 +476,11 @@ int pfdtd_set_params(pfdtd_domain* d, const double params[4]) {
 
 int pfdtd_set_sources(pfdtd_domain* d, int n, const int64_t* xyz, const int32_t* type,
                       const void* samples, int64_t n_samples) {
+  return pfdtd_set_sources_batched(d, n, xyz, nullptr, type, samples, n_samples);
+}
+
+int pfdtd_set_sources_batched(pfdtd_domain* d, int n, const int64_t* xyz, const int32_t* field,
+                              const int32_t* type, const void* samples, int64_t n_samples) {
   if (int rc = check_domain(d)) return rc;
   if (n < 0 || (n > 0 && (!xyz || !type || (!samples && n_samples > 0))) || n_samples < 0)
     return fail(PFDTD_ERR_ARG, "invalid source arrays");
@@ -466,7 +496,8 @@ int pfdtd_set_sources(pfdtd_domain* d, int n, const int64_t* xyz, const int32_t*
   d->src_type_h.assign(type, type + n);
   std::vector<int32_t> mode(n);
   for (int i = 0; i < n; ++i) {
-    d->src_idx_h[i] = flat_index(d, xyz[3 * i], xyz[3 * i + 1], xyz[3 * i + 2]);
+    d->src_idx_h[i] = element_index(d, xyz[3 * i], xyz[3 * i + 1], xyz[3 * i + 2],
+                                    field ? field[i] : 0);
     if (type[i] < 0 || type[i] > 2) return fail(PFDTD_ERR_ARG, "unknown source type");
     mode[i] = (type[i] == PFDTD_SRC_HARD || (d->quirks & PFDTD_QUIRK_SOFTSRC)) ? 0 : 1;
   }
@@ -486,6 +517,10 @@ int pfdtd_set_sources(pfdtd_domain* d, int n, const int64_t* xyz, const int32_t*
 }
 
 int pfdtd_set_receivers(pfdtd_domain* d, int n, const int64_t* xyz) {
+  return pfdtd_set_receivers_batched(d, n, xyz, nullptr);
+}
+
+int pfdtd_set_receivers_batched(pfdtd_domain* d, int n, const int64_t* xyz, const int32_t* field) {
   if (int rc = check_domain(d)) return rc;
   if (n < 0 || (n > 0 && !xyz)) return fail(PFDTD_ERR_ARG, "invalid receiver array");
   DeviceGuard g(d->device);
@@ -496,7 +531,8 @@ int pfdtd_set_receivers(pfdtd_domain* d, int n, const int64_t* xyz) {
   d->n_rec = n;
   d->rec_idx_h.assign(n, -1);
   for (int i = 0; i < n; ++i)
-    d->rec_idx_h[i] = flat_index(d, xyz[3 * i], xyz[3 * i + 1], xyz[3 * i + 2]);
+    d->rec_idx_h[i] = element_index(d, xyz[3 * i], xyz[3 * i + 1], xyz[3 * i + 2],
+                                    field ? field[i] : 0);
   PFDTD_CK(cudaMalloc((void**)&d->d_rec_idx, std::max(n, 1) * sizeof(int64_t)));
   if (n > 0)
     PFDTD_CK(cudaMemcpy(d->d_rec_idx, d->rec_idx_h.data(), n * sizeof(int64_t), cudaMemcpyHostToDevice));
@@ -620,7 +656,7 @@ int pfdtd_step(pfdtd_domain* d, int64_t step, int step_direction, void* out, int
 }
 
 static int sample_ptr(pfdtd_domain* d, int64_t x, int64_t y, int64_t z, char** p) {
-  const int64_t i = flat_index(d, x, y, z);
+  const int64_t i = element_index(d, x, y, z, 0);
   if (i < 0) return fail(PFDTD_ERR_ARG, "element outside the grid");
   *p = (char*)d->cur_field() + (size_t)i * d->esize;
   return PFDTD_OK;
@@ -678,10 +714,11 @@ int pfdtd_flip(pfdtd_domain* d) {
 int pfdtd_reset_fields(pfdtd_domain* d) {
   if (int rc = check_domain(d)) return rc;
   DeviceGuard g(d->device);
-  const size_t fbytes = (size_t)(d->N + 2 * d->margin) * d->esize;
+  const size_t fbytes = (size_t)(d->NE + 2 * d->margin) * d->esize;
   for (int i = 0; i < 2; ++i) PFDTD_CK(cudaMemsetAsync(d->field_base[i], 0, fbytes, d->stream));
   if (d->n_dif > 0)
-    PFDTD_CK(cudaMemsetAsync(d->d_dif_state, 0, (size_t)d->n_dif * 4 * d->arith_size(), d->stream));
+    PFDTD_CK(cudaMemsetAsync(d->d_dif_state, 0, (size_t)d->n_dif * d->K * 4 * d->arith_size(),
+                             d->stream));
   PFDTD_CK(cudaStreamSynchronize(d->stream));
   return PFDTD_OK;
 }
@@ -725,7 +762,7 @@ int pfdtd_download_field(pfdtd_domain* d, int which, void* host) {
   if (!host) return fail(PFDTD_ERR_ARG, "null host buffer");
   DeviceGuard g(d->device);
   PFDTD_CK(cudaStreamSynchronize(d->stream));
-  PFDTD_CK(cudaMemcpy(host, p, (size_t)d->N * d->esize, cudaMemcpyDeviceToHost));
+  PFDTD_CK(cudaMemcpy(host, p, (size_t)d->NE * d->esize, cudaMemcpyDeviceToHost));
   return PFDTD_OK;
 }
 
@@ -735,7 +772,7 @@ int pfdtd_upload_field(pfdtd_domain* d, int which, const void* host) {
   if (!host) return fail(PFDTD_ERR_ARG, "null host buffer");
   DeviceGuard g(d->device);
   PFDTD_CK(cudaStreamSynchronize(d->stream));
-  PFDTD_CK(cudaMemcpy(p, host, (size_t)d->N * d->esize, cudaMemcpyHostToDevice));
+  PFDTD_CK(cudaMemcpy(p, host, (size_t)d->NE * d->esize, cudaMemcpyHostToDevice));
   return PFDTD_OK;
 }
 

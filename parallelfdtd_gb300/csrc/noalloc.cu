@@ -50,7 +50,7 @@ int scratch_address(int device, void** out) {
 template <typename S>
 __global__ void k_slice_into(const S* __restrict__ P, const uint8_t* __restrict__ pos, int X,
                              int Y, int Z, int orientation, int64_t slice,
-                             float* __restrict__ p_out, uint8_t* __restrict__ pos_out) {
+                             float* __restrict__ p_out, uint8_t* __restrict__ pos_out, int K) {
   const int64_t w = orientation == 2 ? Y : X;
   const int64_t h = orientation == 0 ? Y : Z;
   const int64_t XY = (int64_t)X * Y;
@@ -62,7 +62,7 @@ __global__ void k_slice_into(const S* __restrict__ P, const uint8_t* __restrict_
     else if (orientation == 1) src = v * XY + slice * X + u;
     else src = v * XY + u * X + slice;
     const bool keep = orientation == 0 || v < Z - 1;
-    p_out[i] = keep ? (float)Store<S>::load(P[src]) : 0.f;
+    p_out[i] = keep ? (float)Store<S>::load(P[src * K]) : 0.f;
     pos_out[i] = keep ? pos[src] : 0;
   }
 }
@@ -102,10 +102,10 @@ extern "C" int pfdtd_capture_slice_noalloc(pfdtd_domain* d, int orientation, int
     const void* cur = d->cur_field();
     const int X = (int)d->X, Y = (int)d->Y, Z = (int)d->Z;
     switch (d->precision) {
-      case PFDTD_F32: k_slice_into<float><<<grid, 256, 0, s>>>((const float*)cur, d->d_pos, X, Y, Z, orientation, slice, dp, dq); break;
-      case PFDTD_F64: k_slice_into<double><<<grid, 256, 0, s>>>((const double*)cur, d->d_pos, X, Y, Z, orientation, slice, dp, dq); break;
-      case PFDTD_F16: k_slice_into<__half><<<grid, 256, 0, s>>>((const __half*)cur, d->d_pos, X, Y, Z, orientation, slice, dp, dq); break;
-      default: k_slice_into<__nv_bfloat16><<<grid, 256, 0, s>>>((const __nv_bfloat16*)cur, d->d_pos, X, Y, Z, orientation, slice, dp, dq); break;
+      case PFDTD_F32: k_slice_into<float><<<grid, 256, 0, s>>>((const float*)cur, d->d_pos, X, Y, Z, orientation, slice, dp, dq, d->K); break;
+      case PFDTD_F64: k_slice_into<double><<<grid, 256, 0, s>>>((const double*)cur, d->d_pos, X, Y, Z, orientation, slice, dp, dq, d->K); break;
+      case PFDTD_F16: k_slice_into<__half><<<grid, 256, 0, s>>>((const __half*)cur, d->d_pos, X, Y, Z, orientation, slice, dp, dq, d->K); break;
+      default: k_slice_into<__nv_bfloat16><<<grid, 256, 0, s>>>((const __nv_bfloat16*)cur, d->d_pos, X, Y, Z, orientation, slice, dp, dq, d->K); break;
     }
     count_launch();
     cudaError_t e = cudaGetLastError();

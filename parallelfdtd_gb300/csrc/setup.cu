@@ -83,7 +83,7 @@ __global__ void k_pad(const uint8_t* __restrict__ in, int64_t in_len, uint32_t d
 template <typename S>
 __global__ void k_slice(const S* __restrict__ P, const uint8_t* __restrict__ pos, int X, int Y,
                         int Z, int orientation, int64_t slice, float* __restrict__ p_out,
-                        uint8_t* __restrict__ pos_out) {
+                        uint8_t* __restrict__ pos_out, int K) {
   const int64_t w = orientation == 0 ? X : (orientation == 1 ? X : Y);
   const int64_t h = orientation == 0 ? Y : Z;
   const int64_t XY = (int64_t)X * Y;
@@ -95,7 +95,7 @@ __global__ void k_slice(const S* __restrict__ P, const uint8_t* __restrict__ pos
     else if (orientation == 1) src = v * XY + slice * X + u;
     else src = v * XY + u * X + slice;
     const bool keep = orientation == 0 || v < Z - 1;
-    if (p_out) p_out[i] = keep ? (float)Store<S>::load(P[src]) : 0.f;
+    if (p_out) p_out[i] = keep ? (float)Store<S>::load(P[src * K]) : 0.f;
     if (pos_out) pos_out[i] = keep ? pos[src] : 0;
   }
 }
@@ -188,10 +188,10 @@ int pfdtd_capture_slice(pfdtd_domain* d, int orientation, int64_t slice, float* 
   PFDTD_CK(cudaMallocAsync((void**)&dq, n, s));
   const void* cur = d->cur_field();
   switch (d->precision) {
-    case PFDTD_F32: k_slice<float><<<grid_for(n), 256, 0, s>>>((const float*)cur, d->d_pos, (int)d->X, (int)d->Y, (int)d->Z, orientation, slice, dp, dq); break;
-    case PFDTD_F64: k_slice<double><<<grid_for(n), 256, 0, s>>>((const double*)cur, d->d_pos, (int)d->X, (int)d->Y, (int)d->Z, orientation, slice, dp, dq); break;
-    case PFDTD_F16: k_slice<__half><<<grid_for(n), 256, 0, s>>>((const __half*)cur, d->d_pos, (int)d->X, (int)d->Y, (int)d->Z, orientation, slice, dp, dq); break;
-    default: k_slice<__nv_bfloat16><<<grid_for(n), 256, 0, s>>>((const __nv_bfloat16*)cur, d->d_pos, (int)d->X, (int)d->Y, (int)d->Z, orientation, slice, dp, dq); break;
+    case PFDTD_F32: k_slice<float><<<grid_for(n), 256, 0, s>>>((const float*)cur, d->d_pos, (int)d->X, (int)d->Y, (int)d->Z, orientation, slice, dp, dq, d->K); break;
+    case PFDTD_F64: k_slice<double><<<grid_for(n), 256, 0, s>>>((const double*)cur, d->d_pos, (int)d->X, (int)d->Y, (int)d->Z, orientation, slice, dp, dq, d->K); break;
+    case PFDTD_F16: k_slice<__half><<<grid_for(n), 256, 0, s>>>((const __half*)cur, d->d_pos, (int)d->X, (int)d->Y, (int)d->Z, orientation, slice, dp, dq, d->K); break;
+    default: k_slice<__nv_bfloat16><<<grid_for(n), 256, 0, s>>>((const __nv_bfloat16*)cur, d->d_pos, (int)d->X, (int)d->Y, (int)d->Z, orientation, slice, dp, dq, d->K); break;
   }
   count_launch();
   cudaError_t e = cudaGetLastError();

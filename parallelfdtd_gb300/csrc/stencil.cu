@@ -29,7 +29,7 @@ template <typename S, typename C, int SCHEME>
 __global__ void __launch_bounds__(kBX * kBY)
 k_update_zmarch(const C* __restrict__ cls, const S* __restrict__ P, S* __restrict__ Pp,
                 ClassTab<typename Store<S>::A> tab, int X, int Y, int64_t XY, int z_last,
-                int zc, typename Store<S>::A l2) {
+                int zc, typename Store<S>::A l2, int ks, int kshift) {
   using A = typename Store<S>::A;
   using R = Rn<A>;
   using St = Store<S>;
@@ -46,6 +46,8 @@ k_update_zmarch(const C* __restrict__ cls, const S* __restrict__ P, S* __restric
     }
     __syncthreads();
   }
+  // X and XY count field elements (nodes times ks fields); ks is the element
+  // distance of the x neighbour.
   const int x = blockIdx.x * kBX + threadIdx.x;
   const int y = blockIdx.y * kBY + threadIdx.y;
   const int z0 = 1 + blockIdx.z * zc;
@@ -56,11 +58,11 @@ k_update_zmarch(const C* __restrict__ cls, const S* __restrict__ P, S* __restric
   A pc = St::load(P[idx]);
   for (int z = z0; z < z1; ++z, idx += XY) {
     const A pn = St::load(P[idx + XY]);
-    const A xm = St::load(P[idx - 1]);
-    const A xp = St::load(P[idx + 1]);
+    const A xm = St::load(P[idx - ks]);
+    const A xp = St::load(P[idx + ks]);
     const A ym = St::load(P[idx - X]);
     const A yp = St::load(P[idx + X]);
-    const unsigned c = cls[idx];
+    const unsigned c = cls[idx >> kshift];
     const A pp = St::load(Pp[idx]);
     A ca, cb, cc;
     uint32_t cp;
@@ -104,7 +106,8 @@ k_update_zmarch(const C* __restrict__ cls, const S* __restrict__ P, S* __restric
 template <typename S, typename C>
 __global__ void __launch_bounds__(kBX * kBY)
 k_update_iwb(const C* __restrict__ cls, const S* __restrict__ P, S* __restrict__ Pp,
-             ClassTab<typename Store<S>::A> tab, int X, int Y, int64_t XY, int z_last, int zc) {
+             ClassTab<typename Store<S>::A> tab, int X, int Y, int64_t XY, int z_last, int zc,
+             int ks, int kshift) {
   using A = typename Store<S>::A;
   using R = Rn<A>;
   using St = Store<S>;
@@ -120,14 +123,14 @@ k_update_iwb(const C* __restrict__ cls, const S* __restrict__ P, S* __restrict__
     for (int dy = -1; dy <= 1; ++dy)
 #pragma unroll
       for (int dx = -1; dx <= 1; ++dx)
-        v[slot][dy + 1][dx + 1] = St::load(__ldg(P + base + (int64_t)dy * X + dx));
+        v[slot][dy + 1][dx + 1] = St::load(__ldg(P + base + (int64_t)dy * X + dx * ks));
   };
   int64_t idx = (int64_t)z0 * XY + (int64_t)y * X + x;
   load_plane(0, idx - XY);
   load_plane(1, idx);
   for (int z = z0; z < z1; ++z, idx += XY) {
     load_plane(2, idx + XY);
-    const unsigned c = cls[idx];
+    const unsigned c = cls[idx >> kshift];
     const A pp = St::load(Pp[idx]);
     const A ca = __ldg(tab.a + c), cb = __ldg(tab.b + c), cc = __ldg(tab.c + c);
     const uint32_t cp = __ldg(tab.pos + c);
@@ -253,7 +256,8 @@ int launch_update_t(pfdtd_domain* d, const void* cur, void* past, cudaStream_t s
   using A = typename Store<S>::A;
   const int64_t nz = d->Z - 2;
   if (nz <= 0) return PFDTD_OK;
-  const int gx = (int)((d->X + kBX - 1) / kBX);
+  const int64_t XE = d->X * d->K;
+  const int gx = (int)((XE + kBX - 1) / kBX);
   const int gy = (int)((d->Y + kBY - 1) / kBY);
   // Enough z-chunks for several waves of 8 resident blocks on each SM.
   const int64_t target = (int64_t)d->sm_count * 8 * 4;
@@ -266,8 +270,8 @@ int launch_update_t(pfdtd_domain* d, const void* cur, void* past, cudaStream_t s
                   (const A*)(tb + 2 * as * d->n_classes),
                   (const uint32_t*)(tb + 3 * as * d->n_classes), d->n_classes};
   k_update_zmarch<S, C, SCHEME><<<dim3(gx, gy, gz), dim3(kBX, kBY), 0, s>>>(
-      (const C*)d->d_cls, (const S*)cur, (S*)past, tab, (int)d->X, (int)d->Y, d->XY,
-      (int)(d->Z - 1), (int)zc, (A)d->params[1]);
+      (const C*)d->d_cls, (const S*)cur, (S*)past, tab, (int)XE, (int)d->Y, d->XY * d->K,
+      (int)(d->Z - 1), (int)zc, (A)d->params[1], d->K, d->kshift);
   count_launch();
   PFDTD_CK(cudaGetLastError());
   return PFDTD_OK;
@@ -278,7 +282,8 @@ int launch_iwb_t(pfdtd_domain* d, const void* cur, void* past, cudaStream_t s) {
   using A = typename Store<S>::A;
   const int64_t nz = d->Z - 2;
   if (nz <= 0) return PFDTD_OK;
-  const int gx = (int)((d->X + kBX - 1) / kBX);
+  const int64_t XE = d->X * d->K;
+  const int gx = (int)((XE + kBX - 1) / kBX);
   const int gy = (int)((d->Y + kBY - 1) / kBY);
   const int64_t target = (int64_t)d->sm_count * 8 * 4;
   int64_t zc = std::max<int64_t>(8, (nz * (int64_t)gx * gy + target - 1) / target);
@@ -290,8 +295,8 @@ int launch_iwb_t(pfdtd_domain* d, const void* cur, void* past, cudaStream_t s) {
                   (const A*)(tb + 2 * as * d->n_classes),
                   (const uint32_t*)(tb + 3 * as * d->n_classes), d->n_classes};
   k_update_iwb<S, C><<<dim3(gx, gy, gz), dim3(kBX, kBY), 0, s>>>(
-      (const C*)d->d_cls, (const S*)cur, (S*)past, tab, (int)d->X, (int)d->Y, d->XY,
-      (int)(d->Z - 1), (int)zc);
+      (const C*)d->d_cls, (const S*)cur, (S*)past, tab, (int)XE, (int)d->Y, d->XY * d->K,
+      (int)(d->Z - 1), (int)zc, d->K, d->kshift);
   count_launch();
   PFDTD_CK(cudaGetLastError());
   return PFDTD_OK;

@@ -524,6 +524,7 @@ int launch_tma_s<double>(pfdtd_domain* d, const void* cur, void* past, cudaStrea
 int tma_tile_count() { return 9; }
 
 bool tma_supported(const pfdtd_domain* d) {
+  if (d->K != 1) return false;
   if ((d->X * (int64_t)d->esize) % 16 != 0) return false;
   if ((d->X * (int64_t)d->cls_bytes) % 16 != 0) return false;
   if (d->Y * d->Z >= ((int64_t)1 << 31)) return false;

@@ -47,14 +47,16 @@ def _ptr(a: np.ndarray) -> C.c_void_p:
 class Domain:
     """One FDTD grid on one GPU (pfdtd_create ... pfdtd_destroy)."""
 
-    def __init__(self, dims: Sequence[int], precision="f32", device: int = 0):
+    def __init__(self, dims: Sequence[int], precision="f32", device: int = 0, fields: int = 1):
         self._lib = L.load()
         X, Y, Z = (int(v) for v in dims)
         self.dims = (X, Y, Z)
         self.n = X * Y * Z
+        self.fields = int(fields)
         self.precision = precision_code(precision)
         h = C.c_void_p()
-        L.call("pfdtd_create", X, Y, Z, self.precision, int(device), C.byref(h))
+        L.call("pfdtd_create_batched", X, Y, Z, self.fields, self.precision, int(device),
+               C.byref(h))
         self._h = h
         self.n_rec = 0
         self.n_src = 0
@@ -148,22 +150,29 @@ class Domain:
         p = np.ascontiguousarray(default_params() if params is None else params, dtype=np.float64)
         L.call("pfdtd_set_params", self.handle, p.ctypes.data_as(C.POINTER(C.c_double)))
 
-    def set_sources(self, xyz: np.ndarray, types: Sequence[int], samples: np.ndarray) -> None:
+    def set_sources(self, xyz: np.ndarray, types: Sequence[int], samples: np.ndarray,
+                    fields: Optional[Sequence[int]] = None) -> None:
+        """Sources at element coordinates; `fields` picks the field each one
+        drives (batched domains; default field 0)."""
         xyz = np.ascontiguousarray(np.asarray(xyz, dtype=np.int64).reshape(-1, 3))
         types = np.ascontiguousarray(np.asarray(types, dtype=np.int32).reshape(-1))
+        f = np.ascontiguousarray(np.zeros(xyz.shape[0], np.int32) if fields is None
+                                 else np.asarray(fields, dtype=np.int32).reshape(-1))
         dt = arith_dtype(self.precision)
         smp = np.ascontiguousarray(np.asarray(samples, dtype=dt).reshape(xyz.shape[0], -1))
         self.n_src = xyz.shape[0]
-        L.call("pfdtd_set_sources", self.handle, xyz.shape[0],
-               xyz.ctypes.data_as(C.POINTER(C.c_int64)),
+        L.call("pfdtd_set_sources_batched", self.handle, xyz.shape[0],
+               xyz.ctypes.data_as(C.POINTER(C.c_int64)), f.ctypes.data_as(C.POINTER(C.c_int32)),
                types.ctypes.data_as(C.POINTER(C.c_int32)), _ptr(smp), smp.shape[1])
-        self._src_keep = (xyz, types, smp)
+        self._src_keep = (xyz, types, smp, f)
 
-    def set_receivers(self, xyz: np.ndarray) -> None:
+    def set_receivers(self, xyz: np.ndarray, fields: Optional[Sequence[int]] = None) -> None:
         xyz = np.ascontiguousarray(np.asarray(xyz, dtype=np.int64).reshape(-1, 3))
+        f = np.ascontiguousarray(np.zeros(xyz.shape[0], np.int32) if fields is None
+                                 else np.asarray(fields, dtype=np.int32).reshape(-1))
         self.n_rec = xyz.shape[0]
-        L.call("pfdtd_set_receivers", self.handle, xyz.shape[0],
-               xyz.ctypes.data_as(C.POINTER(C.c_int64)))
+        L.call("pfdtd_set_receivers_batched", self.handle, xyz.shape[0],
+               xyz.ctypes.data_as(C.POINTER(C.c_int64)), f.ctypes.data_as(C.POINTER(C.c_int32)))
 
     # -- running ---------------------------------------------------------
     def run(self, steps: int, interrupt: Optional[Callable[[], bool]] = None,
@@ -205,14 +214,15 @@ class Domain:
         L.call("pfdtd_reset_fields", self.handle)
 
     def download_field(self, which: int = L.FIELD_CURRENT) -> np.ndarray:
-        a = np.empty(self.n, dtype=_STORE_DTYPE[self.precision])
+        """The whole field, N * fields elements (node-major)."""
+        a = np.empty(self.n * self.fields, dtype=_STORE_DTYPE[self.precision])
         L.call("pfdtd_download_field", self.handle, int(which), _ptr(a))
         return a
 
     def upload_field(self, which: int, data: np.ndarray) -> None:
         a = np.ascontiguousarray(data, dtype=_STORE_DTYPE[self.precision]).reshape(-1)
-        if a.size != self.n:
-            raise ValueError("field must hold X*Y*Z values")
+        if a.size != self.n * self.fields:
+            raise ValueError("field must hold X*Y*Z*fields values")
         L.call("pfdtd_upload_field", self.handle, int(which), _ptr(a))
 
     def capture_slice(self, orientation: int, slice_idx: int) -> Tuple[np.ndarray, np.ndarray]:

@@ -532,3 +532,39 @@ def test_dif_boundaries_bit_identical(gpu, O, prec, scheme):
     assert n_dif == int(np.count_nonzero(inside & flagged & boundary)) > 0
     assert_parity(g, r, prec)
     assert np.array_equal(P, rP)
+
+
+@pytest.mark.parametrize("fields,prec,scheme", [(4, "f32", "forward"), (16, "f32", "forward"),
+                                                (16, "f16", "forward"), (4, "f64", "centred"),
+                                                (8, "f32", "iwb")])
+def test_batched_fields_equal_independent_runs(gpu, O, fields, prec, scheme):
+    """K fields sharing one geometry: field f equals an independent oracle run
+    of field f's source (bit-identical), with DIF boundaries on some materials."""
+    from parallelfdtd_gb300 import materials
+    room = rooms.boxes_room((64, 48, 40), n_boxes=5, edge=(5, 14), n_materials=6, seed=21)
+    steps = 120
+    pulse = rooms.gaussian_pulse(steps, 3.0)
+    srcs = room.random_air_nodes(fields, seed=5)
+    recs = room.random_air_nodes(2 * fields, seed=6)
+    rec_fields = [i // 2 for i in range(2 * fields)]
+    params = default_params(scheme=scheme)
+    code = {"forward": 0, "centred": 2, "iwb": 3}[scheme]
+    flags = np.array([m % 2 for m in range(6)], np.int32)
+    table = materials.dif_table(materials.positive_real_filters(6, 2, seed=3), 2)
+    with Domain(room.dims, prec, fields=fields) as d:
+        d.set_voxels(room.bid, room.mat, centred=(scheme != "forward"))
+        d.set_materials(room.admittance)
+        d.set_params(params)
+        d.set_scheme(scheme)
+        d.set_dif_filters(flags, table)
+        d.set_sources(srcs, [1] * fields, np.repeat(pulse[None], fields, axis=0),
+                      fields=list(range(fields)))
+        d.set_receivers(recs, fields=rec_fields)
+        g, _, _ = d.run(steps)
+    pos, mat = O.encode_nodes(room.bid, room.mat, scheme != "forward")
+    for f in range(fields):
+        r, _, _ = O.run(pos, mat, room.dims, room.admittance, params, [room.flat(*srcs[f])], [1],
+                        pulse[None], [room.flat(*recs[2 * f]), room.flat(*recs[2 * f + 1])], steps,
+                        scheme=code, double=(prec == "f64"),
+                        storage=(prec if prec in ("f16", "bf16") else None), dif=(flags, table))
+        assert np.array_equal(g[2 * f:2 * f + 2], r), f"field {f}"
