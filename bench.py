@@ -44,7 +44,6 @@ METRIC = "node-updates/s"
 DIMS = (512, 384, 256)
 FDTD_STEPS = 2000
 N_REC = 8
-BYTES_PER_UPDATE = {"f32": 14, "f64": 26, "f16": 8, "bf16": 8}
 
 
 def parse():
@@ -58,6 +57,9 @@ def parse():
     p.add_argument("--dims", type=str, default=None, help="X,Y,Z override (testing)")
     p.add_argument("--no-cpu-baseline", action="store_true")
     p.add_argument("--cpu-seconds", type=float, default=12.0)
+    p.add_argument("--fields", type=int, default=1,
+                   help="batched: K source fields sharing the room (the 384x320x256 multi-source "
+                        "room, 4 receivers per field, when --dims is not given)")
     return p.parse_args()
 
 
@@ -68,13 +70,30 @@ def dist_env():
     return world, rank, local
 
 
-def make_room(dims):
+C4_DIMS = (384, 320, 256)
+C4_STEPS = 4000
+
+
+def make_room(dims, fields=1):
+    """The benchmark room; for fields > 1 one seeded air source per field and
+    4 receivers per field (the multi-source workload)."""
     from parallelfdtd_gb300 import rooms
     room = rooms.boxes_room(dims, n_boxes=40, edge=(8, 64), n_materials=20,
                             admittance_range=(0.01, 0.9), seed=2)
-    src = room.random_air_nodes(1, seed=8)[0]
-    rec = room.random_air_nodes(N_REC, seed=9)
-    return room, src, rec
+    if fields == 1:
+        src = [room.random_air_nodes(1, seed=8)[0]]
+        rec = room.random_air_nodes(N_REC, seed=9)
+        return room, src, rec, [0], [0] * N_REC
+    src = room.random_air_nodes(fields, seed=8)
+    rec = room.random_air_nodes(4 * fields, seed=9)
+    return room, src, rec, list(range(fields)), [i // 4 for i in range(4 * fields)]
+
+
+def bytes_per_update(prec, fields):
+    """Algorithmic bytes per node-update: 2 geometry bytes per node shared by
+    the fields, read P^n and P^{n-1}, write P^{n+1} per field."""
+    s = {"f32": 4, "f64": 8, "f16": 2, "bf16": 2}[prec]
+    return (2 + 3 * s * fields) / fields
 
 
 class ClockSampler:
@@ -139,18 +158,19 @@ def peak_hbm():
         return 6800.0, "fallback"
 
 
-def traffic_per_launch(prec):
+def traffic_per_launch(prec, fields=1):
     """DRAM bytes per update-kernel launch from the committed ncu summary."""
     path = os.path.join(ROOT, "profiles", "traffic.json")
     try:
         with open(path) as f:
             t = json.load(f)
-        return t.get(f"update_{prec}_bytes_per_launch")
+        return t.get(f"update_{prec}_bytes_per_launch" if fields == 1 else
+                     f"update_{prec}_k{fields}_bytes_per_launch")
     except Exception:
         return None
 
 
-def cpu_baseline(room, src, rec, budget_s: float):
+def cpu_baseline(room, src, rec, budget_s: float, fields=1):
     """Oracle on all host cores over a bounded number of steps of the room."""
     import numpy as np
     from oracle import oracle as O
@@ -160,8 +180,8 @@ def cpu_baseline(room, src, rec, budget_s: float):
     X, Y, Z = room.dims
     threads = O.max_threads()
     args = (pos, mat, room.dims, room.admittance, default_params(),
-            [room.flat(*src)], [1])
-    rec_idx = [room.flat(*r) for r in rec]
+            [room.flat(*src[0])], [1])
+    rec_idx = [room.flat(*r) for r in rec[:N_REC]]
     probe = 2
     t0 = time.perf_counter()
     O.run(*args, rooms.impulse(probe)[None], rec_idx, probe, threads=threads)
@@ -172,7 +192,7 @@ def cpu_baseline(room, src, rec, budget_s: float):
     dt = time.perf_counter() - t0
     return {"value": X * Y * (Z - 2) * n / dt, "unit": METRIC, "cores": threads,
             "kind": "port",
-            "sample": f"{X}x{Y}x{Z} room, {n} of the {FDTD_STEPS} leapfrog steps, FP32 "
+            "sample": f"{X}x{Y}x{Z} room, {n} leapfrog steps of one field, FP32 "
                       f"SRL forward, {threads} OpenMP threads"}
 
 
@@ -180,8 +200,9 @@ def run_reference_arm(a, world, rank):
     """--impl reference: the CPU restatement of the reference's update rule."""
     if rank != 0:
         return 0
-    dims = tuple(int(v) for v in a.dims.split(",")) if a.dims else DIMS
-    room, src, rec = make_room(dims)
+    dims = tuple(int(v) for v in a.dims.split(",")) if a.dims else (C4_DIMS if a.fields > 1 else DIMS)
+    room, src, rec, _, _ = make_room(dims)
+    src = src[0]
     import numpy as np
     from oracle import oracle as O
     from parallelfdtd_gb300 import rooms
@@ -235,24 +256,27 @@ def main():
     if world > 1:
         import torch.distributed as dist
         dist.init_process_group("nccl" if torch.cuda.is_available() else "gloo")
-    dims = tuple(int(v) for v in a.dims.split(",")) if a.dims else DIMS
-    S = a.fdtd_steps
-    room, src, rec = make_room(dims)
+    K = a.fields
+    dims = tuple(int(v) for v in a.dims.split(",")) if a.dims else (C4_DIMS if K > 1 else DIMS)
+    S = a.fdtd_steps if (a.fdtd_steps != FDTD_STEPS or K == 1) else C4_STEPS
+    room, src, rec, src_f, rec_f = make_room(dims, K)
+    n_rec = len(rec)
     X, Y, Z = dims
-    updates_per_run = X * Y * (Z - 2) * S
+    updates_per_run = X * Y * (Z - 2) * S * K
     prec = a.precision
-    samples = rooms.impulse(S)[None].astype(np.float64 if prec == "f64" else np.float32)
+    samples = np.repeat(rooms.impulse(S)[None], len(src), axis=0).astype(
+        np.float64 if prec == "f64" else np.float32)
     esize = {"f32": 4, "f64": 8, "f16": 2, "bf16": 2}[prec]
-    d = Domain(dims, prec, device=local)
+    d = Domain(dims, prec, device=local, fields=K)
     d.set_voxels(room.bid, room.mat, centred=False)
     pos_host, mat_host = d.get_nodes()
     d.set_materials(room.admittance)
     d.set_params(default_params())
     d.set_scheme("forward")
-    d.set_sources([src], [1], samples)
-    d.set_receivers(rec)
+    d.set_sources(src, [1] * len(src), samples, fields=src_f)
+    d.set_receivers(rec, fields=rec_f)
     stream = torch.cuda.ExternalStream(d.stream_ptr())
-    d_out = torch.zeros(N_REC * S, dtype=torch.float64 if prec == "f64" else torch.float32,
+    d_out = torch.zeros(n_rec * S, dtype=torch.float64 if prec == "f64" else torch.float32,
                         device=f"cuda:{local}")
 
     def barrier():
@@ -300,23 +324,23 @@ def main():
     torch.cuda.synchronize()
     kms = k0.elapsed_time(k1) / prof_iters
     nodes = X * Y * (Z - 2)
-    algo_bytes = BYTES_PER_UPDATE[prec] * nodes
+    bpu = bytes_per_update(prec, K)
+    algo_bytes = bpu * nodes * K
     achieved = algo_bytes / (kms * 1e-3) / 1e9
     peak, peak_kind = peak_hbm()
-    traffic = traffic_per_launch(prec)
+    traffic = traffic_per_launch(prec, K)
 
     # ---- end to end through the C ABI with host buffers ------------------------
-    out_host = np.zeros((N_REC, S), dtype=np.float64 if prec == "f64" else np.float32)
-    sec = C.c_double()
+    out_host = np.zeros((n_rec, S), dtype=np.float64 if prec == "f64" else np.float32)
     for _ in range(max(1, a.warmup)):
         d.set_nodes(pos_host, mat_host)
-        d.set_sources([src], [1], samples)
+        d.set_sources(src, [1] * len(src), samples, fields=src_f)
         d.run(S, out=out_host)
     barrier()
     t0 = time.perf_counter()
     for _ in range(a.steps):
         d.set_nodes(pos_host, mat_host)
-        d.set_sources([src], [1], samples)
+        d.set_sources(src, [1] * len(src), samples, fields=src_f)
         d.run(S, out=out_host)
     barrier()
     e2e_s = (time.perf_counter() - t0) / a.steps
@@ -327,23 +351,26 @@ def main():
         e2e_s = float(t.item())
     e2e = {"value": updates_per_run * world / e2e_s, "unit": METRIC,
            "h2d_bytes_per_step": int(2 * room.n_nodes + samples.nbytes),
-           "d2h_bytes_per_step": int(N_REC * S * (8 if prec == "f64" else 4))}
+           "d2h_bytes_per_step": int(n_rec * S * (8 if prec == "f64" else 4))}
 
     if rank == 0:
         base = None
         if not a.no_cpu_baseline and world == 1:
             base = cpu_baseline(room, src, rec, a.cpu_seconds)
+        src_txt = (f"soft impulse, {N_REC} air receivers" if K == 1 else
+                   f"{K} fields (one soft impulse each), 4 receivers per field")
         line = {
             "metric": METRIC, "value": value, "unit": METRIC, "n_gpus": world,
             "steps": a.steps, "warmup": a.warmup, "ms_per_step": ms,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
             "dtype": prec, "data": "synthetic",
             "config": {"workload": f"boxes room {X}x{Y}x{Z}, 40 boxes (edges 8-64), 20 materials "
-                                   f"U(0.01,0.9), soft impulse, {N_REC} air receivers, {S} "
-                                   f"leapfrog steps, SRL forward, {prec}",
-                       "fdtd_steps_per_step": S, "nodes": X * Y * Z,
+                                   f"U(0.01,0.9), {src_txt}, {S} leapfrog steps, SRL forward, "
+                                   f"{prec}",
+                       "fdtd_steps_per_step": S, "nodes": X * Y * Z, "fields": K,
+                       "bytes_per_update": bpu,
                        "parallelism": f"replicas x{world}",
-                       "l2": f"inputs larger than L2 (fields 2 x {X * Y * Z * esize / 1e6:.0f} MB "
+                       "l2": f"inputs larger than L2 (fields 2 x {X * Y * Z * K * esize / 1e6:.0f} MB "
                              f"+ {X * Y * Z / 1e6:.0f} MB class ids)"},
             "e2e": e2e,
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",

@@ -145,6 +145,28 @@ __device__ __forceinline__ V4<__half> lds4(const __half* p) { return lds4_16<__h
 __device__ __forceinline__ V4<__nv_bfloat16> lds4(const __nv_bfloat16* p) {
   return lds4_16<__nv_bfloat162>(p);
 }
+__device__ __forceinline__ V4<float> ldg4(const float* p) {
+  const float4 t = __ldg(reinterpret_cast<const float4*>(p));
+  return V4<float>{{t.x, t.y, t.z, t.w}};
+}
+__device__ __forceinline__ V4<double> ldg4(const double* p) {
+  const double2 a = __ldg(reinterpret_cast<const double2*>(p));
+  const double2 b = __ldg(reinterpret_cast<const double2*>(p) + 1);
+  return V4<double>{{a.x, a.y, b.x, b.y}};
+}
+template <typename H2, typename S>
+__device__ __forceinline__ V4<S> ldg4_16(const S* p) {
+  const uint2 t = __ldg(reinterpret_cast<const uint2*>(p));
+  H2 a, b;
+  memcpy(&a, &t.x, 4);
+  memcpy(&b, &t.y, 4);
+  return V4<S>{{a.x, a.y, b.x, b.y}};
+}
+__device__ __forceinline__ V4<__half> ldg4(const __half* p) { return ldg4_16<__half2>(p); }
+__device__ __forceinline__ V4<__nv_bfloat16> ldg4(const __nv_bfloat16* p) {
+  return ldg4_16<__nv_bfloat162>(p);
+}
+
 template <typename S>
 __device__ __forceinline__ void stg4_16(S* p, const S (&v)[4]) {
   uint16_t u[4];
@@ -161,12 +183,16 @@ __device__ __forceinline__ void stg4(double* p, const double (&v)[4]) {
   reinterpret_cast<double2*>(p)[1] = make_double2(v[2], v[3]);
 }
 
-template <typename S, typename C, int SCHEME, typename Lay>
+// BATCHED: the field holds K = 1 << kshift interleaved fields per node (K a
+// multiple of 4): X and XY count elements, a consumer thread's 4 elements are
+// 4 fields of one node, the x neighbours are K elements away and the class
+// ids (one per node) come in a box K times narrower.
+template <typename S, typename C, int SCHEME, typename Lay, bool BATCHED = false>
 __global__ void __launch_bounds__(Lay::THREADS)
 k_update_tma(const __grid_constant__ CUtensorMap map_cur, const __grid_constant__ CUtensorMap map_past,
              const __grid_constant__ CUtensorMap map_cls, const S* __restrict__ P,
              S* __restrict__ Pp, ClassTab<typename Store<S>::A> tab, int X, int Y, int64_t XY,
-             int z_last, int zc, typename Store<S>::A l2, int* __restrict__ err) {
+             int z_last, int zc, typename Store<S>::A l2, int* __restrict__ err, int kshift = 0) {
   using A = typename Store<S>::A;
   using R = Rn<A>;
   using St = Store<S>;
@@ -226,13 +252,13 @@ k_update_tma(const __grid_constant__ CUtensorMap map_cur, const __grid_constant_
         const uint32_t bar = bar_full + 8 * slot;
         const int zp = z0 - 1 + k;
         uint32_t bytes = Lay::P_BYTES;
-        if (k >= 2) bytes += Lay::PP_BYTES + Lay::CL_BYTES;
+        if (k >= 2) bytes += Lay::PP_BYTES + (Lay::CL_BYTES >> kshift);
         mbar_expect_tx(bar, bytes);
         tma_load_2d(smem_u32(st + Lay::P_OFF), &map_cur, x0 - H, zp * Y + y0 - 1, bar);
         if (k >= 2) {
           const int zc_ = z0 + k - 2;
           tma_load_2d(smem_u32(st + Lay::PP_OFF), &map_past, x0, zc_ * Y + y0, bar);
-          tma_load_2d(smem_u32(st + Lay::CL_OFF), &map_cls, x0, zc_ * Y + y0, bar);
+          tma_load_2d(smem_u32(st + Lay::CL_OFF), &map_cls, x0 >> kshift, zc_ * Y + y0, bar);
         }
         issued = k + 1;
       }
@@ -274,13 +300,24 @@ k_update_tma(const __grid_constant__ CUtensorMap map_cur, const __grid_constant_
       const V4<S> vzm = lds4(Pm + si);
       const V4<S> vzp = lds4(Pn + si);
       const V4<S> vpp = lds4(Pq + ly * kTX + lx);
-      A left, right;
-      if (x == 0 || (!Lay::XHALO && lx == 0)) left = St::load(P[idx - 1]);
-      else left = St::load(Pc[si - 1]);
-      if (x + kVec == X || (!Lay::XHALO && lx + kVec == kTX)) right = St::load(P[idx + kVec]);
-      else right = St::load(Pc[si + kVec]);
+      A left = (A)0, right = (A)0;
+      V4<S> vxm, vxp;
       unsigned cid[kVec];
-      if (sizeof(C) == 1) {
+      if (BATCHED) {
+        const int kk = 1 << kshift;
+        vxm = lx >= kk ? lds4(Pc + si - kk) : ldg4(P + idx - kk);
+        vxp = lx + kk < kTX ? lds4(Pc + si + kk) : ldg4(P + idx + kk);
+        const unsigned c = Cl[ly * (kTX >> kshift) + (lx >> kshift)];
+#pragma unroll
+        for (int e = 0; e < kVec; ++e) cid[e] = c;
+      } else {
+        if (x == 0 || (!Lay::XHALO && lx == 0)) left = St::load(P[idx - 1]);
+        else left = St::load(Pc[si - 1]);
+        if (x + kVec == X || (!Lay::XHALO && lx + kVec == kTX)) right = St::load(P[idx + kVec]);
+        else right = St::load(Pc[si + kVec]);
+      }
+      if (BATCHED) {
+      } else if (sizeof(C) == 1) {
         const uint32_t w = *reinterpret_cast<const uint32_t*>(Cl + ly * kTX + lx);
 #pragma unroll
         for (int e = 0; e < kVec; ++e) cid[e] = (w >> (8 * e)) & 0xFFu;
@@ -292,8 +329,14 @@ k_update_tma(const __grid_constant__ CUtensorMap map_cur, const __grid_constant_
 #pragma unroll
       for (int e = 0; e < kVec; ++e) {
         const A pc = St::load(vc.v[e]);
-        const A xm = e == 0 ? left : St::load(vc.v[e - 1]);
-        const A xp = e == kVec - 1 ? right : St::load(vc.v[e + 1]);
+        A xm, xp;
+        if (BATCHED) {
+          xm = St::load(vxm.v[e]);
+          xp = St::load(vxp.v[e]);
+        } else {
+          xm = e == 0 ? left : St::load(vc.v[e - 1]);
+          xp = e == kVec - 1 ? right : St::load(vc.v[e + 1]);
+        }
         const A ym = St::load(vym.v[e]), yp = St::load(vyp.v[e]);
         const A pm = St::load(vzm.v[e]), pn = St::load(vzp.v[e]);
         const A pp = St::load(vpp.v[e]);
@@ -373,15 +416,16 @@ bool make_map(CUtensorMap* m, CUtensorMapDataType dt, size_t esize, void* base, 
             CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
 }
 
-template <typename S, typename C, int SCHEME, typename Lay>
+template <typename S, typename C, int SCHEME, typename Lay, bool BATCHED = false>
 int launch_tma_t(pfdtd_domain* d, const void* cur, void* past, cudaStream_t s) {
   using A = typename Store<S>::A;
   constexpr int kTX = Lay::TX;
+  const int64_t XE = d->X * d->K;  // row length in elements
   const int64_t nz = d->Z - 2;
   if (nz <= 0) return PFDTD_OK;
   TmaState& ts = d->tma;
   const int cur_i = (cur == d->field(0)) ? 0 : 1;
-  const int64_t key[4] = {(int64_t)(intptr_t)d->d_cls, d->cls_bytes, d->precision,
+  const int64_t key[4] = {(int64_t)(intptr_t)d->d_cls, d->cls_bytes, d->precision * 100 + d->K,
                           (int64_t)Lay::TX * 10000 + Lay::TY * 10 + (Lay::XHALO ? 1 : 0)};
   if (!ts.ready || std::memcmp(key, ts.key, sizeof(key)) != 0) {
     const CUtensorMapDataType dt = TmaType<S>::value;
@@ -390,21 +434,21 @@ int launch_tma_t(pfdtd_domain* d, const void* cur, void* past, cudaStream_t s) {
     const int64_t rows = d->Y * d->Z;
     bool ok = true;
     for (int f = 0; f < 2; ++f) {
-      ok = ok && make_map(&ts.halo[f], dt, sizeof(S), d->field(f), d->X, rows, Lay::PW, Lay::TY + 2);
-      ok = ok && make_map(&ts.tile[f], dt, sizeof(S), d->field(f), d->X, rows, kTX, Lay::TY);
+      ok = ok && make_map(&ts.halo[f], dt, sizeof(S), d->field(f), XE, rows, Lay::PW, Lay::TY + 2);
+      ok = ok && make_map(&ts.tile[f], dt, sizeof(S), d->field(f), XE, rows, kTX, Lay::TY);
     }
-    ok = ok && make_map(&ts.cls, ct, sizeof(C), d->d_cls, d->X, rows, kTX, Lay::TY);
+    ok = ok && make_map(&ts.cls, ct, sizeof(C), d->d_cls, d->X, rows, kTX >> d->kshift, Lay::TY);
     if (!ok) return fail(PFDTD_ERR_UNSUPPORTED, "tensor map encoding failed");
     std::memcpy(ts.key, key, sizeof(key));
     ts.ready = true;
   }
   static bool attr_done = false;  // one instantiation, one attribute (per process)
   if (!attr_done) {
-    PFDTD_CK(cudaFuncSetAttribute(k_update_tma<S, C, SCHEME, Lay>,
+    PFDTD_CK(cudaFuncSetAttribute(k_update_tma<S, C, SCHEME, Lay, BATCHED>,
                                   cudaFuncAttributeMaxDynamicSharedMemorySize, Lay::SMEM));
     attr_done = true;
   }
-  const int gx = (int)((d->X + kTX - 1) / kTX);
+  const int gx = (int)((XE + kTX - 1) / kTX);
   const int gy = (int)((d->Y + Lay::TY - 1) / Lay::TY);
   // z-chunks: several per tile so that the grid fills the machine in whole
   // waves of (SMs x resident CTAs), each chunk at least 16 planes long.
@@ -428,12 +472,22 @@ int launch_tma_t(pfdtd_domain* d, const void* cur, void* past, cudaStream_t s) {
   ClassTab<A> tab{(const A*)tb, (const A*)(tb + as * d->n_classes),
                   (const A*)(tb + 2 * as * d->n_classes),
                   (const uint32_t*)(tb + 3 * as * d->n_classes), d->n_classes};
-  k_update_tma<S, C, SCHEME, Lay><<<dim3(gx, gy, gz), Lay::THREADS, Lay::SMEM, s>>>(
-      ts.halo[cur_i], ts.tile[1 - cur_i], ts.cls, (const S*)cur, (S*)past, tab, (int)d->X,
-      (int)d->Y, d->XY, (int)(d->Z - 1), (int)zc, (A)d->params[1], d->d_err);
+  k_update_tma<S, C, SCHEME, Lay, BATCHED><<<dim3(gx, gy, gz), Lay::THREADS, Lay::SMEM, s>>>(
+      ts.halo[cur_i], ts.tile[1 - cur_i], ts.cls, (const S*)cur, (S*)past, tab, (int)XE,
+      (int)d->Y, d->XY * d->K, (int)(d->Z - 1), (int)zc, (A)d->params[1], d->d_err, d->kshift);
   count_launch();
   PFDTD_CK(cudaGetLastError());
   return PFDTD_OK;
+}
+
+template <typename S, typename Lay8, typename Lay16>
+int launch_tma_batched(pfdtd_domain* d, const void* cur, void* past, cudaStream_t s) {
+  const bool centred = (d->class_scheme == PFDTD_SRL);
+  if (d->cls_bytes == 1)
+    return centred ? launch_tma_t<S, uint8_t, 1, Lay8, true>(d, cur, past, s)
+                   : launch_tma_t<S, uint8_t, 0, Lay8, true>(d, cur, past, s);
+  return centred ? launch_tma_t<S, uint16_t, 1, Lay16, true>(d, cur, past, s)
+                 : launch_tma_t<S, uint16_t, 0, Lay16, true>(d, cur, past, s);
 }
 
 template <typename S, typename Lay8, typename Lay16>
@@ -468,6 +522,9 @@ int auto_tile(const pfdtd_domain* d) {
 
 template <>
 int launch_tma_s<float>(pfdtd_domain* d, const void* cur, void* past, cudaStream_t s) {
+  if (d->K > 1)  // 256 elements (256/K nodes) x 4 rows
+    return launch_tma_batched<float, Layout<float, uint8_t, 256, 4, 8, false>,
+                              Layout<float, uint16_t, 256, 4, 8, false>>(d, cur, past, s);
   switch (d->tma_tile < 0 ? auto_tile(d) : d->tma_tile) {
 #define PFDTD_CASE(id, tx, ty, ns, xh)                                                    \
   case id:                                                                                \
@@ -491,6 +548,9 @@ int auto_tile16(const pfdtd_domain* d) {
 
 template <typename S>
 int launch_tma_16(pfdtd_domain* d, const void* cur, void* past, cudaStream_t s) {
+  if (d->K > 1)
+    return launch_tma_batched<S, Layout<S, uint8_t, 256, 8, 8, false>,
+                              Layout<S, uint16_t, 256, 8, 8, false>>(d, cur, past, s);
   switch (d->tma_tile < 0 ? auto_tile16(d) : d->tma_tile) {
 #define PFDTD_CASE16(id, tx, ty, ns, xh)                                                  \
   case id:                                                                                \
@@ -514,6 +574,9 @@ int launch_tma_s<__nv_bfloat16>(pfdtd_domain* d, const void* cur, void* past, cu
 
 template <>
 int launch_tma_s<double>(pfdtd_domain* d, const void* cur, void* past, cudaStream_t s) {
+  if (d->K > 1)
+    return launch_tma_batched<double, Layout<double, uint8_t, 128, 4, 6, false>,
+                              Layout<double, uint16_t, 128, 4, 6, false>>(d, cur, past, s);
   return launch_tma_l<double, Layout<double, uint8_t, 64, 8, 6>, Layout<double, uint16_t, 64, 8, 6>>(
       d, cur, past, s);
 }
@@ -524,7 +587,13 @@ int launch_tma_s<double>(pfdtd_domain* d, const void* cur, void* past, cudaStrea
 int tma_tile_count() { return 9; }
 
 bool tma_supported(const pfdtd_domain* d) {
-  if (d->K != 1) return false;
+  // Batched fields: a thread's 4 elements must be 4 fields of one node, and
+  // the class box (tile elements / K, at least 16 bytes) must stay valid.
+  if (d->K > 1) {
+    const int tile = d->precision == PFDTD_F64 ? 128 : 256;
+    if (d->K % 4 != 0 || (tile / d->K) * d->cls_bytes < 16) return false;
+    if ((d->X * d->K) % tile != 0) return false;
+  }
   if ((d->X * (int64_t)d->esize) % 16 != 0) return false;
   if ((d->X * (int64_t)d->cls_bytes) % 16 != 0) return false;
   if (d->Y * d->Z >= ((int64_t)1 << 31)) return false;

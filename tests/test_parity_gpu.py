@@ -534,10 +534,11 @@ def test_dif_boundaries_bit_identical(gpu, O, prec, scheme):
     assert np.array_equal(P, rP)
 
 
+@pytest.mark.parametrize("variant", ["zmarch", "auto"])
 @pytest.mark.parametrize("fields,prec,scheme", [(4, "f32", "forward"), (16, "f32", "forward"),
                                                 (16, "f16", "forward"), (4, "f64", "centred"),
-                                                (8, "f32", "iwb")])
-def test_batched_fields_equal_independent_runs(gpu, O, fields, prec, scheme):
+                                                (8, "bf16", "centred"), (8, "f32", "iwb")])
+def test_batched_fields_equal_independent_runs(gpu, O, fields, prec, scheme, variant):
     """K fields sharing one geometry: field f equals an independent oracle run
     of field f's source (bit-identical), with DIF boundaries on some materials."""
     from parallelfdtd_gb300 import materials
@@ -557,10 +558,13 @@ def test_batched_fields_equal_independent_runs(gpu, O, fields, prec, scheme):
         d.set_params(params)
         d.set_scheme(scheme)
         d.set_dif_filters(flags, table)
+        d.set_kernel(variant)
         d.set_sources(srcs, [1] * fields, np.repeat(pulse[None], fields, axis=0),
                       fields=list(range(fields)))
         d.set_receivers(recs, fields=rec_fields)
         g, _, _ = d.run(steps)
+        if variant == "auto" and scheme != "iwb":
+            assert d.kernel() == "tma"
     pos, mat = O.encode_nodes(room.bid, room.mat, scheme != "forward")
     for f in range(fields):
         r, _, _ = O.run(pos, mat, room.dims, room.admittance, params, [room.flat(*srcs[f])], [1],
