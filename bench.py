@@ -57,6 +57,8 @@ def parse():
     p.add_argument("--dims", type=str, default=None, help="X,Y,Z override (testing)")
     p.add_argument("--no-cpu-baseline", action="store_true")
     p.add_argument("--cpu-seconds", type=float, default=12.0)
+    p.add_argument("--tb", type=int, default=0,
+                   help="temporal block depth (0 = one update kernel per step; 2, 3, 4)")
     p.add_argument("--fields", type=int, default=1,
                    help="batched: K source fields sharing the room (the 384x320x256 multi-source "
                         "room, 4 receivers per field, when --dims is not given)")
@@ -275,6 +277,10 @@ def main():
     d.set_scheme("forward")
     d.set_sources(src, [1] * len(src), samples, fields=src_f)
     d.set_receivers(rec, fields=rec_f)
+    d.set_temporal_block(a.tb)
+    tb_info = d.temporal_block()
+    if a.tb and not tb_info[1]:
+        raise SystemExit(f"temporal blocking requested but inactive: {tb_info[2]}")
     stream = torch.cuda.ExternalStream(d.stream_ptr())
     d_out = torch.zeros(n_rec * S, dtype=torch.float64 if prec == "f64" else torch.float32,
                         device=f"cuda:{local}")
@@ -325,8 +331,16 @@ def main():
     kms = k0.elapsed_time(k1) / prof_iters
     nodes = X * Y * (Z - 2)
     bpu = bytes_per_update(prec, K)
-    algo_bytes = bpu * nodes * K
+    T = a.tb if a.tb else 1
+    if T > 1:
+        # a blocked launch advances T steps; its compulsory traffic is one
+        # read of P^n, P^{n-1} and the class ids and one write of the two
+        # output levels (4 field passes + 1 byte per node)
+        algo_bytes = (4 * esize * K + 1) * nodes
+    else:
+        algo_bytes = bpu * nodes * K
     achieved = algo_bytes / (kms * 1e-3) / 1e9
+    effective = bpu * nodes * K * T / (kms * 1e-3) / 1e9
     peak, peak_kind = peak_hbm()
     traffic = traffic_per_launch(prec, K)
 
@@ -368,6 +382,7 @@ def main():
                                    f"U(0.01,0.9), {src_txt}, {S} leapfrog steps, SRL forward, "
                                    f"{prec}",
                        "fdtd_steps_per_step": S, "nodes": X * Y * Z, "fields": K,
+                       "temporal_block": a.tb,
                        "bytes_per_update": bpu,
                        "parallelism": f"replicas x{world}",
                        "l2": f"inputs larger than L2 (fields 2 x {X * Y * Z * K * esize / 1e6:.0f} MB "
@@ -377,6 +392,8 @@ def main():
                          "frac": achieved / peak, "traffic": traffic,
                          "kernel": "k_update_" + d.kernel(), "kernel_ms": kms,
                          "algorithmic_bytes_per_launch": algo_bytes,
+                         "steps_per_launch": T,
+                         "effective_gbs": effective,
                          "peak_kind": f"of {peak_kind}"},
             "clocks": clk.summary(),
             "gpu_launches": int(launches),

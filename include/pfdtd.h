@@ -247,10 +247,12 @@ int pfdtd_capture_slice_noalloc(pfdtd_domain* d, int orientation, int64_t slice,
 /* Update kernel variant: 0 automatic (the TMA-pipelined kernel when the
  * grid's rows are 16-byte aligned, i.e. X a multiple of 16, FP32/FP64), 1 the
  * register z-marching kernel, 2 the TMA kernel.  pfdtd_get_kernel reports the
- * variant the next launch will use (1 or 2). */
+ * variant the next launch will use (1 or 2, or 3 when the temporally blocked
+ * kernel of pfdtd_set_temporal_block will run). */
 #define PFDTD_KERNEL_AUTO 0
 #define PFDTD_KERNEL_ZMARCH 1
 #define PFDTD_KERNEL_TMA 2
+#define PFDTD_KERNEL_TB 3 /* reported only: temporal blocking active */
 int pfdtd_set_kernel(pfdtd_domain* d, int variant);
 /* Tile shape of the TMA kernel for FP32 fields: 0 64x16, 1 128x8, 2 32x32,
  * 3 128x16, 4 128x4 (x halo in the TMA box); 5 128x8, 6 256x4, 7 256x8,
@@ -258,6 +260,26 @@ int pfdtd_set_kernel(pfdtd_domain* d, int variant);
  * 256/128/64 that divides X.  FP64 always uses 64x8. */
 int pfdtd_set_tile(pfdtd_domain* d, int tile);
 int pfdtd_get_kernel(pfdtd_domain* d, int* variant);
+
+/* Temporal blocking (no counterpart in the reference, whose launchFDTD3d
+ * loop at kernels3d.cu:86-175 runs one kernel per step).  depth 0 (default)
+ * runs one update per step; 2, 3 or 4 runs pfdtd_run / pfdtd_run_device
+ * with one kernel per `depth` steps that keeps the intermediate steps on
+ * chip, records the receivers of and injects the sources into every
+ * intermediate step, and writes two fields out of place (two more field
+ * buffers are allocated on the next run).  Results equal the per-step path
+ * (a zero on an x/y face node may differ in sign).  The blocked kernel is
+ * used only when: FP32, FP16 or BF16 storage; the SRL forward or centred
+ * scheme; no frequency-dependent boundary; at most 256 node classes; X a
+ * multiple of 4; K = 1 or a multiple of 4 fields; every node on the x and y
+ * faces of planes 1..Z-2 outside (position bit 7 clear); at most 64 sources
+ * and 256 receivers, none on plane 0 or Z-1.  Otherwise the run falls back
+ * to the per-step path.  pfdtd_get_temporal_block reports the depth, whether
+ * the next run will block (after building the node classes) and, in `why`,
+ * the first condition that fails. */
+int pfdtd_set_temporal_block(pfdtd_domain* d, int depth);
+int pfdtd_get_temporal_block(pfdtd_domain* d, int* depth, int* active, char* why,
+                             size_t why_len);
 
 /* Wait for the domain's queued work and report a kernel pipeline failure
  * (a bounded wait that expired) as PFDTD_ERR_CUDA. */

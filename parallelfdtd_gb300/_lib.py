@@ -30,7 +30,7 @@ SRL_FORWARD, SHARED, SRL, IWB = 0, 1, 2, 3
 SRC_HARD, SRC_SOFT, SRC_TRANSPARENT = 0, 1, 2
 QUIRK_MATIDX, QUIRK_SOFTSRC = 1, 2
 FIELD_CURRENT, FIELD_PAST = 0, 1
-KERNEL_AUTO, KERNEL_ZMARCH, KERNEL_TMA = 0, 1, 2
+KERNEL_AUTO, KERNEL_ZMARCH, KERNEL_TMA, KERNEL_TB = 0, 1, 2, 3
 
 INTERRUPT_FN = C.CFUNCTYPE(C.c_int)
 PROGRESS_FN = C.CFUNCTYPE(None, C.c_int, C.c_int, C.c_float)
@@ -86,6 +86,9 @@ _SIGNATURES = {
     "pfdtd_set_kernel": (_i32, [_vp, _i32]),
     "pfdtd_set_tile": (_i32, [_vp, _i32]),
     "pfdtd_get_kernel": (_i32, [_vp, C.POINTER(_i32)]),
+    "pfdtd_set_temporal_block": (_i32, [_vp, _i32]),
+    "pfdtd_get_temporal_block": (_i32, [_vp, C.POINTER(_i32), C.POINTER(_i32), C.c_char_p,
+                                        C.c_size_t]),
     "pfdtd_synchronize": (_i32, [_vp]),
     "pfdtd_kernel_launches": (_i64, []),
     "pfdtd_encode_nodes": (_i32, [_i32, _vp, _vp, _i64, _i32]),

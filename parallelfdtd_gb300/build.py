@@ -22,7 +22,8 @@ INCLUDE = os.path.join(ROOT, "include")
 BUILD = os.path.join(PKG, "_build")
 LIB = os.path.join(PKG, "libpfdtd.so")
 
-CUDA_SOURCES = ["stencil.cu", "stencil_tma.cu", "dif.cu", "domain.cu", "setup.cu", "noalloc.cu"]
+CUDA_SOURCES = ["stencil.cu", "stencil_tma.cu", "stencil_tb.cu", "dif.cu", "domain.cu", "setup.cu",
+                "noalloc.cu"]
 CXX_SOURCES = [
     "classes_host.cpp",
     "host/logger.cpp",

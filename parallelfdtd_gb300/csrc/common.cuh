@@ -99,6 +99,7 @@ struct TmaState {
 #define PFDTD_KERNEL_AUTO 0
 #define PFDTD_KERNEL_ZMARCH 1
 #define PFDTD_KERNEL_TMA 2
+#define PFDTD_KERNEL_TB 3
 
 struct GraphCache {
   cudaGraphExec_t exec = nullptr;
@@ -122,8 +123,12 @@ struct pfdtd_domain {
   int64_t NE = 0;            // field elements, N * K
   size_t esize = 4;          // storage bytes per field element
   int64_t margin = 0;        // elements before node 0 / after node N-1
-  void* field_base[2] = {nullptr, nullptr};
-  int cur = 0;               // index of the current field
+  // Field buffers: two for the plain leapfrog (P^{n+1} written over P^{n-1}),
+  // two more allocated for the temporally blocked update, which writes its
+  // two output levels out of place.
+  void* field_base[4] = {nullptr, nullptr, nullptr, nullptr};
+  int cur = 0;               // index of the current field P^n
+  int prev = 1;              // index of the past field P^{n-1}
   uint8_t* d_pos = nullptr;
   uint8_t* d_mat = nullptr;
   bool nodes_set = false;
@@ -178,19 +183,26 @@ struct pfdtd_domain {
   int* d_err = nullptr;
   pfdtd::TmaState tma;
 
+  // temporal blocking (stencil_tb.cu): requested depth (0 off) and the
+  // geometry check it depends on, cached per class build
+  int tb_depth = 0;
+  int tb_faces_ok = 0;       // every x/y face node of planes 1..Z-2 is outside
+  int tb_shape = -1;         // tile shape index, -1 automatic
+
   size_t arith_size() const { return precision == PFDTD_F64 ? 8 : 4; }
   void* field(int which) const {
     return (char*)field_base[which] + (size_t)margin * esize;
   }
   void* cur_field() const { return field(cur); }
-  void* past_field() const { return field(1 - cur); }
+  void* past_field() const { return field(prev); }
+  void swap_fields() { const int t = cur; cur = prev; prev = t; }
 };
 
 namespace pfdtd {
 // Implemented in stencil.cu
 int launch_update(pfdtd_domain* d, const void* cur, void* past, cudaStream_t s);
 int launch_io(pfdtd_domain* d, void* cur, void* rec_out, int64_t rec_ld, int64_t inject_end,
-              cudaStream_t s);
+              cudaStream_t s, int advance = 1);
 int build_classes(pfdtd_domain* d);
 // Implemented in stencil_tma.cu
 bool tma_supported(const pfdtd_domain* d);
@@ -201,4 +213,9 @@ int launch_dif(pfdtd_domain* d, const void* cur, void* past, cudaStream_t s);
 int launch_dif_init(pfdtd_domain* d, cudaStream_t s);
 int tma_tile_count();
 int launch_update_tma(pfdtd_domain* d, const void* cur, void* past, cudaStream_t s);
+// Implemented in stencil_tb.cu
+int tb_usable(const pfdtd_domain* d, std::string* why);
+int launch_tb(pfdtd_domain* d, void* rec_out, int64_t rec_ld, int64_t inject_end, cudaStream_t s);
+int check_tb_faces(pfdtd_domain* d);
+int tb_shape_count();
 }  // namespace pfdtd

@@ -124,14 +124,23 @@ int enqueue_step(pfdtd_domain* d, void* rec_out, int64_t rec_ld, int64_t inject_
   if (rc) return rc;
   rc = launch_dif(d, d->cur_field(), d->past_field(), s);
   if (rc) return rc;
-  d->cur = 1 - d->cur;
+  d->swap_fields();
   return PFDTD_OK;
 }
 
-// A graph of kChunk steps starting from the domain's current field.
+// Steps per captured graph with temporal blocking: a multiple of 2T for
+// T = 2, 3, 4, so the four buffers return to their roles after a chunk.
+constexpr int64_t kChunkTb = 48;
+
+bool tb_active(const pfdtd_domain* d) { return tb_usable(d, nullptr) != 0; }
+
+// A graph of kChunk steps (kChunkTb when blocked) starting from the
+// domain's current fields.
 int get_chunk_graph(pfdtd_domain* d, void* rec_out, int64_t rec_ld, int64_t inject_end,
                     cudaGraphExec_t* exec) {
-  const int64_t key[8] = {d->cur, kChunk, d->class_version, d->io_version,
+  const int tb = tb_active(d) ? d->tb_depth : 0;
+  const int64_t chunk = tb ? kChunkTb : kChunk;
+  const int64_t key[8] = {d->cur * 16 + d->prev * 4 + tb, chunk, d->class_version, d->io_version,
                           (int64_t)(intptr_t)rec_out, rec_ld, inject_end,
                           (int64_t)(intptr_t)d->d_cls};
   if (d->graph.exec && std::memcmp(key, d->graph.key, sizeof(key)) == 0) {
@@ -144,13 +153,19 @@ int get_chunk_graph(pfdtd_domain* d, void* rec_out, int64_t rec_ld, int64_t inje
   }
   cudaStream_t s = d->stream;
   PFDTD_CK(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal));
-  const int cur0 = d->cur;
+  const int cur0 = d->cur, prev0 = d->prev;
   const int64_t before = g_launches.load();
   int rc = PFDTD_OK;
-  for (int64_t i = 0; i < kChunk && rc == PFDTD_OK; ++i)
-    rc = enqueue_step(d, rec_out, rec_ld, inject_end, s);
+  if (tb) {
+    for (int64_t i = 0; i < chunk && rc == PFDTD_OK; i += tb)
+      rc = launch_tb(d, rec_out, rec_ld, inject_end, s);
+  } else {
+    for (int64_t i = 0; i < chunk && rc == PFDTD_OK; ++i)
+      rc = enqueue_step(d, rec_out, rec_ld, inject_end, s);
+  }
   g_launches.store(before);  // captured, not launched
   d->cur = cur0;
+  d->prev = prev0;
   cudaGraph_t graph = nullptr;
   cudaError_t e = cudaStreamEndCapture(s, &graph);
   if (rc != PFDTD_OK) {
@@ -181,7 +196,22 @@ int check_pipeline(pfdtd_domain* d) {
 int prepare_run(pfdtd_domain* d) {
   if (!d->nodes_set) return fail(PFDTD_ERR_STATE, "node bytes not set");
   if (d->n_mat <= 0) return fail(PFDTD_ERR_STATE, "material table not set");
-  return build_classes(d);
+  int rc = build_classes(d);
+  if (rc) return rc;
+  // the temporally blocked update writes out of place: two more fields
+  if (d->tb_depth >= 2 && !d->field_base[2]) {
+    const size_t fbytes = (size_t)(d->NE + 2 * d->margin) * d->esize;
+    for (int i = 2; i < 4; ++i) {
+      if (cudaMalloc(&d->field_base[i], fbytes) != cudaSuccess) {
+        cudaGetLastError();
+        if (d->field_base[2]) cudaFree(d->field_base[2]);
+        d->field_base[2] = nullptr;
+        return fail(PFDTD_ERR_NOMEM, "allocation of the temporal blocking fields failed");
+      }
+      PFDTD_CK(cudaMemsetAsync(d->field_base[i], 0, fbytes, d->stream));
+    }
+  }
+  return PFDTD_OK;
 }
 
 // Queue `steps` steps recording into rec_out (device, [n_rec * steps]).
@@ -193,8 +223,10 @@ int enqueue_run(pfdtd_domain* d, int64_t steps, void* rec_out, F&& between, bool
   cudaStream_t s = d->stream;
   PFDTD_CK(cudaMemsetAsync(d->d_step, 0, sizeof(int64_t), s));
   if (int rc0 = launch_dif_init(d, s)) return rc0;
-  const int64_t chunks = steps / kChunk;
-  const int64_t rem = steps - chunks * kChunk;
+  const int tb = tb_active(d) ? d->tb_depth : 0;
+  const int64_t chunk = tb ? kChunkTb : kChunk;
+  const int64_t chunks = steps / chunk;
+  const int64_t rem = steps - chunks * chunk;
   cudaEvent_t ev[2] = {nullptr, nullptr};
   PFDTD_CK(cudaEventCreateWithFlags(&ev[0], cudaEventDisableTiming));
   PFDTD_CK(cudaEventCreateWithFlags(&ev[1], cudaEventDisableTiming));
@@ -209,20 +241,25 @@ int enqueue_run(pfdtd_domain* d, int64_t steps, void* rec_out, F&& between, bool
       e = cudaMemcpy(&perr, d->d_err, sizeof(int), cudaMemcpyDeviceToHost);
       if (e != cudaSuccess) { rc = cuda_fail(e, "error flag read", __FILE__, __LINE__); break; }
       if (perr) { *stopped = true; break; }  // reported by check_pipeline after the sync
-      if (between((k - 1) * kChunk)) { *stopped = true; break; }
+      if (between((k - 1) * chunk)) { *stopped = true; break; }
     }
     cudaGraphExec_t exec = nullptr;
     rc = get_chunk_graph(d, rec_out, steps, steps, &exec);
     if (rc) break;
     cudaError_t e = cudaGraphLaunch(exec, s);
     if (e != cudaSuccess) { rc = cuda_fail(e, "cudaGraphLaunch", __FILE__, __LINE__); break; }
-    count_launch(2 * kChunk);
+    count_launch(tb ? 2 * (chunk / tb) : 2 * chunk);
     e = cudaEventRecord(ev[k % 2], s);
     if (e != cudaSuccess) { rc = cuda_fail(e, "cudaEventRecord", __FILE__, __LINE__); break; }
-    queued += kChunk;
+    queued += chunk;
   }
   if (rc == PFDTD_OK && !*stopped) {
-    for (int64_t i = 0; i < rem && rc == PFDTD_OK; ++i) {
+    int64_t i = 0;
+    for (; tb && i + tb <= rem && rc == PFDTD_OK; i += tb) {
+      rc = launch_tb(d, rec_out, steps, steps, s);
+      if (rc == PFDTD_OK) queued += tb;
+    }
+    for (; i < rem && rc == PFDTD_OK; ++i) {
       rc = enqueue_step(d, rec_out, steps, steps, s);
       if (rc == PFDTD_OK) ++queued;
     }
@@ -347,7 +384,7 @@ int pfdtd_destroy(pfdtd_domain* d) {
   DeviceGuard g(d->device);
   if (d->stream) cudaStreamSynchronize(d->stream);
   if (d->graph.exec) cudaGraphExecDestroy(d->graph.exec);
-  void* ptrs[] = {d->field_base[0], d->field_base[1], d->d_pos, d->d_mat, d->d_cls,
+  void* ptrs[] = {d->field_base[0], d->field_base[1], d->field_base[2], d->field_base[3], d->d_pos, d->d_mat, d->d_cls,
                   d->d_ctab, d->d_src_idx, d->d_src_mode, d->d_src_samples, d->d_rec_idx,
                   d->d_step, d->d_rec_out, d->d_err, d->d_dif_list, d->d_dif_tab,
                   d->d_dif_state};
@@ -609,9 +646,17 @@ int pfdtd_profile_update(pfdtd_domain* d, int iters) {
   DeviceGuard g(d->device);
   int rc = prepare_run(d);
   if (rc) return rc;
+  if (tb_active(d)) {
+    // one blocked launch (and its io kernel) per iteration: depth steps,
+    // no sources or receivers
+    PFDTD_CK(cudaMemsetAsync(d->d_step, 0, sizeof(int64_t), d->stream));
+    for (int i = 0; i < iters && rc == PFDTD_OK; ++i)
+      rc = launch_tb(d, nullptr, 0, 0, d->stream);
+    return rc;
+  }
   for (int i = 0; i < iters && rc == PFDTD_OK; ++i) {
     rc = launch_update(d, d->cur_field(), d->past_field(), d->stream);
-    d->cur = 1 - d->cur;
+    d->swap_fields();
   }
   return rc;
 }
@@ -634,7 +679,7 @@ int pfdtd_step(pfdtd_domain* d, int64_t step, int step_direction, void* out, int
   rc = launch_dif(d, d->cur_field(), d->past_field(), s);
   if (rc) return rc;
   // kernels3d.cu:462-465: swap only while the direction is unchanged.
-  if (d->past_step_direction == step_direction) d->cur = 1 - d->cur;
+  if (d->past_step_direction == step_direction) d->swap_fields();
   d->past_step_direction = step_direction;
   PFDTD_CK(cudaStreamSynchronize(s));
   if (int e = check_pipeline(d)) return e;
@@ -707,7 +752,7 @@ int pfdtd_get_sample(pfdtd_domain* d, int64_t x, int64_t y, int64_t z, double* v
 
 int pfdtd_flip(pfdtd_domain* d) {
   if (int rc = check_domain(d)) return rc;
-  d->cur = 1 - d->cur;
+  d->swap_fields();
   return PFDTD_OK;
 }
 
@@ -715,7 +760,8 @@ int pfdtd_reset_fields(pfdtd_domain* d) {
   if (int rc = check_domain(d)) return rc;
   DeviceGuard g(d->device);
   const size_t fbytes = (size_t)(d->NE + 2 * d->margin) * d->esize;
-  for (int i = 0; i < 2; ++i) PFDTD_CK(cudaMemsetAsync(d->field_base[i], 0, fbytes, d->stream));
+  for (int i = 0; i < 4; ++i)
+    if (d->field_base[i]) PFDTD_CK(cudaMemsetAsync(d->field_base[i], 0, fbytes, d->stream));
   if (d->n_dif > 0)
     PFDTD_CK(cudaMemsetAsync(d->d_dif_state, 0, (size_t)d->n_dif * d->K * 4 * d->arith_size(),
                              d->stream));
@@ -806,6 +852,37 @@ int pfdtd_get_kernel(pfdtd_domain* d, int* variant) {
   if (!variant) return fail(PFDTD_ERR_ARG, "null output");
   const bool tma = d->kernel_variant != PFDTD_KERNEL_ZMARCH && tma_supported(d);
   *variant = tma ? PFDTD_KERNEL_TMA : PFDTD_KERNEL_ZMARCH;
+  if (d->tb_depth >= 2 && tb_active(d)) *variant = PFDTD_KERNEL_TB;
+  return PFDTD_OK;
+}
+
+int pfdtd_set_temporal_block(pfdtd_domain* d, int depth) {
+  if (int rc = check_domain(d)) return rc;
+  if (depth != 0 && (depth < 2 || depth > 4))
+    return fail(PFDTD_ERR_ARG, "temporal block depth must be 0 (off), 2, 3 or 4");
+  d->tb_depth = depth;
+  if (d->graph.exec) {
+    cudaGraphExecDestroy(d->graph.exec);
+    d->graph.exec = nullptr;
+  }
+  return PFDTD_OK;
+}
+
+int pfdtd_get_temporal_block(pfdtd_domain* d, int* depth, int* active, char* why,
+                             size_t why_len) {
+  if (int rc = check_domain(d)) return rc;
+  DeviceGuard g(d->device);
+  if (d->tb_depth >= 2 && d->nodes_set && d->n_mat > 0) {
+    if (int rc = prepare_run(d)) return rc;
+  }
+  std::string w = "active";
+  const int a = tb_usable(d, &w);
+  if (depth) *depth = d->tb_depth;
+  if (active) *active = a;
+  if (why && why_len > 0) {
+    std::strncpy(why, w.c_str(), why_len - 1);
+    why[why_len - 1] = 0;
+  }
   return PFDTD_OK;
 }
 

@@ -208,7 +208,7 @@ __global__ void k_step_io(S* __restrict__ cur, int64_t* __restrict__ d_step, int
                           int64_t rec_ld, int n_src, const int64_t* __restrict__ src_idx,
                           const int32_t* __restrict__ src_mode,
                           const typename Store<S>::A* __restrict__ samples, int64_t n_samples,
-                          int64_t inject_end) {
+                          int64_t inject_end, int advance) {
   using A = typename Store<S>::A;
   using St = Store<S>;
   const int64_t n = *d_step;
@@ -231,7 +231,8 @@ __global__ void k_step_io(S* __restrict__ cur, int64_t* __restrict__ d_step, int
           cur[i] = St::store(Rn<A>::add(St::load(cur[i]), v));
       }
     }
-    *d_step = n + 1;
+    // A temporally blocked update that follows advances by its depth.
+    *d_step = n + advance;
   }
 }
 
@@ -317,12 +318,13 @@ int launch_update_s(pfdtd_domain* d, const void* cur, void* past, cudaStream_t s
 
 template <typename S>
 int launch_io_t(pfdtd_domain* d, void* cur, void* rec_out, int64_t rec_ld, int64_t inject_end,
-                cudaStream_t s) {
+                cudaStream_t s, int advance) {
   using A = typename Store<S>::A;
   const int threads = std::max(32, std::min(1024, ((d->n_rec + 31) / 32) * 32));
   k_step_io<S><<<1, threads, 0, s>>>((S*)cur, d->d_step, d->n_rec, d->d_rec_idx, (A*)rec_out,
                                     rec_ld, d->n_src, d->d_src_idx, d->d_src_mode,
-                                    (const A*)d->d_src_samples, d->n_samples, inject_end);
+                                    (const A*)d->d_src_samples, d->n_samples, inject_end,
+                                    advance);
   count_launch();
   PFDTD_CK(cudaGetLastError());
   return PFDTD_OK;
@@ -349,12 +351,13 @@ int launch_update(pfdtd_domain* d, const void* cur, void* past, cudaStream_t s) 
 }
 
 int launch_io(pfdtd_domain* d, void* cur, void* rec_out, int64_t rec_ld, int64_t inject_end,
-              cudaStream_t s) {
+              cudaStream_t s, int advance) {
   switch (d->precision) {
-    case PFDTD_F32: return launch_io_t<float>(d, cur, rec_out, rec_ld, inject_end, s);
-    case PFDTD_F64: return launch_io_t<double>(d, cur, rec_out, rec_ld, inject_end, s);
-    case PFDTD_F16: return launch_io_t<__half>(d, cur, rec_out, rec_ld, inject_end, s);
-    case PFDTD_BF16: return launch_io_t<__nv_bfloat16>(d, cur, rec_out, rec_ld, inject_end, s);
+    case PFDTD_F32: return launch_io_t<float>(d, cur, rec_out, rec_ld, inject_end, s, advance);
+    case PFDTD_F64: return launch_io_t<double>(d, cur, rec_out, rec_ld, inject_end, s, advance);
+    case PFDTD_F16: return launch_io_t<__half>(d, cur, rec_out, rec_ld, inject_end, s, advance);
+    case PFDTD_BF16:
+      return launch_io_t<__nv_bfloat16>(d, cur, rec_out, rec_ld, inject_end, s, advance);
   }
   return fail(PFDTD_ERR_UNSUPPORTED, "unknown precision");
 }
@@ -424,6 +427,8 @@ int build_classes(pfdtd_domain* d) {
   d->n_classes = n_classes;
   d->class_scheme = scheme;
   rc = build_dif(d, keys, tab);
+  if (rc != PFDTD_OK) return rc;
+  rc = check_tb_faces(d);
   if (rc != PFDTD_OK) return rc;
   d->classes_dirty = false;
   d->class_version++;

@@ -252,7 +252,18 @@ class Domain:
     def kernel(self) -> str:
         v = C.c_int()
         L.call("pfdtd_get_kernel", self.handle, C.byref(v))
-        return {L.KERNEL_ZMARCH: "zmarch", L.KERNEL_TMA: "tma"}[v.value]
+        return {L.KERNEL_ZMARCH: "zmarch", L.KERNEL_TMA: "tma", L.KERNEL_TB: "tb"}[v.value]
+
+    def set_temporal_block(self, depth: int) -> None:
+        """Steps per update kernel: 0 (one kernel per step) or 2, 3, 4."""
+        L.call("pfdtd_set_temporal_block", self.handle, int(depth))
+
+    def temporal_block(self):
+        """(depth, active, reason): whether the next run uses the blocked kernel."""
+        depth, active = C.c_int(), C.c_int()
+        why = C.create_string_buffer(256)
+        L.call("pfdtd_get_temporal_block", self.handle, C.byref(depth), C.byref(active), why, 256)
+        return depth.value, bool(active.value), why.value.decode()
 
     def synchronize(self) -> None:
         L.call("pfdtd_synchronize", self.handle)
