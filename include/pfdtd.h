@@ -280,6 +280,23 @@ int pfdtd_get_kernel(pfdtd_domain* d, int* variant);
 int pfdtd_set_temporal_block(pfdtd_domain* d, int depth);
 int pfdtd_get_temporal_block(pfdtd_domain* d, int* depth, int* active, char* why,
                              size_t why_len);
+/* Tile shape of the blocked kernel, -1 (default) or 0..2:
+ *   one field per node: 0 = 64 x 32 nodes, 256 threads of two rows;
+ *     1 = 64 x 32, 512 threads of one row; 2 = 64 x 64, 512 threads of two
+ *     rows (depths 2, 3); depth 4 has only shape 1;
+ *   batched fields: 0 = 32 x 32 nodes of 4 fields, 512 threads of two rows;
+ *     1 = one row per thread (FP32 depth 4: 32 x 24); depth 4 only shape 1.
+ * A shape that does not exist for the depth makes the next run fail with
+ * PFDTD_ERR_ARG. */
+int pfdtd_set_tb_shape(pfdtd_domain* d, int shape);
+/* Autotuner (no counterpart in the reference): times the per-step update and
+ * every available (depth <= max_depth, shape) of the blocked update on this
+ * domain, `iters` launches each after one warm-up launch, keeps the fastest
+ * per step on the domain and reports it.  The fields are copied before and
+ * restored after the timing launches; node classes are built first.
+ * max_depth 0 times the per-step update only. */
+int pfdtd_autotune(pfdtd_domain* d, int max_depth, int iters, int* best_depth, int* best_shape,
+                   double* best_ms_per_step);
 
 /* Wait for the domain's queued work and report a kernel pipeline failure
  * (a bounded wait that expired) as PFDTD_ERR_CUDA. */

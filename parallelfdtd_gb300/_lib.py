@@ -87,6 +87,9 @@ _SIGNATURES = {
     "pfdtd_set_tile": (_i32, [_vp, _i32]),
     "pfdtd_get_kernel": (_i32, [_vp, C.POINTER(_i32)]),
     "pfdtd_set_temporal_block": (_i32, [_vp, _i32]),
+    "pfdtd_set_tb_shape": (_i32, [_vp, _i32]),
+    "pfdtd_autotune": (_i32, [_vp, _i32, _i32, C.POINTER(_i32), C.POINTER(_i32),
+                              C.POINTER(C.c_double)]),
     "pfdtd_get_temporal_block": (_i32, [_vp, C.POINTER(_i32), C.POINTER(_i32), C.c_char_p,
                                         C.c_size_t]),
     "pfdtd_synchronize": (_i32, [_vp]),

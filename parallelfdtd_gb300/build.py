@@ -22,7 +22,8 @@ INCLUDE = os.path.join(ROOT, "include")
 BUILD = os.path.join(PKG, "_build")
 LIB = os.path.join(PKG, "libpfdtd.so")
 
-CUDA_SOURCES = ["stencil.cu", "stencil_tma.cu", "stencil_tb.cu", "dif.cu", "domain.cu", "setup.cu",
+CUDA_SOURCES = ["stencil.cu", "stencil_tma.cu", "stencil_tb.cu", "stencil_tb_f32.cu",
+                "stencil_tb_f16.cu", "stencil_tb_bf16.cu", "dif.cu", "domain.cu", "setup.cu",
                 "noalloc.cu"]
 CXX_SOURCES = [
     "classes_host.cpp",
@@ -38,6 +39,20 @@ CXX_SOURCES = [
 HEADERS_DIRS = [CSRC, os.path.join(CSRC, "host"), INCLUDE, os.path.join(INCLUDE, "pfdtd")]
 
 GENCODE = ["-gencode", "arch=compute_103a,code=sm_103a"]
+
+# The blocked-update units hold only explicitly rounded arithmetic; -fmad=false
+# also keeps nvcc from fusing the packed FP32x2 multiply and add intrinsics.
+# PFDTD_TB_PACKED=1 in the environment builds the packed forward rule.
+TB_SOURCES = ("stencil_tb_f32.cu", "stencil_tb_f16.cu", "stencil_tb_bf16.cu")
+
+
+def _extra_flags(src: str):
+    if os.path.basename(src) in TB_SOURCES:
+        f = ["-fmad=false"]
+        if os.environ.get("PFDTD_TB_PACKED"):
+            f.append("-DPFDTD_TB_PACKED=1")
+        return f
+    return []
 
 
 def _nvcc() -> str:
@@ -78,7 +93,7 @@ def _compile(src: str, cuda: bool) -> str:
     if cuda:
         cmd = [_nvcc(), *GENCODE, "-lineinfo", "-O3", "-std=c++17", "-Xcompiler", "-fPIC",
                "-Xcompiler", "-ffp-contract=off", "-Xptxas", "-v" if os.environ.get("PFDTD_PTXAS_V") else "-O3",
-               *inc, "-c", src, "-o", obj]
+               *_extra_flags(src), *inc, "-c", src, "-o", obj]
     else:
         cmd = ["g++", "-O2", "-std=c++17", "-fPIC", "-ffp-contract=off", "-fno-fast-math",
                *inc, "-c", src, "-o", obj]

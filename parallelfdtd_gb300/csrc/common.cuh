@@ -217,5 +217,5 @@ int launch_update_tma(pfdtd_domain* d, const void* cur, void* past, cudaStream_t
 int tb_usable(const pfdtd_domain* d, std::string* why);
 int launch_tb(pfdtd_domain* d, void* rec_out, int64_t rec_ld, int64_t inject_end, cudaStream_t s);
 int check_tb_faces(pfdtd_domain* d);
-int tb_shape_count();
+bool tb_shape_valid(const pfdtd_domain* d, int shape);
 }  // namespace pfdtd

@@ -369,6 +369,7 @@ int pfdtd_create_batched(int64_t dim_x, int64_t dim_y, int64_t dim_z, int fields
     return cleanup(PFDTD_ERR_NOMEM, "step counter allocation failed");
   cudaMemsetAsync(d->d_err, 0, sizeof(int), d->stream);
   if (const char* tv = std::getenv("PFDTD_TMA_TILE")) d->tma_tile = std::atoi(tv);
+  if (const char* sv = std::getenv("PFDTD_TB_SHAPE")) d->tb_shape = std::atoi(sv);
   if (const char* kv = std::getenv("PFDTD_KERNEL")) {
     if (std::strcmp(kv, "zmarch") == 0) d->kernel_variant = PFDTD_KERNEL_ZMARCH;
     if (std::strcmp(kv, "tma") == 0) d->kernel_variant = PFDTD_KERNEL_TMA;
@@ -883,6 +884,127 @@ int pfdtd_get_temporal_block(pfdtd_domain* d, int* depth, int* active, char* why
     std::strncpy(why, w.c_str(), why_len - 1);
     why[why_len - 1] = 0;
   }
+  return PFDTD_OK;
+}
+
+int pfdtd_set_tb_shape(pfdtd_domain* d, int shape) {
+  if (int rc = check_domain(d)) return rc;
+  if (shape < -1 || shape > 2) return fail(PFDTD_ERR_ARG, "blocked tile shape must be -1..2");
+  d->tb_shape = shape;
+  if (d->graph.exec) {
+    cudaGraphExecDestroy(d->graph.exec);
+    d->graph.exec = nullptr;
+  }
+  return PFDTD_OK;
+}
+
+// Time one update configuration: `iters` launches after one warm-up launch,
+// returned as milliseconds per step.
+static int time_config(pfdtd_domain* d, int iters, double* ms_per_step) {
+  cudaStream_t s = d->stream;
+  const bool tb = d->tb_depth >= 2 && tb_active(d);
+  auto launch = [&]() -> int {
+    if (tb) return launch_tb(d, nullptr, 0, 0, s);
+    int rc = launch_update(d, d->cur_field(), d->past_field(), s);
+    d->swap_fields();
+    return rc;
+  };
+  PFDTD_CK(cudaMemsetAsync(d->d_step, 0, sizeof(int64_t), s));
+  if (int rc = launch()) return rc;
+  cudaEvent_t e0, e1;
+  PFDTD_CK(cudaEventCreate(&e0));
+  PFDTD_CK(cudaEventCreate(&e1));
+  int rc = PFDTD_OK;
+  cudaEventRecord(e0, s);
+  for (int i = 0; i < iters && rc == PFDTD_OK; ++i) rc = launch();
+  cudaEventRecord(e1, s);
+  cudaError_t e = cudaEventSynchronize(e1);
+  float ms = 0.f;
+  if (e == cudaSuccess) e = cudaEventElapsedTime(&ms, e0, e1);
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  if (rc) return rc;
+  if (e != cudaSuccess) return cuda_fail(e, "autotune timing", __FILE__, __LINE__);
+  *ms_per_step = (double)ms / ((double)iters * (tb ? d->tb_depth : 1));
+  return PFDTD_OK;
+}
+
+int pfdtd_autotune(pfdtd_domain* d, int max_depth, int iters, int* best_depth, int* best_shape,
+                   double* best_ms_per_step) {
+  if (int rc = check_domain(d)) return rc;
+  if (max_depth != 0 && (max_depth < 2 || max_depth > 4))
+    return fail(PFDTD_ERR_ARG, "maximum depth must be 0, 2, 3 or 4");
+  if (iters < 1) return fail(PFDTD_ERR_ARG, "iteration count must be positive");
+  DeviceGuard g(d->device);
+  const int depth0 = d->tb_depth, shape0 = d->tb_shape;
+  d->tb_depth = max_depth >= 2 ? 2 : 0;  // allocate the blocking buffers if needed
+  int rc = prepare_run(d);
+  if (rc) {
+    d->tb_depth = depth0;
+    return rc;
+  }
+  // The timing launches advance the fields: keep a copy and put it back.
+  cudaStream_t s = d->stream;
+  const size_t fbytes = (size_t)(d->NE + 2 * d->margin) * d->esize;
+  void* keep[2] = {nullptr, nullptr};
+  for (int i = 0; i < 2; ++i) {
+    if (cudaMallocAsync(&keep[i], fbytes, s) != cudaSuccess) {
+      cudaGetLastError();
+      if (keep[0]) cudaFreeAsync(keep[0], s);
+      d->tb_depth = depth0;
+      return fail(PFDTD_ERR_NOMEM, "autotune field snapshot allocation failed");
+    }
+  }
+  PFDTD_CK(cudaMemcpyAsync(keep[0], d->field_base[d->cur], fbytes, cudaMemcpyDeviceToDevice, s));
+  PFDTD_CK(cudaMemcpyAsync(keep[1], d->field_base[d->prev], fbytes, cudaMemcpyDeviceToDevice, s));
+  double best = 1e300;
+  int bd = 0, bs = -1;
+  struct Cand { int depth, shape; };
+  std::vector<Cand> cands{{0, -1}};
+  for (int depth = 2; depth <= max_depth; ++depth)
+    for (int shape = 0; shape < 3; ++shape) cands.push_back({depth, shape});
+  for (const Cand& c : cands) {
+    d->tb_depth = c.depth;
+    d->tb_shape = c.shape;
+    if (c.depth >= 2 && (!tb_active(d) || !tb_shape_valid(d, c.shape))) continue;
+    double ms = 0;
+    rc = time_config(d, iters, &ms);
+    if (rc == PFDTD_ERR_ARG || rc == PFDTD_ERR_UNSUPPORTED) {  // shape not built here
+      rc = PFDTD_OK;
+      continue;
+    }
+    if (rc) break;
+    if (ms < best) {
+      best = ms;
+      bd = c.depth;
+      bs = c.shape;
+    }
+  }
+  if (rc == PFDTD_OK) {
+    cudaError_t e = cudaMemcpyAsync(d->field_base[d->cur], keep[0], fbytes,
+                                    cudaMemcpyDeviceToDevice, s);
+    if (e == cudaSuccess)
+      e = cudaMemcpyAsync(d->field_base[d->prev], keep[1], fbytes, cudaMemcpyDeviceToDevice, s);
+    if (e != cudaSuccess) rc = cuda_fail(e, "autotune field restore", __FILE__, __LINE__);
+  }
+  cudaFreeAsync(keep[0], s);
+  cudaFreeAsync(keep[1], s);
+  cudaError_t e = cudaStreamSynchronize(s);
+  if (rc == PFDTD_OK && e != cudaSuccess) rc = cuda_fail(e, "autotune", __FILE__, __LINE__);
+  if (d->graph.exec) {
+    cudaGraphExecDestroy(d->graph.exec);
+    d->graph.exec = nullptr;
+  }
+  if (rc) {
+    d->tb_depth = depth0;
+    d->tb_shape = shape0;
+    return rc;
+  }
+  d->tb_depth = bd;
+  d->tb_shape = bs;
+  if (best_depth) *best_depth = bd;
+  if (best_shape) *best_shape = bs;
+  if (best_ms_per_step) *best_ms_per_step = best;
   return PFDTD_OK;
 }
 

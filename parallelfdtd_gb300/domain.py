@@ -258,6 +258,18 @@ class Domain:
         """Steps per update kernel: 0 (one kernel per step) or 2, 3, 4."""
         L.call("pfdtd_set_temporal_block", self.handle, int(depth))
 
+    def set_tb_shape(self, shape: int) -> None:
+        """Tile shape of the blocked kernel (-1 default, 0..2)."""
+        L.call("pfdtd_set_tb_shape", self.handle, int(shape))
+
+    def autotune(self, max_depth: int = 4, iters: int = 10):
+        """Time the per-step and blocked configurations on this domain, keep the
+        fastest; returns (depth, shape, ms per step)."""
+        depth, shape, ms = C.c_int(), C.c_int(), C.c_double()
+        L.call("pfdtd_autotune", self.handle, int(max_depth), int(iters), C.byref(depth),
+               C.byref(shape), C.byref(ms))
+        return depth.value, shape.value, ms.value
+
     def temporal_block(self):
         """(depth, active, reason): whether the next run uses the blocked kernel."""
         depth, active = C.c_int(), C.c_int()

@@ -32,7 +32,7 @@ def values(a, prec):
 
 
 def run(room, prec, scheme, depth, srcs, recs, samples, steps, fields=1, src_fields=None,
-        rec_fields=None, nodes=None):
+        rec_fields=None, nodes=None, shape=-1):
     with Domain(room.dims, prec, fields=fields) as d:
         d.set_voxels(room.bid, room.mat, centred=(scheme != "forward"))
         if nodes is not None:
@@ -43,6 +43,7 @@ def run(room, prec, scheme, depth, srcs, recs, samples, steps, fields=1, src_fie
         d.set_sources([s[0] for s in srcs], [s[1] for s in srcs], samples, fields=src_fields)
         d.set_receivers(recs, fields=rec_fields)
         d.set_temporal_block(depth)
+        d.set_tb_shape(shape)
         info = d.temporal_block()
         g, _, st = d.run(steps)
         assert st == 0
@@ -154,3 +155,65 @@ def test_blocked_depth_validation(gpu):
             with pytest.raises(L.PfdtdError):
                 d.set_temporal_block(bad)
         d.set_temporal_block(0)
+
+
+@pytest.mark.parametrize("fields,depth,shape", [(1, 2, 1), (1, 2, 2), (1, 3, 1), (1, 3, 2),
+                                                (1, 4, 1), (4, 2, 1), (8, 3, 1), (4, 4, 1)])
+def test_blocked_shapes(gpu, fields, depth, shape):
+    room = rooms.boxes_room((136, 100, 70), n_boxes=8, edge=(6, 20), n_materials=7, seed=31)
+    steps = 77
+    pulse = rooms.gaussian_pulse(steps, 3.0)
+    pts = room.random_air_nodes(3 * fields, seed=8)
+    srcs = [(tuple(p), 1) for p in pts[:fields]]
+    recs = [tuple(p) for p in pts[fields:]]
+    src_f = list(range(fields)) if fields > 1 else None
+    rec_f = [i // 2 for i in range(2 * fields)] if fields > 1 else None
+    samples = np.stack([pulse * (1 + 0.1 * f) for f in range(fields)])
+    g0, P0, Pp0, _ = run(room, "f32", "forward", 0, srcs, recs, samples, steps, fields, src_f,
+                         rec_f)
+    g1, P1, Pp1, info = run(room, "f32", "forward", depth, srcs, recs, samples, steps, fields,
+                            src_f, rec_f, shape=shape)
+    assert info[1], info[2]
+    assert np.array_equal(g1, g0)
+    assert np.array_equal(P1, P0) and np.array_equal(Pp1, Pp0)
+
+
+def test_blocked_missing_shape_fails(gpu):
+    room = rooms.boxes_room((64, 48, 40), n_boxes=3, edge=(5, 10), n_materials=4, seed=23)
+    with Domain(room.dims, "f32") as d:
+        d.set_voxels(room.bid, room.mat, centred=False)
+        d.set_materials(room.admittance)
+        d.set_params(default_params())
+        d.set_sources([tuple(room.random_air_nodes(1, seed=1)[0])], [1], np.ones((1, 60)))
+        d.set_receivers([tuple(room.random_air_nodes(1, seed=2)[0])])
+        d.set_temporal_block(4)
+        d.set_tb_shape(0)  # depth 4 exists in shape 1 only
+        with pytest.raises(L.PfdtdError):
+            d.run(60)
+
+
+def test_autotune_restores_fields_and_keeps_results(gpu):
+    """The autotuner times configurations on the domain's own fields, puts the
+    fields back, and the configuration it keeps gives the per-step results."""
+    room = room_a()
+    srcs, recs = io_a(room)
+    steps = 90
+    pulse = rooms.gaussian_pulse(steps, 3.0)
+    samples = np.stack([pulse, -0.5 * pulse, pulse, 0.25 * pulse])
+    g0, P0, Pp0, _ = run(room, "f32", "forward", 0, srcs, recs, samples, steps)
+    with Domain(room.dims, "f32") as d:
+        d.set_voxels(room.bid, room.mat, centred=False)
+        d.set_materials(room.admittance)
+        d.set_params(default_params())
+        d.set_sources([s[0] for s in srcs], [s[1] for s in srcs], samples)
+        d.set_receivers(recs)
+        rnd = np.random.default_rng(0).standard_normal(d.n).astype(np.float32)
+        d.upload_field(L.FIELD_CURRENT, rnd)
+        depth, shape, ms = d.autotune(max_depth=4, iters=3)
+        assert depth in (0, 2, 3, 4) and ms > 0
+        assert np.array_equal(d.download_field(L.FIELD_CURRENT), rnd)
+        d.reset_fields()
+        g1, _, st = d.run(steps)
+        assert st == 0
+        assert np.array_equal(g1, g0)
+        assert np.array_equal(values(d.download_field(L.FIELD_CURRENT), "f32"), P0)
