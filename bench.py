@@ -57,6 +57,13 @@ def parse():
     p.add_argument("--dims", type=str, default=None, help="X,Y,Z override (testing)")
     p.add_argument("--no-cpu-baseline", action="store_true")
     p.add_argument("--cpu-seconds", type=float, default=12.0)
+    p.add_argument("--serve", type=int, default=0,
+                   help="serving workload: replay N requests of the seeded trace (Poisson "
+                        "arrivals at 20/s, rooms U(64,512) per axis, SRL/IWB, FI/DIF, "
+                        "500-8000 steps, 1-16 sources) through the request loop")
+    p.add_argument("--serve-seed", type=int, default=0)
+    p.add_argument("--serve-slots", type=int, default=8)
+    p.add_argument("--serve-budget-gb", type=float, default=160.0)
     p.add_argument("--tb", type=int, default=0,
                    help="temporal block depth (0 = one update kernel per step; 2, 3, 4)")
     p.add_argument("--fields", type=int, default=1,
@@ -240,11 +247,62 @@ def run_reference_arm(a, world, rank):
     return 0
 
 
+def run_serving(a, world, rank, local):
+    """Replay the seeded serving trace through the native request loop."""
+    import concurrent.futures as cf
+    import __graft_entry__ as g
+    g.build()
+    import torch
+    from parallelfdtd_gb300.serving import Server, build_request, run_trace, serving_trace
+    torch.cuda.set_device(local)
+    trace = serving_trace(a.serve, seed=a.serve_seed + 1000 * rank)
+    with cf.ThreadPoolExecutor(max_workers=min(8, os.cpu_count() or 4)) as ex:
+        reqs = list(ex.map(lambda it: build_request(it, a.precision), trace))
+    budget = int(a.serve_budget_gb * (1 << 30))
+    with ClockSampler(local) as clk:
+        with Server(local, hbm_budget=budget, max_active=a.serve_slots) as srv:
+            res = run_trace(srv, reqs, [it.arrival for it in trace])
+    wall = res["wall_s"]
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl" if torch.cuda.is_available() else "gloo")
+        t = torch.tensor([wall], device=f"cuda:{local}", dtype=torch.float64)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        wall = float(t.item())
+        dist.destroy_process_group()
+    st = res["stats"]
+    if rank == 0:
+        line = {
+            "metric": METRIC, "value": res["node_updates"] * world / wall, "unit": METRIC,
+            "n_gpus": world, "steps": len(trace), "warmup": 0,
+            "ms_per_step": wall * 1e3 / len(trace), "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": a.precision,
+            "data": "synthetic",
+            "config": {"workload": f"serving trace of {len(trace)} requests (seed "
+                                   f"{a.serve_seed}): Poisson arrivals 20/s, per-axis sizes "
+                                   "U(64,512), SRL forward / IWB 50/50, FI / 3rd-order DIF "
+                                   "50/50, steps U(500,8000), 1-16 sources (one field each, "
+                                   "4 receivers per source)",
+                       "hbm_budget_gb": a.serve_budget_gb, "slots": a.serve_slots,
+                       "parallelism": f"replicas x{world}"},
+            "latency": {k: res[k] for k in ("latency_p50_s", "latency_p99_s", "queue_p50_s",
+                                            "queue_p99_s", "service_p50_s", "service_p99_s")},
+            "e2e": {"value": res["node_updates"] * world / wall, "unit": METRIC,
+                    "h2d_bytes_per_step": None, "d2h_bytes_per_step": None},
+            "server": {k: st[k] for k in ("completed", "failed", "max_running", "bytes_peak")},
+            "clocks": clk.summary(),
+        }
+        print(json.dumps(line), flush=True)
+    return 0
+
+
 def main():
     a = parse()
     world, rank, local = dist_env()
     if a.impl == "reference":
         return run_reference_arm(a, world, rank)
+    if a.serve:
+        return run_serving(a, world, rank, local)
 
     import numpy as np
     import torch

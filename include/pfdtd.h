@@ -244,6 +244,17 @@ int pfdtd_capture_slice(pfdtd_domain* d, int orientation, int64_t slice, float* 
 int pfdtd_capture_slice_noalloc(pfdtd_domain* d, int orientation, int64_t slice, float* p_out,
                                 uint8_t* pos_out);
 
+/* Asynchronous run (no counterpart in the reference): queue `steps` steps
+ * from step 0 on the domain's stream and return without waiting; receivers
+ * are recorded on the device.  pfdtd_query reports whether the domain's queued
+ * work has finished; pfdtd_fetch_receivers waits for it, reports a failed
+ * kernel pipeline and copies the receivers ([n_rec * steps], arithmetic type)
+ * of the last asynchronous run to the host.  No call waits for other
+ * domains' work. */
+int pfdtd_run_async(pfdtd_domain* d, int64_t steps);
+int pfdtd_query(pfdtd_domain* d, int* done);
+int pfdtd_fetch_receivers(pfdtd_domain* d, void* out);
+
 /* Update kernel variant: 0 automatic (the TMA-pipelined kernel when the
  * grid's rows are 16-byte aligned, i.e. X a multiple of 16, FP32/FP64), 1 the
  * register z-marching kernel, 2 the TMA kernel.  pfdtd_get_kernel reports the
@@ -314,6 +325,8 @@ int64_t pfdtd_kernel_launches(void);
  * forward (toBilbao, cudaMesh.cu:328-361) when centred == 0, else centred
  * (toKowalczyk, :363-480).  d_pos, d_mat: device pointers, n nodes. */
 int pfdtd_encode_nodes(int centred, uint8_t* d_pos, uint8_t* d_mat, int64_t n, int device);
+/* The same translation on host arrays (no device work). */
+int pfdtd_encode_nodes_host(int centred, uint8_t* pos, uint8_t* mat, int64_t n);
 
 /* Count air and boundary nodes (calcBoundaries, cudaMesh.cu:500-514). */
 int pfdtd_count_boundaries(const uint8_t* d_pos, int64_t n, uint8_t air_value,

@@ -87,6 +87,33 @@ _SIGNATURES = {
     "pfdtd_set_tile": (_i32, [_vp, _i32]),
     "pfdtd_get_kernel": (_i32, [_vp, C.POINTER(_i32)]),
     "pfdtd_set_temporal_block": (_i32, [_vp, _i32]),
+    "pfdtd_run_async": (_i32, [_vp, _i64]),
+    "pfdtd_query": (_i32, [_vp, C.POINTER(_i32)]),
+    "pfdtd_fetch_receivers": (_i32, [_vp, _vp]),
+    "pfdtd_encode_nodes_host": (_i32, [_i32, _vp, _vp, _i64]),
+    # request loop (pfdtd_server.h)
+    "pfdtd_request_create": (_i32, [_i64, _i64, _i64, _i32, _i32, _i32, _i64, C.POINTER(_vp)]),
+    "pfdtd_request_set_voxels": (_i32, [_vp, _vp, _vp]),
+    "pfdtd_request_set_nodes": (_i32, [_vp, _vp, _vp]),
+    "pfdtd_request_set_materials": (_i32, [_vp, C.POINTER(C.c_double), _i32, _i32]),
+    "pfdtd_request_set_dif_filters": (_i32, [_vp, _i32, C.POINTER(C.c_int32),
+                                             C.POINTER(C.c_double)]),
+    "pfdtd_request_set_params": (_i32, [_vp, C.POINTER(C.c_double)]),
+    "pfdtd_request_set_sources": (_i32, [_vp, _i32, C.POINTER(_i64), C.POINTER(C.c_int32),
+                                         C.POINTER(C.c_int32), C.POINTER(C.c_double), _i64]),
+    "pfdtd_request_set_receivers": (_i32, [_vp, _i32, C.POINTER(_i64), C.POINTER(C.c_int32)]),
+    "pfdtd_request_set_temporal_block": (_i32, [_vp, _i32]),
+    "pfdtd_request_bytes": (_i32, [_vp, C.POINTER(C.c_uint64)]),
+    "pfdtd_request_destroy": (_i32, [_vp]),
+    "pfdtd_server_create": (_i32, [_i32, C.c_uint64, _i32, C.POINTER(_vp)]),
+    "pfdtd_server_submit": (_i32, [_vp, _vp, C.POINTER(_i64)]),
+    "pfdtd_server_wait": (_i32, [_vp, _i64, C.c_double, C.POINTER(_i32)]),
+    "pfdtd_server_result": (_i32, [_vp, _i64, _vp, C.POINTER(C.c_double)]),
+    "pfdtd_server_request_error": (C.c_char_p, [_vp, _i64]),
+    "pfdtd_server_release": (_i32, [_vp, _i64]),
+    "pfdtd_server_stats_get": (_i32, [_vp, _vp]),
+    "pfdtd_server_drain": (_i32, [_vp, C.c_double]),
+    "pfdtd_server_destroy": (_i32, [_vp]),
     "pfdtd_set_tb_shape": (_i32, [_vp, _i32]),
     "pfdtd_autotune": (_i32, [_vp, _i32, _i32, C.POINTER(_i32), C.POINTER(_i32),
                               C.POINTER(C.c_double)]),

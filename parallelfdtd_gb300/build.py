@@ -35,24 +35,19 @@ CXX_SOURCES = [
     "host/kernels3d.cpp",
     "host/App.cpp",
     "host/app_capi.cpp",
+    "host/server.cpp",
 ]
 HEADERS_DIRS = [CSRC, os.path.join(CSRC, "host"), INCLUDE, os.path.join(INCLUDE, "pfdtd")]
 
 GENCODE = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
-# The blocked-update units hold only explicitly rounded arithmetic; -fmad=false
-# also keeps nvcc from fusing the packed FP32x2 multiply and add intrinsics.
-# PFDTD_TB_PACKED=1 in the environment builds the packed forward rule.
+# The blocked-update units hold only explicitly rounded arithmetic and integer
+# indexing; -fmad=false states that no contraction is wanted there.
 TB_SOURCES = ("stencil_tb_f32.cu", "stencil_tb_f16.cu", "stencil_tb_bf16.cu")
 
 
 def _extra_flags(src: str):
-    if os.path.basename(src) in TB_SOURCES:
-        f = ["-fmad=false"]
-        if os.environ.get("PFDTD_TB_PACKED"):
-            f.append("-DPFDTD_TB_PACKED=1")
-        return f
-    return []
+    return ["-fmad=false"] if os.path.basename(src) in TB_SOURCES else []
 
 
 def _nvcc() -> str:

@@ -188,6 +188,7 @@ struct pfdtd_domain {
   int tb_depth = 0;
   int tb_faces_ok = 0;       // every x/y face node of planes 1..Z-2 is outside
   int tb_shape = -1;         // tile shape index, -1 automatic
+  int64_t async_steps = 0;   // steps of the last pfdtd_run_async
 
   size_t arith_size() const { return precision == PFDTD_F64 ? 8 : 4; }
   void* field(int which) const {
@@ -196,6 +197,13 @@ struct pfdtd_domain {
   void* cur_field() const { return field(cur); }
   void* past_field() const { return field(prev); }
   void swap_fields() { const int t = cur; cur = prev; prev = t; }
+  // Device buffers of the domain come from the stream-ordered allocator on
+  // its own stream: neither allocation nor release waits for other domains'
+  // work (cudaFree would synchronise the whole device).
+  cudaError_t alloc(void** p, size_t bytes) { return cudaMallocAsync(p, bytes, stream); }
+  void release(void* p) {
+    if (p) cudaFreeAsync(p, stream);
+  }
 };
 
 namespace pfdtd {

@@ -251,7 +251,7 @@ int build_dif(pfdtd_domain* d, const std::vector<uint16_t>& keys,
               const std::vector<uint8_t>& main_tab) {
   for (void** p : {(void**)&d->d_dif_list, &d->d_dif_tab, &d->d_dif_state})
     if (*p) {
-      PFDTD_CK(cudaFree(*p));
+      d->release(*p);
       *p = nullptr;
     }
   d->n_dif = 0;
@@ -273,8 +273,8 @@ int build_dif(pfdtd_domain* d, const std::vector<uint16_t>& keys,
   const int64_t blocks = (end - begin + kChunkNodes - 1) / kChunkNodes;
   uint8_t* d_is = nullptr;
   int* d_counts = nullptr;
-  PFDTD_CK(cudaMalloc((void**)&d_is, is_dif.size()));
-  PFDTD_CK(cudaMalloc((void**)&d_counts, sizeof(int) * (blocks + 1)));
+  PFDTD_CK(d->alloc((void**)&d_is, is_dif.size()));
+  PFDTD_CK(d->alloc((void**)&d_counts, sizeof(int) * (blocks + 1)));
   PFDTD_CK(cudaMemcpyAsync(d_is, is_dif.data(), is_dif.size(), cudaMemcpyHostToDevice, s));
   k_dif_count<<<(int)blocks, kListThreads, 0, s>>>(d->d_cls, d->cls_bytes, d_is, begin, end, d_counts);
   count_launch();
@@ -289,21 +289,21 @@ int build_dif(pfdtd_domain* d, const std::vector<uint16_t>& keys,
   }
   if (total > 0) {
     PFDTD_CK(cudaMemcpyAsync(d_counts, offsets.data(), sizeof(int) * blocks, cudaMemcpyHostToDevice, s));
-    PFDTD_CK(cudaMalloc((void**)&d->d_dif_list, sizeof(int64_t) * total));
+    PFDTD_CK(d->alloc((void**)&d->d_dif_list, sizeof(int64_t) * total));
     k_dif_list<<<(int)blocks, kListThreads, 0, s>>>(d->d_cls, d->cls_bytes, d_is, begin, end,
                                                    d_counts, d->d_dif_list);
     count_launch();
     PFDTD_CK(cudaGetLastError());
-    PFDTD_CK(cudaMalloc(&d->d_dif_tab, tab_bytes.size()));
+    PFDTD_CK(d->alloc(&d->d_dif_tab, tab_bytes.size()));
     PFDTD_CK(cudaMemcpyAsync(d->d_dif_tab, tab_bytes.data(), tab_bytes.size(),
                              cudaMemcpyHostToDevice, s));
     const size_t sbytes = (size_t)total * d->K * 4 * d->arith_size();
-    PFDTD_CK(cudaMalloc(&d->d_dif_state, sbytes));
+    PFDTD_CK(d->alloc(&d->d_dif_state, sbytes));
     PFDTD_CK(cudaMemsetAsync(d->d_dif_state, 0, sbytes, s));
   }
   PFDTD_CK(cudaStreamSynchronize(s));
-  cudaFree(d_is);
-  cudaFree(d_counts);
+  d->release(d_is);
+  d->release(d_counts);
   d->n_dif = total;
   return PFDTD_OK;
 }

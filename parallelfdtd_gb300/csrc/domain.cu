@@ -106,10 +106,10 @@ int ensure_rec_out(pfdtd_domain* d, int64_t steps) {
   const size_t need = (size_t)std::max(d->n_rec, 1) * (size_t)std::max<int64_t>(steps, 1) *
                       d->arith_size();
   if (need <= d->rec_out_bytes) return PFDTD_OK;
-  if (d->d_rec_out) PFDTD_CK(cudaFree(d->d_rec_out));
+  d->release(d->d_rec_out);
   d->d_rec_out = nullptr;
   d->rec_out_bytes = 0;
-  if (cudaMalloc(&d->d_rec_out, need) != cudaSuccess)
+  if (d->alloc(&d->d_rec_out, need) != cudaSuccess)
     return fail(PFDTD_ERR_NOMEM, "receiver buffer allocation failed");
   d->rec_out_bytes = need;
   return PFDTD_OK;
@@ -202,9 +202,9 @@ int prepare_run(pfdtd_domain* d) {
   if (d->tb_depth >= 2 && !d->field_base[2]) {
     const size_t fbytes = (size_t)(d->NE + 2 * d->margin) * d->esize;
     for (int i = 2; i < 4; ++i) {
-      if (cudaMalloc(&d->field_base[i], fbytes) != cudaSuccess) {
+      if (d->alloc(&d->field_base[i], fbytes) != cudaSuccess) {
         cudaGetLastError();
-        if (d->field_base[2]) cudaFree(d->field_base[2]);
+        d->release(d->field_base[2]);
         d->field_base[2] = nullptr;
         return fail(PFDTD_ERR_NOMEM, "allocation of the temporal blocking fields failed");
       }
@@ -219,7 +219,7 @@ int prepare_run(pfdtd_domain* d) {
 // completion; it returns non-zero to stop.
 template <typename F>
 int enqueue_run(pfdtd_domain* d, int64_t steps, void* rec_out, F&& between, bool* stopped,
-                int64_t* steps_queued) {
+                int64_t* steps_queued, bool poll = true) {
   cudaStream_t s = d->stream;
   PFDTD_CK(cudaMemsetAsync(d->d_step, 0, sizeof(int64_t), s));
   if (int rc0 = launch_dif_init(d, s)) return rc0;
@@ -234,7 +234,7 @@ int enqueue_run(pfdtd_domain* d, int64_t steps, void* rec_out, F&& between, bool
   int64_t queued = 0;
   *stopped = false;
   for (int64_t k = 0; k < chunks; ++k) {
-    if (k >= 2) {
+    if (poll && k >= 2) {
       cudaError_t e = cudaEventSynchronize(ev[k % 2]);
       if (e != cudaSuccess) { rc = cuda_fail(e, "cudaEventSynchronize", __FILE__, __LINE__); break; }
       int perr = 0;
@@ -350,22 +350,22 @@ int pfdtd_create_batched(int64_t dim_x, int64_t dim_y, int64_t dim_z, int fields
   if (cudaStreamCreateWithFlags(&d->stream, cudaStreamNonBlocking) != cudaSuccess)
     return cleanup(PFDTD_ERR_CUDA, "stream creation failed");
   for (int i = 0; i < 2; ++i) {
-    if (cudaMalloc(&d->field_base[i], fbytes) != cudaSuccess) {
+    if (d->alloc(&d->field_base[i], fbytes) != cudaSuccess) {
       cudaGetLastError();
       return cleanup(PFDTD_ERR_NOMEM, "field allocation failed");
     }
     if (cudaMemsetAsync(d->field_base[i], 0, fbytes, d->stream) != cudaSuccess)
       return cleanup(PFDTD_ERR_CUDA, "field clear failed");
   }
-  if (cudaMalloc((void**)&d->d_pos, (size_t)d->N + 1 + dim_x) != cudaSuccess ||
-      cudaMalloc((void**)&d->d_mat, (size_t)d->N + 1 + dim_x) != cudaSuccess) {
+  if (d->alloc((void**)&d->d_pos, (size_t)d->N + 1 + dim_x) != cudaSuccess ||
+      d->alloc((void**)&d->d_mat, (size_t)d->N + 1 + dim_x) != cudaSuccess) {
     cudaGetLastError();
     return cleanup(PFDTD_ERR_NOMEM, "node byte allocation failed");
   }
   cudaMemsetAsync(d->d_pos, 0, (size_t)d->N + 1 + dim_x, d->stream);
   cudaMemsetAsync(d->d_mat, 0, (size_t)d->N + 1 + dim_x, d->stream);
-  if (cudaMalloc((void**)&d->d_step, sizeof(int64_t)) != cudaSuccess ||
-      cudaMalloc((void**)&d->d_err, sizeof(int)) != cudaSuccess)
+  if (d->alloc((void**)&d->d_step, sizeof(int64_t)) != cudaSuccess ||
+      d->alloc((void**)&d->d_err, sizeof(int)) != cudaSuccess)
     return cleanup(PFDTD_ERR_NOMEM, "step counter allocation failed");
   cudaMemsetAsync(d->d_err, 0, sizeof(int), d->stream);
   if (const char* tv = std::getenv("PFDTD_TMA_TILE")) d->tma_tile = std::atoi(tv);
@@ -390,7 +390,7 @@ int pfdtd_destroy(pfdtd_domain* d) {
                   d->d_step, d->d_rec_out, d->d_err, d->d_dif_list, d->d_dif_tab,
                   d->d_dif_state};
   for (void* p : ptrs)
-    if (p) cudaFree(p);
+    d->release(p);
   if (d->stream) cudaStreamDestroy(d->stream);
   delete d;
   return PFDTD_OK;
@@ -525,7 +525,7 @@ int pfdtd_set_sources_batched(pfdtd_domain* d, int n, const int64_t* xyz, const 
   DeviceGuard g(d->device);
   for (void** p : {(void**)&d->d_src_idx, (void**)&d->d_src_mode, &d->d_src_samples})
     if (*p) {
-      PFDTD_CK(cudaFree(*p));
+      d->release(*p);
       *p = nullptr;
     }
   d->n_src = n;
@@ -542,14 +542,19 @@ int pfdtd_set_sources_batched(pfdtd_domain* d, int n, const int64_t* xyz, const 
   const size_t sbytes = (size_t)n * (size_t)n_samples * d->arith_size();
   d->src_samples_h.assign((const uint8_t*)samples, (const uint8_t*)samples + sbytes);
   const size_t n1 = std::max(n, 1);
-  PFDTD_CK(cudaMalloc((void**)&d->d_src_idx, n1 * sizeof(int64_t)));
-  PFDTD_CK(cudaMalloc((void**)&d->d_src_mode, n1 * sizeof(int32_t)));
-  PFDTD_CK(cudaMalloc(&d->d_src_samples, std::max<size_t>(sbytes, 16)));
+  PFDTD_CK(d->alloc((void**)&d->d_src_idx, n1 * sizeof(int64_t)));
+  PFDTD_CK(d->alloc((void**)&d->d_src_mode, n1 * sizeof(int32_t)));
+  PFDTD_CK(d->alloc(&d->d_src_samples, std::max<size_t>(sbytes, 16)));
+  cudaStream_t s = d->stream;
   if (n > 0) {
-    PFDTD_CK(cudaMemcpy(d->d_src_idx, d->src_idx_h.data(), n * sizeof(int64_t), cudaMemcpyHostToDevice));
-    PFDTD_CK(cudaMemcpy(d->d_src_mode, mode.data(), n * sizeof(int32_t), cudaMemcpyHostToDevice));
-    if (sbytes) PFDTD_CK(cudaMemcpy(d->d_src_samples, samples, sbytes, cudaMemcpyHostToDevice));
+    PFDTD_CK(cudaMemcpyAsync(d->d_src_idx, d->src_idx_h.data(), n * sizeof(int64_t),
+                             cudaMemcpyHostToDevice, s));
+    PFDTD_CK(cudaMemcpyAsync(d->d_src_mode, mode.data(), n * sizeof(int32_t),
+                             cudaMemcpyHostToDevice, s));
+    if (sbytes)
+      PFDTD_CK(cudaMemcpyAsync(d->d_src_samples, samples, sbytes, cudaMemcpyHostToDevice, s));
   }
+  PFDTD_CK(cudaStreamSynchronize(s));
   d->io_version++;
   return PFDTD_OK;
 }
@@ -563,7 +568,7 @@ int pfdtd_set_receivers_batched(pfdtd_domain* d, int n, const int64_t* xyz, cons
   if (n < 0 || (n > 0 && !xyz)) return fail(PFDTD_ERR_ARG, "invalid receiver array");
   DeviceGuard g(d->device);
   if (d->d_rec_idx) {
-    PFDTD_CK(cudaFree(d->d_rec_idx));
+    d->release(d->d_rec_idx);
     d->d_rec_idx = nullptr;
   }
   d->n_rec = n;
@@ -571,9 +576,11 @@ int pfdtd_set_receivers_batched(pfdtd_domain* d, int n, const int64_t* xyz, cons
   for (int i = 0; i < n; ++i)
     d->rec_idx_h[i] = element_index(d, xyz[3 * i], xyz[3 * i + 1], xyz[3 * i + 2],
                                     field ? field[i] : 0);
-  PFDTD_CK(cudaMalloc((void**)&d->d_rec_idx, std::max(n, 1) * sizeof(int64_t)));
+  PFDTD_CK(d->alloc((void**)&d->d_rec_idx, std::max(n, 1) * sizeof(int64_t)));
   if (n > 0)
-    PFDTD_CK(cudaMemcpy(d->d_rec_idx, d->rec_idx_h.data(), n * sizeof(int64_t), cudaMemcpyHostToDevice));
+    PFDTD_CK(cudaMemcpyAsync(d->d_rec_idx, d->rec_idx_h.data(), n * sizeof(int64_t),
+                             cudaMemcpyHostToDevice, d->stream));
+  PFDTD_CK(cudaStreamSynchronize(d->stream));
   d->io_version++;
   return PFDTD_OK;
 }
@@ -639,6 +646,56 @@ int pfdtd_run_device(pfdtd_domain* d, int64_t steps, void* d_out) {
   bool stopped = false;
   int64_t queued = 0;
   return enqueue_run(d, steps, d_out, [](int64_t) { return 0; }, &stopped, &queued);
+}
+
+int pfdtd_run_async(pfdtd_domain* d, int64_t steps) {
+  if (int rc = check_domain(d)) return rc;
+  if (steps < 0) return fail(PFDTD_ERR_ARG, "negative step count");
+  DeviceGuard g(d->device);
+  int rc = prepare_run(d);
+  if (rc || steps == 0) return rc;
+  rc = ensure_rec_out(d, steps);
+  if (rc) return rc;
+  const size_t rec_bytes = (size_t)d->n_rec * (size_t)steps * d->arith_size();
+  if (rec_bytes) PFDTD_CK(cudaMemsetAsync(d->d_rec_out, 0, rec_bytes, d->stream));
+  bool stopped = false;
+  int64_t queued = 0;
+  rc = enqueue_run(d, steps, d->d_rec_out, [](int64_t) { return 0; }, &stopped, &queued, false);
+  if (rc == PFDTD_OK) d->async_steps = steps;
+  return rc;
+}
+
+int pfdtd_query(pfdtd_domain* d, int* done) {
+  if (int rc = check_domain(d)) return rc;
+  if (!done) return fail(PFDTD_ERR_ARG, "null output");
+  DeviceGuard g(d->device);
+  const cudaError_t e = cudaStreamQuery(d->stream);
+  if (e == cudaSuccess) {
+    *done = 1;
+    return PFDTD_OK;
+  }
+  if (e == cudaErrorNotReady) {
+    cudaGetLastError();
+    *done = 0;
+    return PFDTD_OK;
+  }
+  return cuda_fail(e, "stream query", __FILE__, __LINE__);
+}
+
+int pfdtd_fetch_receivers(pfdtd_domain* d, void* out) {
+  if (int rc = check_domain(d)) return rc;
+  if (!out && d->n_rec > 0) return fail(PFDTD_ERR_ARG, "null output buffer");
+  DeviceGuard g(d->device);
+  PFDTD_CK(cudaStreamSynchronize(d->stream));
+  if (int e = check_pipeline(d)) return e;
+  const int64_t steps = d->async_steps;
+  const size_t row = (size_t)steps * d->arith_size();
+  for (int r = 0; r < d->n_rec && steps > 0; ++r)
+    if (d->rec_idx_h[r] >= 0)
+      PFDTD_CK(cudaMemcpyAsync((char*)out + r * row, (char*)d->d_rec_out + r * row, row,
+                               cudaMemcpyDeviceToHost, d->stream));
+  PFDTD_CK(cudaStreamSynchronize(d->stream));
+  return PFDTD_OK;
 }
 
 int pfdtd_profile_update(pfdtd_domain* d, int iters) {

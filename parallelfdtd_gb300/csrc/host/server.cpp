@@ -1,0 +1,491 @@
+// Request loop with continuous batching over the C ABI (pfdtd_server.h).
+//
+// One scheduler thread per server.  It keeps a FIFO of submitted requests
+// and a set of running ones.  Each pass it (1) retires running requests
+// whose domain stream has drained: receivers to the host, domain destroyed,
+// memory back to the budget; (2) admits queued requests in arrival order
+// while a slot is free and the head request's estimated bytes fit beside
+// the running ones: domain created and set up on its own stream, the whole
+// run queued with pfdtd_run_async.  The scheduler never waits on the device
+// as a whole: queries are per stream and allocations are stream-ordered, so
+// admitted requests overlap on the GPU while the host admits and retires.
+#include <algorithm>
+#include <chrono>
+#include <cmath>
+#include <condition_variable>
+#include <cstring>
+#include <deque>
+#include <map>
+#include <mutex>
+#include <string>
+#include <thread>
+#include <vector>
+
+#include "pfdtd.h"
+#include "pfdtd_server.h"
+
+namespace pfdtd {
+int fail(int code, const std::string& msg);
+}
+using pfdtd::fail;
+
+struct pfdtd_request {
+  int64_t X = 0, Y = 0, Z = 0;
+  int fields = 1, precision = PFDTD_F32, scheme = PFDTD_SRL_FORWARD;
+  int64_t steps = 0;
+  std::vector<uint8_t> pos, mat;
+  bool nodes_set = false;
+  int64_t n_boundary = 0;  // nodes with a boundary update (for the filter-state estimate)
+  std::vector<double> materials;
+  int n_mat = 0, n_coef = 20;
+  std::vector<int32_t> dif_flags;
+  std::vector<double> dif_coefs;
+  double params[4] = {0.57735026918962576, 1.0 / 3.0, 1.0 / 3.0, 0.0};
+  int n_src = 0;
+  int64_t n_samples = 0;
+  std::vector<int64_t> src_xyz;
+  std::vector<int32_t> src_field, src_type;
+  std::vector<double> samples;
+  int n_rec = 0;
+  std::vector<int64_t> rec_xyz;
+  std::vector<int32_t> rec_field;
+  int tb_depth = 0;
+};
+
+namespace {
+
+using Clock = std::chrono::steady_clock;
+
+size_t storage_size(int precision) {
+  return precision == PFDTD_F64 ? 8 : (precision == PFDTD_F32 ? 4 : 2);
+}
+size_t arith_size(int precision) { return precision == PFDTD_F64 ? 8 : 4; }
+
+struct Job {
+  pfdtd_request* req = nullptr;
+  int state = PFDTD_REQ_QUEUED;
+  pfdtd_domain* dom = nullptr;
+  uint64_t bytes = 0;
+  Clock::time_point t_submit, t_admit, t_done;
+  std::vector<uint8_t> result;
+  std::string error;
+};
+
+}  // namespace
+
+struct pfdtd_server {
+  int device = 0;
+  uint64_t budget = 0;
+  int max_active = 1;
+  std::mutex mu;
+  std::condition_variable cv_sched, cv_done;
+  std::deque<int64_t> queue;
+  std::vector<int64_t> active;
+  std::map<int64_t, Job> jobs;
+  int64_t next_ticket = 1;
+  bool stop = false;
+  int in_transit = 0;  // requests being admitted or retired with the lock released
+  std::thread thread;
+  pfdtd_server_stats st{};
+};
+
+namespace {
+
+uint64_t estimate_bytes(const pfdtd_request* r) {
+  const uint64_t es = storage_size(r->precision), as = arith_size(r->precision);
+  const uint64_t N = (uint64_t)(r->X * r->Y * r->Z), K = (uint64_t)r->fields;
+  const uint64_t align = 256 / es;
+  const uint64_t margin = (((uint64_t)r->X + 64) * K + align - 1) / align * align;
+  const uint64_t nfields = r->tb_depth >= 2 ? 4 : 2;
+  uint64_t b = nfields * (N * K + 2 * margin) * es;
+  b += 2 * (N + 1 + (uint64_t)r->X) + N + 64;                  // node bytes, class ids
+  b += (uint64_t)r->n_rec * (uint64_t)r->steps * as;         // receiver buffer
+  b += (uint64_t)r->n_src * (uint64_t)r->n_samples * as + 4096;  // sources
+  bool dif = false;
+  for (int32_t f : r->dif_flags) dif |= f != 0;
+  if (dif) b += (uint64_t)r->n_boundary * (K * 4 * as + 8);   // filter states + node list
+  return b + (4u << 20);                                     // tables, graphs, scratch
+}
+
+// Create and set up the request's domain and queue its run.  Returns the
+// status; on failure the domain is destroyed and the message kept.
+int admit(pfdtd_server* s, Job& j) {
+  pfdtd_request* r = j.req;
+  pfdtd_domain* d = nullptr;
+  int rc = pfdtd_create_batched(r->X, r->Y, r->Z, r->fields, r->precision, s->device, &d);
+  if (rc) return rc;
+  const size_t as = arith_size(r->precision);
+  std::vector<uint8_t> samples(r->samples.size() * as);
+  if (as == 8) {
+    std::memcpy(samples.data(), r->samples.data(), samples.size());
+  } else {
+    for (size_t i = 0; i < r->samples.size(); ++i) {
+      const float v = (float)r->samples[i];
+      std::memcpy(samples.data() + 4 * i, &v, 4);
+    }
+  }
+  if (!rc) rc = pfdtd_set_nodes(d, r->pos.data(), r->mat.data(), 0);
+  if (!rc) rc = pfdtd_set_scheme(d, r->scheme);
+  if (!rc) rc = pfdtd_set_materials(d, r->materials.data(), r->n_mat, r->n_coef);
+  if (!rc && !r->dif_flags.empty())
+    rc = pfdtd_set_dif_filters(d, (int)r->dif_flags.size(), r->dif_flags.data(),
+                               r->dif_coefs.data());
+  if (!rc) rc = pfdtd_set_params(d, r->params);
+  if (!rc)
+    rc = pfdtd_set_sources_batched(d, r->n_src, r->src_xyz.data(), r->src_field.data(),
+                                   r->src_type.data(), samples.data(), r->n_samples);
+  if (!rc) rc = pfdtd_set_receivers_batched(d, r->n_rec, r->rec_xyz.data(), r->rec_field.data());
+  if (!rc) rc = pfdtd_set_temporal_block(d, r->tb_depth);
+  if (!rc) rc = pfdtd_run_async(d, r->steps);
+  if (rc) {
+    j.error = pfdtd_last_error();
+    pfdtd_destroy(d);
+    return rc;
+  }
+  j.dom = d;
+  return PFDTD_OK;
+}
+
+int retire(Job& j) {
+  pfdtd_request* r = j.req;
+  j.result.assign((size_t)r->n_rec * (size_t)r->steps * arith_size(r->precision), 0);
+  int rc = pfdtd_fetch_receivers(j.dom, j.result.data());
+  if (rc) j.error = pfdtd_last_error();
+  pfdtd_destroy(j.dom);
+  j.dom = nullptr;
+  return rc;
+}
+
+void scheduler(pfdtd_server* s) {
+  std::unique_lock<std::mutex> lk(s->mu);
+  for (;;) {
+    bool progress = false;
+    // retire finished requests
+    for (size_t i = 0; i < s->active.size();) {
+      Job& j = s->jobs[s->active[i]];
+      int done = 0;
+      const int q = pfdtd_query(j.dom, &done);
+      if (q == PFDTD_OK && !done) {
+        ++i;
+        continue;
+      }
+      s->active.erase(s->active.begin() + (ptrdiff_t)i);
+      s->in_transit++;
+      lk.unlock();
+      const int rc = retire(j);
+      lk.lock();
+      s->in_transit--;
+      j.t_done = Clock::now();
+      j.state = rc == PFDTD_OK && q == PFDTD_OK ? PFDTD_REQ_DONE : PFDTD_REQ_FAILED;
+      s->st.bytes_in_use -= j.bytes;
+      s->st.running = (int64_t)s->active.size();
+      if (j.state == PFDTD_REQ_DONE) {
+        s->st.completed++;
+        const pfdtd_request* r = j.req;
+        s->st.node_updates += (double)r->X * (double)r->Y * (double)(r->Z - 2) *
+                              (double)r->steps * (double)r->fields;
+      } else {
+        s->st.failed++;
+      }
+      progress = true;
+      s->cv_done.notify_all();
+    }
+    // admit in arrival order while a slot and the memory are free
+    while (!s->stop && !s->queue.empty() && (int)s->active.size() < s->max_active) {
+      const int64_t t = s->queue.front();
+      Job& j = s->jobs[t];
+      if (s->st.bytes_in_use + j.bytes > s->budget) break;
+      s->queue.pop_front();
+      s->st.queued = (int64_t)s->queue.size();
+      s->st.bytes_in_use += j.bytes;
+      s->st.bytes_peak = std::max(s->st.bytes_peak, s->st.bytes_in_use);
+      j.state = PFDTD_REQ_RUNNING;
+      j.t_admit = Clock::now();
+      s->in_transit++;
+      lk.unlock();
+      const int rc = admit(s, j);
+      lk.lock();
+      s->in_transit--;
+      if (rc) {
+        j.state = PFDTD_REQ_FAILED;
+        j.t_done = Clock::now();
+        s->st.bytes_in_use -= j.bytes;
+        s->st.failed++;
+        s->cv_done.notify_all();
+      } else {
+        s->active.push_back(t);
+        s->st.admitted++;
+        s->st.running = (int64_t)s->active.size();
+        s->st.max_running = std::max<int>(s->st.max_running, (int)s->active.size());
+      }
+      progress = true;
+    }
+    if (s->stop && s->active.empty()) break;
+    if (!progress) s->cv_sched.wait_for(lk, std::chrono::microseconds(200));
+  }
+  // queued requests left at shutdown fail
+  for (int64_t t : s->queue) {
+    Job& j = s->jobs[t];
+    j.state = PFDTD_REQ_FAILED;
+    j.error = "server stopped before admission";
+    s->st.failed++;
+  }
+  s->queue.clear();
+  s->cv_done.notify_all();
+}
+
+int check_req(const pfdtd_request* r) {
+  return r ? PFDTD_OK : fail(PFDTD_ERR_ARG, "null request");
+}
+
+}  // namespace
+
+extern "C" {
+
+int pfdtd_request_create(int64_t dim_x, int64_t dim_y, int64_t dim_z, int fields, int precision,
+                         int scheme, int64_t steps, pfdtd_request** out) {
+  if (!out) return fail(PFDTD_ERR_ARG, "null output");
+  if (dim_x <= 0 || dim_y <= 0 || dim_z < 3 || steps < 0)
+    return fail(PFDTD_ERR_ARG, "invalid dimensions or step count");
+  if (fields < 1 || fields > 64 || (fields & (fields - 1)))
+    return fail(PFDTD_ERR_ARG, "fields must be a power of two in 1..64");
+  if (precision < PFDTD_F32 || precision > PFDTD_BF16) return fail(PFDTD_ERR_ARG, "precision");
+  if (scheme < PFDTD_SRL_FORWARD || scheme > PFDTD_IWB) return fail(PFDTD_ERR_ARG, "scheme");
+  pfdtd_request* r = new pfdtd_request();
+  r->X = dim_x;
+  r->Y = dim_y;
+  r->Z = dim_z;
+  r->fields = fields;
+  r->precision = precision;
+  r->scheme = scheme;
+  r->steps = steps;
+  *out = r;
+  return PFDTD_OK;
+}
+
+int pfdtd_request_set_nodes(pfdtd_request* r, const uint8_t* pos, const uint8_t* mat) {
+  if (int rc = check_req(r)) return rc;
+  if (!pos || !mat) return fail(PFDTD_ERR_ARG, "null node arrays");
+  const size_t n = (size_t)(r->X * r->Y * r->Z);
+  r->pos.assign(pos, pos + n);
+  r->mat.assign(mat, mat + n);
+  int64_t nb = 0;
+  for (size_t i = 0; i < n; ++i) {
+    const uint8_t p = r->pos[i];
+    const bool inside = p & 0x80u;
+    const bool boundary = r->scheme == PFDTD_SRL_FORWARD || r->scheme == PFDTD_SHARED
+                              ? (p & 0x7Fu) != 6
+                              : (p & 0x07u) != 0;
+    nb += inside && boundary;
+  }
+  r->n_boundary = nb;
+  r->nodes_set = true;
+  return PFDTD_OK;
+}
+
+int pfdtd_request_set_voxels(pfdtd_request* r, const uint8_t* bid, const uint8_t* mat) {
+  if (int rc = check_req(r)) return rc;
+  if (!bid || !mat) return fail(PFDTD_ERR_ARG, "null voxel arrays");
+  const size_t n = (size_t)(r->X * r->Y * r->Z);
+  std::vector<uint8_t> p(bid, bid + n), m(mat, mat + n);
+  const int centred = r->scheme == PFDTD_SRL || r->scheme == PFDTD_IWB;
+  if (int rc = pfdtd_encode_nodes_host(centred, p.data(), m.data(), (int64_t)n)) return rc;
+  return pfdtd_request_set_nodes(r, p.data(), m.data());
+}
+
+int pfdtd_request_set_materials(pfdtd_request* r, const double* table, int n_mat, int n_coef) {
+  if (int rc = check_req(r)) return rc;
+  if (!table || n_mat <= 0 || n_coef <= 0) return fail(PFDTD_ERR_ARG, "invalid material table");
+  r->materials.assign(table, table + (size_t)n_mat * n_coef);
+  r->n_mat = n_mat;
+  r->n_coef = n_coef;
+  return PFDTD_OK;
+}
+
+int pfdtd_request_set_dif_filters(pfdtd_request* r, int n_mat, const int32_t* flags,
+                                  const double* coefs) {
+  if (int rc = check_req(r)) return rc;
+  if (n_mat < 0 || (n_mat > 0 && (!flags || !coefs))) return fail(PFDTD_ERR_ARG, "filters");
+  r->dif_flags.assign(flags, flags + n_mat);
+  r->dif_coefs.assign(coefs, coefs + (size_t)n_mat * 7);
+  return PFDTD_OK;
+}
+
+int pfdtd_request_set_params(pfdtd_request* r, const double params[4]) {
+  if (int rc = check_req(r)) return rc;
+  if (!params) return fail(PFDTD_ERR_ARG, "null parameters");
+  std::memcpy(r->params, params, sizeof(r->params));
+  return PFDTD_OK;
+}
+
+int pfdtd_request_set_sources(pfdtd_request* r, int n, const int64_t* xyz, const int32_t* field,
+                              const int32_t* type, const double* samples, int64_t n_samples) {
+  if (int rc = check_req(r)) return rc;
+  if (n < 0 || n_samples < 0 || (n > 0 && (!xyz || !type || (n_samples > 0 && !samples))))
+    return fail(PFDTD_ERR_ARG, "invalid source arrays");
+  r->n_src = n;
+  r->n_samples = n_samples;
+  r->src_xyz.assign(xyz, xyz + 3 * (size_t)n);
+  if (field) r->src_field.assign(field, field + n);
+  else r->src_field.assign(n, 0);
+  r->src_type.assign(type, type + n);
+  r->samples.assign(samples, samples + (size_t)n * (size_t)n_samples);
+  return PFDTD_OK;
+}
+
+int pfdtd_request_set_receivers(pfdtd_request* r, int n, const int64_t* xyz,
+                                const int32_t* field) {
+  if (int rc = check_req(r)) return rc;
+  if (n < 0 || (n > 0 && !xyz)) return fail(PFDTD_ERR_ARG, "invalid receiver array");
+  r->n_rec = n;
+  r->rec_xyz.assign(xyz, xyz + 3 * (size_t)n);
+  if (field) r->rec_field.assign(field, field + n);
+  else r->rec_field.assign(n, 0);
+  return PFDTD_OK;
+}
+
+int pfdtd_request_set_temporal_block(pfdtd_request* r, int depth) {
+  if (int rc = check_req(r)) return rc;
+  if (depth != 0 && (depth < 2 || depth > 4)) return fail(PFDTD_ERR_ARG, "depth 0, 2, 3 or 4");
+  r->tb_depth = depth;
+  return PFDTD_OK;
+}
+
+int pfdtd_request_bytes(const pfdtd_request* r, uint64_t* bytes) {
+  if (int rc = check_req(r)) return rc;
+  if (!bytes) return fail(PFDTD_ERR_ARG, "null output");
+  *bytes = estimate_bytes(r);
+  return PFDTD_OK;
+}
+
+int pfdtd_request_destroy(pfdtd_request* r) {
+  delete r;
+  return PFDTD_OK;
+}
+
+int pfdtd_server_create(int device, uint64_t hbm_budget, int max_active, pfdtd_server** out) {
+  if (!out) return fail(PFDTD_ERR_ARG, "null output");
+  if (hbm_budget == 0 || max_active < 1) return fail(PFDTD_ERR_ARG, "budget and slots");
+  int n = 0;
+  if (int rc = pfdtd_device_count(&n)) return rc;
+  if (device < 0 || device >= n) return fail(PFDTD_ERR_ARG, "device index out of range");
+  pfdtd_server* s = new pfdtd_server();
+  s->device = device;
+  s->budget = hbm_budget;
+  s->max_active = max_active;
+  s->thread = std::thread(scheduler, s);
+  *out = s;
+  return PFDTD_OK;
+}
+
+int pfdtd_server_submit(pfdtd_server* s, pfdtd_request* r, int64_t* ticket) {
+  if (!s || !r || !ticket) return fail(PFDTD_ERR_ARG, "null argument");
+  if (!r->nodes_set || r->n_mat <= 0) return fail(PFDTD_ERR_STATE, "request without room or materials");
+  const uint64_t bytes = estimate_bytes(r);
+  std::lock_guard<std::mutex> g(s->mu);
+  if (s->stop) return fail(PFDTD_ERR_STATE, "server stopping");
+  const int64_t t = s->next_ticket++;
+  Job& j = s->jobs[t];
+  j.req = r;
+  j.bytes = bytes;
+  j.t_submit = Clock::now();
+  s->st.submitted++;
+  if (bytes > s->budget) {
+    j.state = PFDTD_REQ_FAILED;
+    j.error = "request larger than the server's memory budget";
+    j.t_admit = j.t_done = j.t_submit;
+    s->st.failed++;
+    *ticket = t;
+    return fail(PFDTD_ERR_NOMEM, j.error);
+  }
+  s->queue.push_back(t);
+  s->st.queued = (int64_t)s->queue.size();
+  *ticket = t;
+  s->cv_sched.notify_one();
+  return PFDTD_OK;
+}
+
+int pfdtd_server_wait(pfdtd_server* s, int64_t ticket, double timeout_s, int* state) {
+  if (!s) return fail(PFDTD_ERR_ARG, "null server");
+  std::unique_lock<std::mutex> lk(s->mu);
+  auto it = s->jobs.find(ticket);
+  if (it == s->jobs.end()) return fail(PFDTD_ERR_ARG, "unknown ticket");
+  auto finished = [&] {
+    return it->second.state == PFDTD_REQ_DONE || it->second.state == PFDTD_REQ_FAILED;
+  };
+  if (timeout_s < 0) s->cv_done.wait(lk, finished);
+  else s->cv_done.wait_for(lk, std::chrono::duration<double>(timeout_s), finished);
+  if (state) *state = it->second.state;
+  return PFDTD_OK;
+}
+
+int pfdtd_server_result(pfdtd_server* s, int64_t ticket, void* out, double times[3]) {
+  if (!s) return fail(PFDTD_ERR_ARG, "null server");
+  std::lock_guard<std::mutex> g(s->mu);
+  auto it = s->jobs.find(ticket);
+  if (it == s->jobs.end()) return fail(PFDTD_ERR_ARG, "unknown ticket");
+  const Job& j = it->second;
+  if (j.state == PFDTD_REQ_FAILED) return fail(PFDTD_ERR_STATE, "request failed: " + j.error);
+  if (j.state != PFDTD_REQ_DONE) return fail(PFDTD_ERR_STATE, "request not finished");
+  if (out && !j.result.empty()) std::memcpy(out, j.result.data(), j.result.size());
+  if (times) {
+    times[0] = std::chrono::duration<double>(j.t_admit - j.t_submit).count();
+    times[1] = std::chrono::duration<double>(j.t_done - j.t_admit).count();
+    times[2] = std::chrono::duration<double>(j.t_done - j.t_submit).count();
+  }
+  return PFDTD_OK;
+}
+
+const char* pfdtd_server_request_error(pfdtd_server* s, int64_t ticket) {
+  static thread_local std::string msg;
+  msg.clear();
+  if (!s) return msg.c_str();
+  std::lock_guard<std::mutex> g(s->mu);
+  auto it = s->jobs.find(ticket);
+  if (it != s->jobs.end()) msg = it->second.error;
+  return msg.c_str();
+}
+
+int pfdtd_server_release(pfdtd_server* s, int64_t ticket) {
+  if (!s) return fail(PFDTD_ERR_ARG, "null server");
+  std::lock_guard<std::mutex> g(s->mu);
+  auto it = s->jobs.find(ticket);
+  if (it == s->jobs.end()) return fail(PFDTD_ERR_ARG, "unknown ticket");
+  if (it->second.state != PFDTD_REQ_DONE && it->second.state != PFDTD_REQ_FAILED)
+    return fail(PFDTD_ERR_STATE, "request not finished");
+  delete it->second.req;
+  s->jobs.erase(it);
+  return PFDTD_OK;
+}
+
+int pfdtd_server_stats_get(pfdtd_server* s, pfdtd_server_stats* st) {
+  if (!s || !st) return fail(PFDTD_ERR_ARG, "null argument");
+  std::lock_guard<std::mutex> g(s->mu);
+  *st = s->st;
+  return PFDTD_OK;
+}
+
+int pfdtd_server_drain(pfdtd_server* s, double timeout_s) {
+  if (!s) return fail(PFDTD_ERR_ARG, "null server");
+  std::unique_lock<std::mutex> lk(s->mu);
+  auto idle = [&] { return s->queue.empty() && s->active.empty() && s->in_transit == 0; };
+  if (timeout_s < 0) s->cv_done.wait(lk, idle);
+  else if (!s->cv_done.wait_for(lk, std::chrono::duration<double>(timeout_s), idle))
+    return fail(PFDTD_ERR_STATE, "requests still pending after the timeout");
+  return PFDTD_OK;
+}
+
+int pfdtd_server_destroy(pfdtd_server* s) {
+  if (!s) return PFDTD_OK;
+  {
+    std::lock_guard<std::mutex> g(s->mu);
+    s->stop = true;
+    s->cv_sched.notify_all();
+  }
+  if (s->thread.joinable()) s->thread.join();
+  for (auto& kv : s->jobs) delete kv.second.req;
+  delete s;
+  return PFDTD_OK;
+}
+
+}  // extern "C"

@@ -9,9 +9,11 @@ namespace {
 
 // Voxelizer id 0..27 -> centred DIR/SIGN byte, the values of
 // src/kernels/cudaMesh.cu:363-480 in table form.
-__constant__ uint8_t c_kowalczyk[28] = {
-    0x00, 0xC7, 0xD7, 0xE7, 0xF7, 0x87, 0x97, 0xA7, 0xB7, 0xC6, 0xE6, 0xC5, 0xD5, 0x86,
-    0xA6, 0x85, 0x95, 0x83, 0x93, 0xA3, 0xB3, 0xC4, 0xA2, 0x82, 0x91, 0x81, 0x84, 0x80};
+#define PFDTD_KOWALCZYK_BYTES                                                                 \
+  {0x00, 0xC7, 0xD7, 0xE7, 0xF7, 0x87, 0x97, 0xA7, 0xB7, 0xC6, 0xE6, 0xC5, 0xD5, 0x86,           \
+   0xA6, 0x85, 0x95, 0x83, 0x93, 0xA3, 0xB3, 0xC4, 0xA2, 0x82, 0x91, 0x81, 0x84, 0x80}
+__constant__ uint8_t c_kowalczyk[28] = PFDTD_KOWALCZYK_BYTES;
+const uint8_t h_kowalczyk[28] = PFDTD_KOWALCZYK_BYTES;
 
 // toBilbao / toKowalczyk applied per node (cudaMesh.cu:482-498).
 __global__ void k_encode(int centred, uint8_t* __restrict__ pos, uint8_t* __restrict__ mat,
@@ -115,6 +117,20 @@ using namespace pfdtd;
 
 extern "C" {
 
+int pfdtd_encode_nodes_host(int centred, uint8_t* pos, uint8_t* mat, int64_t n) {
+  if ((!pos || !mat) && n > 0) return fail(PFDTD_ERR_ARG, "invalid node arrays");
+  for (int64_t i = 0; i < n; ++i) {
+    const unsigned k = pos[i];
+    if (k == 0) {
+      mat[i] = 0;
+    } else if (k <= 27) {
+      if (centred) pos[i] = h_kowalczyk[k];
+      else pos[i] = (uint8_t)((k <= 8 ? 3u : (k <= 20 ? 4u : (k <= 26 ? 5u : 6u))) | 0x80u);
+    }
+  }
+  return PFDTD_OK;
+}
+
 int pfdtd_encode_nodes(int centred, uint8_t* d_pos, uint8_t* d_mat, int64_t n, int device) {
   if (!d_pos || !d_mat || n < 0) return fail(PFDTD_ERR_ARG, "invalid node arrays");
   if (n == 0) return PFDTD_OK;
@@ -132,8 +148,9 @@ int pfdtd_count_boundaries(const uint8_t* d_pos, int64_t n, uint8_t air_value,
   if (!d_pos || n < 0 || !air || !boundary) return fail(PFDTD_ERR_ARG, "invalid arguments");
   DevGuard g(device);
   unsigned long long* d_counts = nullptr;
-  PFDTD_CK(cudaMalloc((void**)&d_counts, 2 * sizeof(unsigned long long)));
-  PFDTD_CK(cudaMemset(d_counts, 0, 2 * sizeof(unsigned long long)));
+  // stream-ordered scratch on the legacy stream: no device-wide synchronisation
+  PFDTD_CK(cudaMallocAsync((void**)&d_counts, 2 * sizeof(unsigned long long), 0));
+  PFDTD_CK(cudaMemsetAsync(d_counts, 0, 2 * sizeof(unsigned long long), 0));
   if (n > 0) {
     k_count<<<grid_for(n), 256>>>(d_pos, n, air_value, outside_value, d_counts);
     count_launch();
@@ -141,7 +158,7 @@ int pfdtd_count_boundaries(const uint8_t* d_pos, int64_t n, uint8_t air_value,
   cudaError_t e = cudaGetLastError();
   unsigned long long h[2] = {0, 0};
   if (e == cudaSuccess) e = cudaMemcpy(h, d_counts, sizeof(h), cudaMemcpyDeviceToHost);
-  cudaFree(d_counts);
+  cudaFreeAsync(d_counts, 0);
   if (e != cudaSuccess) return cuda_fail(e, "boundary count", __FILE__, __LINE__);
   *air = (uint32_t)h[0];
   *boundary = (uint32_t)h[1];

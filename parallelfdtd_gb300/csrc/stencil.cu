@@ -400,15 +400,15 @@ int build_classes(pfdtd_domain* d) {
   const int n_classes = (int)keys.size();
   const int cls_bytes = n_classes <= 256 ? 1 : 2;
   if (d->d_cls == nullptr || cls_bytes > d->cls_bytes) {
-    if (d->d_cls) PFDTD_CK(cudaFree(d->d_cls));
+    d->release(d->d_cls);
     d->d_cls = nullptr;
-    if (cudaMalloc(&d->d_cls, (size_t)d->N * cls_bytes + 64) != cudaSuccess)
+    if (d->alloc(&d->d_cls, (size_t)d->N * cls_bytes + 64) != cudaSuccess)
       return fail(PFDTD_ERR_NOMEM, "class id allocation failed");
   }
   d->cls_bytes = cls_bytes;
-  if (d->d_ctab) PFDTD_CK(cudaFree(d->d_ctab));
+  d->release(d->d_ctab);
   d->d_ctab = nullptr;
-  PFDTD_CK(cudaMalloc(&d->d_ctab, tab.size()));
+  PFDTD_CK(d->alloc(&d->d_ctab, tab.size()));
   PFDTD_CK(cudaMemcpyAsync(d->d_ctab, tab.data(), tab.size(), cudaMemcpyHostToDevice, s));
   uint16_t* d_lut = nullptr;
   PFDTD_CK(cudaMallocAsync((void**)&d_lut, 65536 * sizeof(uint16_t), s));

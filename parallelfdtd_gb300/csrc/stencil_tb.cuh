@@ -49,13 +49,6 @@
 namespace pfdtd {
 namespace tb {
 
-// Forward rule with the packed FP32x2 add / multiply (off: scalar rounded
-// intrinsics, as the per-step kernels).
-#ifndef PFDTD_TB_PACKED
-#define PFDTD_TB_PACKED 0
-#endif
-constexpr bool kPackedF32x2 = PFDTD_TB_PACKED != 0;
-
 constexpr int kNS = 4;        // cp.async stages (loads run two iterations ahead)
 constexpr int kMaxSrc = 64;   // sources per domain the kernel's lists can hold
 constexpr int kMaxRec = 256;  // receivers per domain
@@ -200,10 +193,7 @@ k_update_tb(const S* __restrict__ Pa, const S* __restrict__ Pb, S* __restrict__ 
   using Rf = Rn<float>;
   extern __shared__ __align__(128) unsigned char smem_raw[];
   unsigned char* smem = (unsigned char*)(((uintptr_t)smem_raw + 127) & ~(uintptr_t)127);
-  constexpr bool kPairs = SCHEME == 0 && kPackedF32x2;
-  __shared__ PackedCoef<float> stab[kPairs ? 1 : 256];
-  // packed forward rule: a, b and -c by class, read in element pairs
-  __shared__ float sa[kPairs ? 256 : 1], sb[kPairs ? 256 : 1], snc[kPairs ? 256 : 1];
+  __shared__ PackedCoef<float> stab[256];
   __shared__ int s_nsrc, s_nrec;
   ListEntry* src_list = (ListEntry*)(smem + Sh::LIST_OFF);
   ListEntry* rec_list = src_list + kMaxSrc;
@@ -242,15 +232,8 @@ k_update_tb(const S* __restrict__ Pa, const S* __restrict__ Pb, S* __restrict__ 
     ebase[r] = BATCHED ? (node << kshift) + f0 : node;
   }
 
-  for (int i = tid; i < tab.n && i < 256; i += Sh::THREADS) {
-    if constexpr (kPairs) {
-      sa[i] = tab.a[i];
-      sb[i] = tab.b[i];
-      snc[i] = -tab.c[i];
-    } else {
-      stab[i] = PackedCoef<float>{tab.a[i], tab.b[i], tab.c[i], tab.pos[i]};
-    }
-  }
+  for (int i = tid; i < tab.n && i < 256; i += Sh::THREADS)
+    stab[i] = PackedCoef<float>{tab.a[i], tab.b[i], tab.c[i], tab.pos[i]};
 
   // Sources and receivers inside this CTA's extended tile, in list order
   // (one warp, ballot + prefix count keeps the order of the global lists).
@@ -444,34 +427,6 @@ k_update_tb(const S* __restrict__ Pa, const S* __restrict__ Pb, S* __restrict__ 
               xp[0] = cv[t][r][1]; xp[1] = cv[t][r][2]; xp[2] = cv[t][r][3]; xp[3] = xr[r];
             }
             const uint32_t cw = creg[t][r];
-            if constexpr (SCHEME == 0 && kPackedF32x2) {
-              // Forward rule on element pairs with the packed FP32x2 add and
-              // multiply: each component rounds exactly as __fadd_rn /
-              // __fmul_rn, and x - c*pp is issued as x + (-c)*pp, which IEEE
-              // arithmetic defines to be the same value.
-              const float2 l22 = make_float2(l2, l2);
-#pragma unroll
-              for (int h = 0; h < 2; ++h) {
-                const int e0 = 2 * h, e1 = 2 * h + 1;
-                const unsigned c0 = BATCHED ? cw : ((cw >> (8 * e0)) & 0xFFu);
-                const unsigned c1 = BATCHED ? cw : ((cw >> (8 * e1)) & 0xFFu);
-                float2 s6 = __fadd2_rn(make_float2(fr[t][r][e0], fr[t][r][e1]),
-                                       make_float2(mv[t][r][e0], mv[t][r][e1]));
-                s6 = __fadd2_rn(s6, make_float2(yp[e0], yp[e1]));
-                s6 = __fadd2_rn(s6, make_float2(ym[e0], ym[e1]));
-                s6 = __fadd2_rn(s6, make_float2(xp[e0], xp[e1]));
-                s6 = __fadd2_rn(s6, make_float2(xm[e0], xm[e1]));
-                float2 u = __fadd2_rn(
-                    __fmul2_rn(make_float2(sb[c0], sb[c1]),
-                               make_float2(cv[t][r][e0], cv[t][r][e1])),
-                    __fmul2_rn(l22, s6));
-                u = __fadd2_rn(u, __fmul2_rn(make_float2(snc[c0], snc[c1]),
-                                             make_float2(past[e0], past[e1])));
-                u = __fmul2_rn(make_float2(sa[c0], sa[c1]), u);
-                out[e0] = rnd<S>(u.x);
-                out[e1] = rnd<S>(u.y);
-              }
-            } else {
 #pragma unroll
             for (int e = 0; e < 4; ++e) {
               const unsigned c = BATCHED ? cw : ((cw >> (8 * e)) & 0xFFu);
@@ -500,7 +455,6 @@ k_update_tb(const S* __restrict__ Pa, const S* __restrict__ Pb, S* __restrict__ 
                                          Rf::mul(k.c, past[e])));
               }
               out[e] = rnd<S>(o);
-            }
             }
           }
           if (!rin[r]) zero4(out);

@@ -1,0 +1,45 @@
+"""CPU: request construction, footprint estimate and the serving trace."""
+import numpy as np
+import pytest
+
+from parallelfdtd_gb300 import _lib as L
+from parallelfdtd_gb300.serving import Request, serving_trace
+
+
+def test_request_bytes_estimate(built):
+    r = Request((64, 48, 40), 100, fields=4, precision="f32")
+    r.set_voxels(np.zeros(64 * 48 * 40, np.uint8), np.zeros(64 * 48 * 40, np.uint8))
+    r.set_receivers([(5, 5, 5)] * 8, fields=[0] * 8)
+    b = r.bytes()
+    n = 64 * 48 * 40
+    assert b >= 2 * n * 4 * 4 + 3 * n + 8 * 100 * 4
+    assert b < 2 * n * 4 * 4 + 3 * n + 8 * 100 * 4 + (8 << 20)
+    r.set_temporal_block(2)
+    assert r.bytes() > b + 2 * n * 4 * 4 - 1
+
+
+def test_request_validation(built):
+    with pytest.raises(L.PfdtdError):
+        Request((64, 48, 2), 100)
+    with pytest.raises(L.PfdtdError):
+        Request((64, 48, 40), 100, fields=3)
+    r = Request((16, 16, 16), 10)
+    with pytest.raises(L.PfdtdError):
+        r.set_temporal_block(5)
+
+
+def test_serving_trace_is_seeded_and_bounded():
+    a = serving_trace(200, seed=1)
+    b = serving_trace(200, seed=1)
+    assert a == b
+    arr = np.array([t.arrival for t in a])
+    assert np.all(np.diff(arr) > 0)
+    rate = len(a) / arr[-1]
+    assert 14 < rate < 27  # Poisson, mean 20 per second
+    dims = np.array([t.dims for t in a])
+    assert dims.min() >= 64 and dims.max() <= 512 and np.all(dims % 4 == 0)
+    assert {t.scheme for t in a} == {"forward", "iwb"}
+    steps = np.array([t.steps for t in a])
+    assert steps.min() >= 500 and steps.max() <= 8000
+    srcs = np.array([t.n_src for t in a])
+    assert srcs.min() >= 1 and srcs.max() <= 16
