@@ -64,6 +64,16 @@ def parse():
     p.add_argument("--serve-seed", type=int, default=0)
     p.add_argument("--serve-slots", type=int, default=8)
     p.add_argument("--serve-budget-gb", type=float, default=160.0)
+    p.add_argument("--scheme", default="forward", choices=["forward", "centred", "iwb"],
+                   help="update scheme (iwb: the 27-point compact scheme at lambda = 1)")
+    p.add_argument("--dif", action="store_true",
+                   help="3rd-order frequency-dependent admittance on every material (seeded "
+                        "stable poles |p| < 0.95, positive real)")
+    p.add_argument("--iwb-lambda", type=float, default=1.0,
+                   help="Courant number of the IWB scheme (1 = its stability limit)")
+    p.add_argument("--vs-f64", action="store_true",
+                   help="also run the same workload with FP64 fields and report each "
+                        "receiver's relative L2 error against it")
     p.add_argument("--tb", type=int, default=0,
                    help="temporal block depth (0 = one update kernel per step; 2, 3, 4)")
     p.add_argument("--fields", type=int, default=1,
@@ -327,12 +337,25 @@ def main():
     samples = np.repeat(rooms.impulse(S)[None], len(src), axis=0).astype(
         np.float64 if prec == "f64" else np.float32)
     esize = {"f32": 4, "f64": 8, "f16": 2, "bf16": 2}[prec]
+    dif = None
+    if a.dif:
+        from parallelfdtd_gb300 import materials
+        n_mat = room.admittance.shape[0]
+        dif = (np.ones(n_mat, np.int32),
+               materials.dif_table(materials.positive_real_filters(n_mat, 3, seed=77), 3))
+
+    def setup(dom):
+        dom.set_voxels(room.bid, room.mat, centred=(a.scheme != "forward"))
+        dom.set_materials(room.admittance)
+        if dif is not None:
+            dom.set_dif_filters(*dif)
+        dom.set_params(default_params(scheme=a.scheme,
+                                      lam=a.iwb_lambda if a.scheme == "iwb" else None))
+        dom.set_scheme(a.scheme)
+
     d = Domain(dims, prec, device=local, fields=K)
-    d.set_voxels(room.bid, room.mat, centred=False)
+    setup(d)
     pos_host, mat_host = d.get_nodes()
-    d.set_materials(room.admittance)
-    d.set_params(default_params())
-    d.set_scheme("forward")
     d.set_sources(src, [1] * len(src), samples, fields=src_f)
     d.set_receivers(rec, fields=rec_f)
     d.set_temporal_block(a.tb)
@@ -390,6 +413,7 @@ def main():
     nodes = X * Y * (Z - 2)
     bpu = bytes_per_update(prec, K)
     T = a.tb if a.tb else 1
+    n_dif = d.dif_count() if a.dif else 0
     if T > 1:
         # a blocked launch advances T steps; its compulsory traffic is one
         # read of P^n, P^{n-1} and the class ids and one write of the two
@@ -407,12 +431,14 @@ def main():
     for _ in range(max(1, a.warmup)):
         d.set_nodes(pos_host, mat_host)
         d.set_sources(src, [1] * len(src), samples, fields=src_f)
+        d.reset_fields()
         d.run(S, out=out_host)
     barrier()
     t0 = time.perf_counter()
     for _ in range(a.steps):
         d.set_nodes(pos_host, mat_host)
         d.set_sources(src, [1] * len(src), samples, fields=src_f)
+        d.reset_fields()
         d.run(S, out=out_host)
     barrier()
     e2e_s = (time.perf_counter() - t0) / a.steps
@@ -425,9 +451,23 @@ def main():
            "h2d_bytes_per_step": int(2 * room.n_nodes + samples.nbytes),
            "d2h_bytes_per_step": int(n_rec * S * (8 if prec == "f64" else 4))}
 
+    err64 = None
+    if a.vs_f64 and prec != "f64":
+        ref = np.zeros((n_rec, S), dtype=np.float64)
+        with Domain(dims, "f64", device=local, fields=K) as d64:
+            setup(d64)
+            d64.set_sources(src, [1] * len(src), samples.astype(np.float64), fields=src_f)
+            d64.set_receivers(rec, fields=rec_f)
+            d64.run(S, out=ref)
+        num = np.linalg.norm(out_host.astype(np.float64) - ref, axis=1)
+        den = np.maximum(np.linalg.norm(ref, axis=1), 1e-300)
+        e = num / den
+        err64 = {"max_rel_l2": float(e.max()), "median_rel_l2": float(np.median(e)),
+                 "per_receiver": [float(v) for v in e]}
+
     if rank == 0:
         base = None
-        if not a.no_cpu_baseline and world == 1:
+        if not a.no_cpu_baseline and world == 1 and a.scheme == "forward" and not a.dif:
             base = cpu_baseline(room, src, rec, a.cpu_seconds)
         src_txt = (f"soft impulse, {N_REC} air receivers" if K == 1 else
                    f"{K} fields (one soft impulse each), 4 receivers per field")
@@ -437,8 +477,13 @@ def main():
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
             "dtype": prec, "data": "synthetic",
             "config": {"workload": f"boxes room {X}x{Y}x{Z}, 40 boxes (edges 8-64), 20 materials "
-                                   f"U(0.01,0.9), {src_txt}, {S} leapfrog steps, SRL forward, "
+                                   f"U(0.01,0.9){', 3rd-order DIF admittance' if a.dif else ''}"
+                                   f", {src_txt}, {S} leapfrog steps, "
+                                   f"{ {'forward': 'SRL forward', 'centred': 'SRL centred', 'iwb': 'IWB 27-point'}[a.scheme]}, "
                                    f"{prec}",
+                       "scheme": a.scheme, "dif_nodes": int(n_dif),
+                       "courant": float(default_params(scheme=a.scheme, lam=a.iwb_lambda
+                                                       if a.scheme == "iwb" else None)[0]),
                        "fdtd_steps_per_step": S, "nodes": X * Y * Z, "fields": K,
                        "temporal_block": a.tb,
                        "bytes_per_update": bpu,
@@ -457,6 +502,8 @@ def main():
             "gpu_launches": int(launches),
             "cpu_baseline": base,
         }
+        if err64 is not None:
+            line["error_vs_f64"] = err64
         print(json.dumps(line), flush=True)
     d.close()
     if world > 1:

@@ -152,14 +152,51 @@ struct RunDesc {
   // b0..b3, a1..a3 (order <= 3, unused coefficients 0).
   const int32_t* dif_flag;   // [n_mat] or null
   const void* dif_coef;      // [n_mat * 7] of T
+  // IWB only, derived by run(): per node the closed-neighbour mask and the
+  // class code (see iwb_geometry).
+  const uint32_t* iwb_mask = nullptr;
+  const uint8_t* iwb_code = nullptr;
 };
+
+// IWB geometry of one node: bit k of the mask is set when the k-th of the 26
+// neighbours (offsets visited for dz, dy, dx in -1, 0, 1, skipping the
+// centre) is closed, i.e. outside the grid or without the inside bit.  The
+// class code is 0 for a node without the inside bit, else
+// 1 + W16 + 64 * face, with W16 = 4 (closed faces) + 2 (closed edges) +
+// (closed corners) and face = 1 when a face neighbour is closed.
+void iwb_geometry(const uint8_t* pos, int64_t N, int64_t X, int64_t XY, int64_t c,
+                  uint32_t* mask, uint8_t* code) {
+  uint32_t m = 0;
+  int w16 = 0, face = 0, k = 0;
+  for (int dz = -1; dz <= 1; ++dz)
+    for (int dy = -1; dy <= 1; ++dy)
+      for (int dx = -1; dx <= 1; ++dx) {
+        const int n = (dx != 0) + (dy != 0) + (dz != 0);
+        if (n == 0) continue;
+        const int64_t i = c + dz * XY + dy * X + dx;
+        const bool open = i >= 0 && i < N && (pos[i] >> 7);
+        if (!open) {
+          m |= 1u << k;
+          w16 += n == 1 ? 4 : (n == 2 ? 2 : 1);
+          face |= n == 1;
+        }
+        ++k;
+      }
+  *mask = m;
+  *code = (pos[c] >> 7) ? (uint8_t)(1 + w16 + 64 * face) : 0;
+}
 
 // Geometric factor G of a boundary node: the loss term of the FI update is
 // beta (p+ - p-) = 2 G Y x with x = (p+ - p-)/2 (forward: beta = 0.5 Y (6-K)
-// lambda, kernels3d.cu:514; centred and IWB: beta = lambda Y axes).
+// lambda, kernels3d.cu:514; centred: beta = lambda Y axes; IWB: pos is the
+// class code, beta = lambda Y W16/16 when a face neighbour is closed).
 template <typename T>
 T geometric_factor(int scheme, unsigned pos, T lambda) {
   if (scheme == 0) return (T)0.5 * (((T)6 - (T)(pos & kForwardMask)) * lambda);
+  if (scheme == 3) {
+    if (pos < 65) return (T)0;  // outside, or closed diagonally only
+    return lambda * ((T)(int)(pos - 65) * (T)0.0625);
+  }
   const T ndirs = (T)((pos & 1u) + ((pos >> 1) & 1u) + ((pos >> 2) & 1u));
   return lambda * ndirs;
 }
@@ -168,44 +205,46 @@ T geometric_factor(int scheme, unsigned pos, T lambda) {
 // reference's UpdateType has SRL schemes only, SimulationParameters.h:39).
 //
 // Interior: p+ = d1*S1 + d2*S2 + d3*S3 + d4*p - p-, with S1/S2/S3 the sums of
-// the 6 face, 12 edge and 8 corner neighbours and (lambda, a, b) = (1, 1/4,
-// 1/16): d1 = 1/4, d2 = 1/8, d3 = 1/16, d4 = -3/2 (Kowalczyk & van Walstijn,
-// IEEE TASLP 19(1), 2011).
-// Boundary (centred node encoding, cudaMesh.h:35-44): along each boundary
-// axis the neighbour offsets that point out of the room (toward the missing
-// side: -1 when SIGN is set, +1 otherwise) are reflected to the opposite
-// side, and the locally reacting admittance Y adds the loss term
-// beta = lambda * Y * (number of boundary axes):
+// the 6 face, 12 edge and 8 corner neighbours and (a, b) = (1/4, 1/16):
+// d1 = l2/4, d2 = l2/8, d3 = l2/16, d4 = 2 - 7/2 l2 (l2 = lambda^2; at the
+// scheme's stability limit lambda = 1: 1/4, 1/8, 1/16, -3/2; Kowalczyk & van
+// Walstijn, IEEE TASLP 19(1), 2011), evaluated as
+// l2 * ((S1/4 + S2/8) + S3/16) + d4 * p.
+// Boundary (finite-volume closure on the voxel grid): a closed neighbour
+// (see iwb_geometry) contributes the node's own value p, so no flux crosses
+// the closed faces, edges and corners of the node's cell.  The update is then
+// a weighted graph Laplacian over the open nodes, whose spectrum lies inside
+// the full lattice's, so the scheme is energy-stable for lambda <= 1 on any
+// voxel geometry.  A node with a closed face neighbour (a wall node, carrying
+// its wall's material) adds the locally reacting loss
+// beta = lambda * Y * W, W = W16/16 the summed weight of its closed
+// neighbours:
 //   p+ = s * (d1*S1' + d2*S2' + d3*S3' + d4*p - (1 - beta)*p-) / (1 + beta).
 // Canonical evaluation order (shared with the CUDA kernel): offsets visited
 // for dz, dy, dx in -1, 0, 1 (skipping the centre), each added to its class
-// sum in that order; then ((S1*d1 + S2*d2) + S3*d3 + d4*p) - c*p-, times a.
+// sum in that order; then ((l2 * ((S1/4 + S2/8) + S3/16) + d4*p) - c*p-) * a.
 template <typename T, typename St>
-T iwb_node(const St* P, int64_t N, int64_t c, int64_t X, int64_t XY, unsigned pos, T pp, T a,
-           T cc) {
-  const int dirx = pos & 0x01, diry = (pos >> 1) & 1, dirz = (pos >> 2) & 1;
-  const int ox = (pos & 0x10) ? -1 : 1, oy = (pos & 0x20) ? -1 : 1, oz = (pos & 0x40) ? -1 : 1;
+T iwb_node(const St* P, int64_t N, int64_t c, int64_t X, int64_t XY, uint32_t mask, T pp, T a,
+           T cc, T l2) {
+  const T p = (T)to_float(P[c]);
   T s1 = 0, s2 = 0, s3 = 0;
   bool f1 = true, f2 = true, f3 = true;
+  int k = 0;
   for (int dz = -1; dz <= 1; ++dz)
     for (int dy = -1; dy <= 1; ++dy)
       for (int dx = -1; dx <= 1; ++dx) {
         const int n = (dx != 0) + (dy != 0) + (dz != 0);
         if (n == 0) continue;
-        const int mx = (dirx && dx == ox) ? -dx : dx;
-        const int my = (diry && dy == oy) ? -dy : dy;
-        const int mz = (dirz && dz == oz) ? -dz : dz;
-        // Flat neighbours outside the grid read 0, as the zeroed margins
-        // around the device fields do.
-        const int64_t i = c + mz * XY + my * X + mx;
-        const T v = (i >= 0 && i < N) ? (T)to_float(P[i]) : (T)0;
+        const int64_t i = c + dz * XY + dy * X + dx;
+        const T v = ((mask >> k) & 1u) ? p : (T)to_float(P[i]);
+        ++k;
         if (n == 1) { s1 = f1 ? v : s1 + v; f1 = false; }
         else if (n == 2) { s2 = f2 ? v : s2 + v; f2 = false; }
         else { s3 = f3 ? v : s3 + v; f3 = false; }
       }
-  const T p = (T)to_float(P[c]);
-  const T sw = s1 * (T)0.25 + s2 * (T)0.125 + s3 * (T)0.0625;
-  return a * ((sw + (T)(-1.5) * p) - cc * pp);
+  const T sw = l2 * (s1 * (T)0.25 + s2 * (T)0.125 + s3 * (T)0.0625);
+  const T d4 = (T)2 - (T)3.5 * l2;
+  return a * ((sw + d4 * p) - cc * pp);
 }
 
 // One leapfrog update over z in [1, Z-2] writing into Pp.
@@ -234,7 +273,7 @@ int update(const RunDesc& d, const St* P, St* Pp, const std::vector<T>& beta_tab
 #pragma omp parallel for schedule(static) num_threads(d.threads)
   for (int64_t z = 1; z < Z - 1; ++z) {
     for (int64_t c = z * XY; c < (z + 1) * XY; ++c) {
-      const unsigned pos = d.pos[c];
+      const unsigned pos = d.scheme == 3 ? d.iwb_code[c] : d.pos[c];
       const unsigned key = (pos << 8) | d.mat[c];
       T beta = beta_tab[key];
       const T p = to_float(P[c]);
@@ -253,13 +292,14 @@ int update(const RunDesc& d, const St* P, St* Pp, const std::vector<T>& beta_tab
       }
       T ret;
       if (d.scheme == 3) {
-        const T sw = (T)(pos >> kInsideSwitch);
+        const T sw = (T)(pos != 0);
+        const uint32_t mask = d.iwb_mask[c];
         if (slot >= 0) {
-          const T lossless = iwb_node<T, St>(P, XY * Z, c, X, XY, pos, (T)0, (T)1, (T)0);
+          const T lossless = iwb_node<T, St>(P, XY * Z, c, X, XY, mask, (T)0, (T)1, (T)0, l2);
           ret = sw * ((T)1 / ((T)1 + beta)) * ((lossless - ((T)1 - beta) * pp) - g2 * s1);
         } else {
-          ret = iwb_node<T, St>(P, XY * Z, c, X, XY, pos, pp, sw * ((T)1 / ((T)1 + beta)),
-                                (T)1 - beta);
+          ret = iwb_node<T, St>(P, XY * Z, c, X, XY, mask, pp, sw * ((T)1 / ((T)1 + beta)),
+                                (T)1 - beta, l2);
         }
       } else if (d.scheme == 0 && slot >= 0) {
         const T position = (T)(pos & kForwardMask);
@@ -324,7 +364,7 @@ int beta_table(const RunDesc& d, std::vector<T>& beta, std::vector<uint8_t>& val
   std::vector<uint8_t> present(65536, 0);
   const int64_t N = d.X * d.Y * d.Z;
   for (int64_t i = d.X * d.Y; i < N - d.X * d.Y; ++i)
-    present[((unsigned)d.pos[i] << 8) | d.mat[i]] = 1;
+    present[((unsigned)(d.scheme == 3 ? d.iwb_code[i] : d.pos[i]) << 8) | d.mat[i]] = 1;
   for (unsigned key = 0; key < 65536; ++key) {
     if (!present[key]) continue;
     const unsigned pos = key >> 8, m = key & 0xFF;
@@ -336,8 +376,9 @@ int beta_table(const RunDesc& d, std::vector<T>& beta, std::vector<uint8_t>& val
       const T position = (T)(pos & kForwardMask);
       beta[key] = (T)0.5 * (Y * ((T)6 - position) * prm[0]);
     } else if (d.scheme == 3) {
-      const T ndirs = (T)((pos & 1u) + ((pos >> 1) & 1u) + ((pos >> 2) & 1u));
-      beta[key] = Y * prm[0] * ndirs;
+      // pos is the class code: 1 + W16 + 64 * face for inside nodes
+      const T W = pos >= 65 ? (T)(int)(pos - 65) * (T)0.0625 : (T)0;
+      beta[key] = Y * prm[0] * W;
     } else {
       const T dx = (T)(pos & kDirX), dy = (T)((pos & kDirY) >> 1),
               dz = (T)((pos & kDirZ) >> 2);
@@ -352,8 +393,20 @@ int beta_table(const RunDesc& d, std::vector<T>& beta, std::vector<uint8_t>& val
 // inject sources into P (:93-104), update (:109-153), swap (:160),
 // record receivers from the new P (:164-173).
 template <typename T, typename S>
-int run(const RunDesc& d, S* P, S* Pp, T* out) {
-  if (d.X < 1 || d.Y < 1 || d.Z < 3) return -1;
+int run(const RunDesc& d0, S* P, S* Pp, T* out) {
+  if (d0.X < 1 || d0.Y < 1 || d0.Z < 3) return -1;
+  RunDesc d = d0;
+  std::vector<uint32_t> iwb_mask;
+  std::vector<uint8_t> iwb_code;
+  if (d.scheme == 3) {
+    const int64_t N = d.X * d.Y * d.Z;
+    iwb_mask.assign(N, 0);
+    iwb_code.assign(N, 0);
+    for (int64_t c = 0; c < N; ++c)
+      iwb_geometry(d.pos, N, d.X, d.X * d.Y, c, &iwb_mask[c], &iwb_code[c]);
+    d.iwb_mask = iwb_mask.data();
+    d.iwb_code = iwb_code.data();
+  }
   std::vector<T> beta;
   std::vector<uint8_t> valid;
   int rc = beta_table<T>(d, beta, valid);
@@ -367,8 +420,9 @@ int run(const RunDesc& d, S* P, S* Pp, T* out) {
     dif.slot.assign(N, -1);
     int64_t n_slots = 0;
     for (int64_t i = d.X * d.Y; i < N - d.X * d.Y; ++i) {
-      const unsigned pos = d.pos[i];
-      if (!(pos >> kInsideSwitch) || d.mat[i] >= (unsigned)d.n_mat || !d.dif_flag[d.mat[i]]) continue;
+      const unsigned pos = d.scheme == 3 ? d.iwb_code[i] : d.pos[i];
+      const bool inside = d.scheme == 3 ? pos != 0 : (pos >> kInsideSwitch) != 0;
+      if (!inside || d.mat[i] >= (unsigned)d.n_mat || !d.dif_flag[d.mat[i]]) continue;
       if (geometric_factor<T>(d.scheme, pos, l) <= (T)0) continue;
       dif.slot[i] = n_slots++;
     }

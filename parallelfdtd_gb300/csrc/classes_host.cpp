@@ -48,11 +48,14 @@ int eval(int scheme, int quirks, const double* params, const std::vector<double>
     const A Y = (A)materials[mi];
     const A sw = (A)(pos >> 7);
     if (scheme == PFDTD_IWB) {
-      // IWB boundary update (see the kernel): beta = lambda * Y * (boundary axes)
-      const A ndirs = (A)((pos & 0x01u) + ((pos >> 1) & 1u) + ((pos >> 2) & 1u));
-      const A beta = Y * l * ndirs;
-      ca[i] = sw * ((A)1 / ((A)1 + beta));
-      cb[i] = (A)(-1.5);
+      // IWB (finite-volume closure): pos is the geometry code 1 + W16 +
+      // 64 * face of an inside node (0 outside); wall nodes (face = 1) lose
+      // beta = lambda * Y * W16/16, nodes closed only diagonally none.
+      const A swi = (A)(pos != 0);
+      const A W = pos >= 65 ? (A)(int)(pos - 65) * (A)0.0625 : (A)0;
+      const A beta = Y * l * W;
+      ca[i] = swi * ((A)1 / ((A)1 + beta));
+      cb[i] = (A)2 - (A)3.5 * l2;  // d4 = 2 - 7/2 lambda^2 (-3/2 at lambda = 1)
       cc[i] = (A)1 - beta;
     } else if (scheme != PFDTD_SRL) {
       // kernels3d.cu:509-526

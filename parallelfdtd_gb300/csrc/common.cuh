@@ -84,13 +84,14 @@ struct ClassTab {
   int n;
 };
 
-// Tensor maps of the TMA update kernel (stencil_tma.cu): each field viewed as
-// X-wide rows with and without the halo box, and the class ids.
+// Tensor maps of the TMA update kernel (stencil_tma.cu): each field buffer
+// (two, or four with temporal blocking) viewed as X-wide rows with and
+// without the halo box, and the class ids.
 struct TmaState {
-  CUtensorMap halo[2];
-  CUtensorMap tile[2];
+  CUtensorMap halo[4];
+  CUtensorMap tile[4];
   CUtensorMap cls;
-  int64_t key[4] = {0, 0, 0, 0};
+  int64_t key[5] = {0, 0, 0, 0, 0};
   bool ready = false;
   bool attr_set[2][2][2] = {{{false, false}, {false, false}}, {{false, false}, {false, false}}};
 };
@@ -145,6 +146,10 @@ struct pfdtd_domain {
   int cls_bytes = 1;
   void* d_cls = nullptr;     // per node class id (uint8 or uint16)
   void* d_ctab = nullptr;    // coefficient arrays (a|b|c in arithmetic type, then pos u32)
+  // IWB: per node the closed-neighbour mask (26 bits) and the class code
+  // that stands for the position byte in the IWB class key (stencil.cu)
+  uint32_t* d_iwb_mask = nullptr;
+  uint8_t* d_iwb_code = nullptr;
   int64_t class_version = 0;
 
   // sources / receivers
@@ -221,6 +226,8 @@ int launch_dif(pfdtd_domain* d, const void* cur, void* past, cudaStream_t s);
 int launch_dif_init(pfdtd_domain* d, cudaStream_t s);
 int tma_tile_count();
 int launch_update_tma(pfdtd_domain* d, const void* cur, void* past, cudaStream_t s);
+int launch_iwb_tma(pfdtd_domain* d, const void* cur, void* past, cudaStream_t s);
+bool uses_tma(const pfdtd_domain* d);
 // Implemented in stencil_tb.cu
 int tb_usable(const pfdtd_domain* d, std::string* why);
 int launch_tb(pfdtd_domain* d, void* rec_out, int64_t rec_ld, int64_t inject_end, cudaStream_t s);

@@ -99,7 +99,8 @@ __global__ void k_dif_update(const int64_t* __restrict__ list, int64_t n, int ks
                              const void* __restrict__ cls, int cls_bytes,
                              const typename Store<S>::A* __restrict__ dtab, const S* __restrict__ P,
                              S* __restrict__ Pp, typename Store<S>::A* __restrict__ st, int64_t X,
-                             int64_t XY, typename Store<S>::A l2, const uint32_t* __restrict__ cpos) {
+                             int64_t XY, typename Store<S>::A l2, const uint32_t* __restrict__ cpos,
+                             const uint32_t* __restrict__ iwb_mask) {
   using A = typename Store<S>::A;
   using R = Rn<A>;
   using Sto = Store<S>;
@@ -135,24 +136,24 @@ __global__ void k_dif_update(const int64_t* __restrict__ list, int64_t n, int ks
       const A s7 = R::add(R::add(R::add(R::add(R::add(R::add(xm, xp), ym), yp), zp), zm), sb6);
       num = R::sub(R::add(R::sub(R::mul(s7, l2), R::mul(b, p)), R::mul(cc, pp)), R::mul(g2, s1));
     } else {
-      const uint32_t cp = cpos[c];
-      const int ox = (cp & 0x10u) ? -1 : 1, oy = (cp & 0x20u) ? -1 : 1, oz = (cp & 0x40u) ? -1 : 1;
+      // IWB: closed neighbours (mask bits, canonical order) contribute p
+      const uint32_t mk = iwb_mask[node];
       A f1 = (A)0, f2 = (A)0, f3 = (A)0;
       bool n1 = true, n2 = true, n3 = true;
+      int kk = 0;
       for (int dz = -1; dz <= 1; ++dz)
         for (int dy = -1; dy <= 1; ++dy)
           for (int dx = -1; dx <= 1; ++dx) {
             const int nn = (dx != 0) + (dy != 0) + (dz != 0);
             if (nn == 0) continue;
-            const int mx = ((cp & 1u) && dx == ox) ? -dx : dx;
-            const int my = ((cp & 2u) && dy == oy) ? -dy : dy;
-            const int mz = ((cp & 4u) && dz == oz) ? -dz : dz;
-            const A v = Sto::load(P[i + mz * XY + my * X + mx * ks]);
+            const A v = ((mk >> kk) & 1u) ? p : Sto::load(P[i + dz * XY + dy * X + dx * ks]);
+            ++kk;
             if (nn == 1) { f1 = n1 ? v : R::add(f1, v); n1 = false; }
             else if (nn == 2) { f2 = n2 ? v : R::add(f2, v); n2 = false; }
             else { f3 = n3 ? v : R::add(f3, v); n3 = false; }
           }
-      const A sw = R::add(R::add(R::mul(f1, (A)0.25), R::mul(f2, (A)0.125)), R::mul(f3, (A)0.0625));
+      const A sw = R::mul(l2, R::add(R::add(R::mul(f1, (A)0.25), R::mul(f2, (A)0.125)),
+                                     R::mul(f3, (A)0.0625)));
       num = R::sub(R::sub(R::add(sw, R::mul(b, p)), R::mul(cc, pp)), R::mul(g2, s1));
     }
     const A out = R::mul(a, num);
@@ -182,10 +183,13 @@ void eval_dif_classes(const pfdtd_domain* d, int scheme, const std::vector<uint1
   dtab.assign(n * kDifClassVals, (A)0);
   for (size_t i = 0; i < n; ++i) {
     const unsigned pos = keys[i] >> 8, m = keys[i] & 0xFFu;
-    if (!(pos >> 7) || m >= d->dif_flags.size() || !d->dif_flags[m]) continue;
+    const bool inside = scheme == PFDTD_IWB ? pos != 0 : (pos >> 7) != 0;
+    if (!inside || m >= d->dif_flags.size() || !d->dif_flags[m]) continue;
     A G;
     if (scheme == PFDTD_SRL_FORWARD)
       G = (A)0.5 * (((A)6 - (A)(pos & 0x7Fu)) * l);
+    else if (scheme == PFDTD_IWB)  // pos is the geometry code
+      G = pos >= 65 ? l * ((A)(int)(pos - 65) * (A)0.0625) : (A)0;
     else
       G = l * (A)((pos & 1u) + ((pos >> 1) & 1u) + ((pos >> 2) & 1u));
     if (!(G > (A)0)) continue;
@@ -215,17 +219,20 @@ int launch_dif_t(pfdtd_domain* d, const void* cur, void* past, cudaStream_t s) {
     case PFDTD_SRL:
       k_dif_update<S, 1><<<g, 256, 0, s>>>(d->d_dif_list, n, d->kshift, d->d_cls, d->cls_bytes,
                                            (const A*)d->d_dif_tab, (const S*)cur, (S*)past,
-                                           (A*)d->d_dif_state, XE, XYE, l2, cpos);
+                                           (A*)d->d_dif_state, XE, XYE, l2, cpos,
+                                           d->d_iwb_mask);
       break;
     case PFDTD_IWB:
       k_dif_update<S, 2><<<g, 256, 0, s>>>(d->d_dif_list, n, d->kshift, d->d_cls, d->cls_bytes,
                                            (const A*)d->d_dif_tab, (const S*)cur, (S*)past,
-                                           (A*)d->d_dif_state, XE, XYE, l2, cpos);
+                                           (A*)d->d_dif_state, XE, XYE, l2, cpos,
+                                           d->d_iwb_mask);
       break;
     default:
       k_dif_update<S, 0><<<g, 256, 0, s>>>(d->d_dif_list, n, d->kshift, d->d_cls, d->cls_bytes,
                                            (const A*)d->d_dif_tab, (const S*)cur, (S*)past,
-                                           (A*)d->d_dif_state, XE, XYE, l2, cpos);
+                                           (A*)d->d_dif_state, XE, XYE, l2, cpos,
+                                           d->d_iwb_mask);
   }
   count_launch();
   PFDTD_CK(cudaGetLastError());

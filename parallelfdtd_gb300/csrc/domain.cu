@@ -388,7 +388,7 @@ int pfdtd_destroy(pfdtd_domain* d) {
   void* ptrs[] = {d->field_base[0], d->field_base[1], d->field_base[2], d->field_base[3], d->d_pos, d->d_mat, d->d_cls,
                   d->d_ctab, d->d_src_idx, d->d_src_mode, d->d_src_samples, d->d_rec_idx,
                   d->d_step, d->d_rec_out, d->d_err, d->d_dif_list, d->d_dif_tab,
-                  d->d_dif_state};
+                  d->d_dif_state, d->d_iwb_mask, d->d_iwb_code};
   for (void* p : ptrs)
     d->release(p);
   if (d->stream) cudaStreamDestroy(d->stream);
@@ -908,8 +908,7 @@ int pfdtd_set_tile(pfdtd_domain* d, int tile) {
 int pfdtd_get_kernel(pfdtd_domain* d, int* variant) {
   if (int rc = check_domain(d)) return rc;
   if (!variant) return fail(PFDTD_ERR_ARG, "null output");
-  const bool tma = d->kernel_variant != PFDTD_KERNEL_ZMARCH && tma_supported(d);
-  *variant = tma ? PFDTD_KERNEL_TMA : PFDTD_KERNEL_ZMARCH;
+  *variant = uses_tma(d) ? PFDTD_KERNEL_TMA : PFDTD_KERNEL_ZMARCH;
   if (d->tb_depth >= 2 && tb_active(d)) *variant = PFDTD_KERNEL_TB;
   return PFDTD_OK;
 }

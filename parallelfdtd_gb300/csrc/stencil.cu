@@ -98,16 +98,17 @@ k_update_zmarch(const C* __restrict__ cls, const S* __restrict__ P, S* __restric
 // IWB 27-point update (no counterpart in the reference).  One thread per
 // (x, y) column marching z; the 3 x 3 neighbourhood of planes z-1, z and z+1
 // stays in registers and each step reads the 3 x 3 block of plane z+1 through
-// the read-only cache.  Boundary nodes (DIR bits) replace the outward
-// column/row/plane of their neighbourhood by the inward one, one axis after
-// the other (x, y, z), which reflects every outward offset.  Sums follow the
-// canonical order of the oracle: offsets for dz, dy, dx in -1, 0, 1 into the
-// face, edge and corner sums.
+// the read-only cache.  Boundary closure (finite volume on the voxel grid): a
+// neighbour whose bit is set in the node's closed mask (k_iwb_geometry)
+// contributes the node's own value.  Sums follow the canonical order of the
+// oracle: offsets for dz, dy, dx in -1, 0, 1 into the face, edge and corner
+// sums.
 template <typename S, typename C>
 __global__ void __launch_bounds__(kBX * kBY)
-k_update_iwb(const C* __restrict__ cls, const S* __restrict__ P, S* __restrict__ Pp,
-             ClassTab<typename Store<S>::A> tab, int X, int Y, int64_t XY, int z_last, int zc,
-             int ks, int kshift) {
+k_update_iwb(const C* __restrict__ cls, const uint32_t* __restrict__ mask,
+             const S* __restrict__ P, S* __restrict__ Pp, ClassTab<typename Store<S>::A> tab,
+             int X, int Y, int64_t XY, int z_last, int zc, int ks, int kshift,
+             typename Store<S>::A l2) {
   using A = typename Store<S>::A;
   using R = Rn<A>;
   using St = Store<S>;
@@ -131,9 +132,9 @@ k_update_iwb(const C* __restrict__ cls, const S* __restrict__ P, S* __restrict__
   for (int z = z0; z < z1; ++z, idx += XY) {
     load_plane(2, idx + XY);
     const unsigned c = cls[idx >> kshift];
+    const uint32_t mk = __ldg(mask + (idx >> kshift));
     const A pp = St::load(Pp[idx]);
     const A ca = __ldg(tab.a + c), cb = __ldg(tab.b + c), cc = __ldg(tab.c + c);
-    const uint32_t cp = __ldg(tab.pos + c);
     A m[3][3][3];
 #pragma unroll
     for (int a = 0; a < 3; ++a)
@@ -141,34 +142,18 @@ k_update_iwb(const C* __restrict__ cls, const S* __restrict__ P, S* __restrict__
       for (int b = 0; b < 3; ++b)
 #pragma unroll
         for (int e = 0; e < 3; ++e) m[a][b][e] = v[a][b][e];
-    if (cp & 0x07u) {
-      if (cp & 0x01u) {  // x: outward is -1 with SIGN_X, +1 without
-        const bool neg = cp & 0x10u;
+    if (mk) {
+      int k = 0;
 #pragma unroll
-        for (int a = 0; a < 3; ++a)
-#pragma unroll
-          for (int b = 0; b < 3; ++b) {
-            if (neg) m[a][b][0] = m[a][b][2]; else m[a][b][2] = m[a][b][0];
-          }
-      }
-      if (cp & 0x02u) {
-        const bool neg = cp & 0x20u;
-#pragma unroll
-        for (int a = 0; a < 3; ++a)
-#pragma unroll
-          for (int e = 0; e < 3; ++e) {
-            if (neg) m[a][0][e] = m[a][2][e]; else m[a][2][e] = m[a][0][e];
-          }
-      }
-      if (cp & 0x04u) {
-        const bool neg = cp & 0x40u;
+      for (int a = 0; a < 3; ++a)
 #pragma unroll
         for (int b = 0; b < 3; ++b)
 #pragma unroll
           for (int e = 0; e < 3; ++e) {
-            if (neg) m[0][b][e] = m[2][b][e]; else m[2][b][e] = m[0][b][e];
+            if (a == 1 && b == 1 && e == 1) continue;
+            if ((mk >> k) & 1u) m[a][b][e] = v[1][1][1];
+            ++k;
           }
-      }
     }
     A s1 = (A)0, s2 = (A)0, s3 = (A)0;
     bool f1 = true, f2 = true, f3 = true;
@@ -185,7 +170,8 @@ k_update_iwb(const C* __restrict__ cls, const S* __restrict__ P, S* __restrict__
           else if (n == 2) { s2 = f2 ? w : R::add(s2, w); f2 = false; }
           else { s3 = f3 ? w : R::add(s3, w); f3 = false; }
         }
-    const A sw = R::add(R::add(R::mul(s1, (A)0.25), R::mul(s2, (A)0.125)), R::mul(s3, (A)0.0625));
+    const A sw = R::mul(l2, R::add(R::add(R::mul(s1, (A)0.25), R::mul(s2, (A)0.125)),
+                                   R::mul(s3, (A)0.0625)));
     const A out = R::mul(ca, R::sub(R::add(sw, R::mul(cb, v[1][1][1])), R::mul(cc, pp)));
     Pp[idx] = St::store(out);
 #pragma unroll
@@ -195,6 +181,42 @@ k_update_iwb(const C* __restrict__ cls, const S* __restrict__ P, S* __restrict__
         v[0][b][e] = v[1][b][e];
         v[1][b][e] = v[2][b][e];
       }
+  }
+}
+
+// IWB geometry per node: bit k of the mask is set when the k-th of the 26
+// neighbours (flat offsets dz*XY + dy*X + dx for dz, dy, dx in -1, 0, 1,
+// skipping the centre) is closed: outside the grid or without the inside
+// bit.  The code is 0 for a node without the inside bit, else
+// 1 + W16 + 64 * face, W16 = 4 (closed faces) + 2 (closed edges) + (closed
+// corners), face = 1 when a face neighbour is closed; it replaces the
+// position byte in the IWB class key.
+__global__ void k_iwb_geometry(const uint8_t* __restrict__ pos, int64_t N, int64_t X,
+                               int64_t XY, uint32_t* __restrict__ mask,
+                               uint8_t* __restrict__ code) {
+  for (int64_t c = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; c < N;
+       c += (int64_t)gridDim.x * blockDim.x) {
+    uint32_t m = 0;
+    int w16 = 0, face = 0, k = 0;
+#pragma unroll
+    for (int dz = -1; dz <= 1; ++dz)
+#pragma unroll
+      for (int dy = -1; dy <= 1; ++dy)
+#pragma unroll
+        for (int dx = -1; dx <= 1; ++dx) {
+          const int n = (dx != 0) + (dy != 0) + (dz != 0);
+          if (n == 0) continue;
+          const int64_t i = c + dz * XY + dy * X + dx;
+          const bool open = i >= 0 && i < N && (pos[i] >> 7);
+          if (!open) {
+            m |= 1u << k;
+            w16 += n == 1 ? 4 : (n == 2 ? 2 : 1);
+            face |= n == 1;
+          }
+          ++k;
+        }
+    mask[c] = m;
+    code[c] = (pos[c] >> 7) ? (uint8_t)(1 + w16 + 64 * face) : 0;
   }
 }
 
@@ -296,8 +318,8 @@ int launch_iwb_t(pfdtd_domain* d, const void* cur, void* past, cudaStream_t s) {
                   (const A*)(tb + 2 * as * d->n_classes),
                   (const uint32_t*)(tb + 3 * as * d->n_classes), d->n_classes};
   k_update_iwb<S, C><<<dim3(gx, gy, gz), dim3(kBX, kBY), 0, s>>>(
-      (const C*)d->d_cls, (const S*)cur, (S*)past, tab, (int)XE, (int)d->Y, d->XY * d->K,
-      (int)(d->Z - 1), (int)zc, d->K, d->kshift);
+      (const C*)d->d_cls, d->d_iwb_mask, (const S*)cur, (S*)past, tab, (int)XE, (int)d->Y,
+      d->XY * d->K, (int)(d->Z - 1), (int)zc, d->K, d->kshift, (A)d->params[1]);
   count_launch();
   PFDTD_CK(cudaGetLastError());
   return PFDTD_OK;
@@ -338,9 +360,9 @@ int eval_class_coefs(int precision, int scheme, int quirks, const double* params
                      const std::vector<uint16_t>& keys, std::vector<uint8_t>& out_tab);
 
 int launch_update(pfdtd_domain* d, const void* cur, void* past, cudaStream_t s) {
-  if (d->kernel_variant != PFDTD_KERNEL_ZMARCH && d->class_scheme != PFDTD_IWB &&
-      tma_supported(d))
-    return launch_update_tma(d, cur, past, s);
+  if (uses_tma(d))
+    return d->class_scheme == PFDTD_IWB ? launch_iwb_tma(d, cur, past, s)
+                                        : launch_update_tma(d, cur, past, s);
   switch (d->precision) {
     case PFDTD_F32: return launch_update_s<float>(d, cur, past, s);
     case PFDTD_F64: return launch_update_s<double>(d, cur, past, s);
@@ -374,10 +396,25 @@ int build_classes(pfdtd_domain* d) {
   uint8_t* d_present = nullptr;
   PFDTD_CK(cudaMallocAsync((void**)&d_present, 65536, s));
   PFDTD_CK(cudaMemsetAsync(d_present, 0, 65536, s));
+  // IWB classes are keyed by the geometry code instead of the position byte.
+  const uint8_t* key_bytes = d->d_pos;
+  if (scheme == PFDTD_IWB) {
+    if (!d->d_iwb_mask) {
+      if (d->alloc((void**)&d->d_iwb_mask, (size_t)d->N * sizeof(uint32_t)) != cudaSuccess ||
+          d->alloc((void**)&d->d_iwb_code, (size_t)d->N) != cudaSuccess)
+        return fail(PFDTD_ERR_NOMEM, "IWB geometry allocation failed");
+    }
+    const int64_t gb = std::min<int64_t>((d->N + 255) / 256, 152 * 32);
+    k_iwb_geometry<<<(int)gb, 256, 0, s>>>(d->d_pos, d->N, d->X, d->XY, d->d_iwb_mask,
+                                           d->d_iwb_code);
+    count_launch();
+    PFDTD_CK(cudaGetLastError());
+    key_bytes = d->d_iwb_code;
+  }
   const int64_t begin = d->XY, end = d->N - d->XY;
   if (end > begin) {
     const int64_t blocks = std::min<int64_t>((end - begin + 255) / 256, 152 * 32);
-    k_key_presence<<<(int)blocks, 256, 0, s>>>(d->d_pos, d->d_mat, begin, end, d_present);
+    k_key_presence<<<(int)blocks, 256, 0, s>>>(key_bytes, d->d_mat, begin, end, d_present);
     count_launch();
     PFDTD_CK(cudaGetLastError());
   }
@@ -415,10 +452,10 @@ int build_classes(pfdtd_domain* d) {
   PFDTD_CK(cudaMemcpyAsync(d_lut, lut.data(), 65536 * sizeof(uint16_t), cudaMemcpyHostToDevice, s));
   const int64_t blocks = std::min<int64_t>((d->N + 255) / 256, 152 * 32);
   if (cls_bytes == 1)
-    k_map_classes<uint8_t><<<(int)blocks, 256, 0, s>>>(d->d_pos, d->d_mat, d->N, d_lut,
+    k_map_classes<uint8_t><<<(int)blocks, 256, 0, s>>>(key_bytes, d->d_mat, d->N, d_lut,
                                                         (uint8_t*)d->d_cls);
   else
-    k_map_classes<uint16_t><<<(int)blocks, 256, 0, s>>>(d->d_pos, d->d_mat, d->N, d_lut,
+    k_map_classes<uint16_t><<<(int)blocks, 256, 0, s>>>(key_bytes, d->d_mat, d->N, d_lut,
                                                          (uint16_t*)d->d_cls);
   count_launch();
   PFDTD_CK(cudaGetLastError());

@@ -183,16 +183,161 @@ __device__ __forceinline__ void stg4(double* p, const double (&v)[4]) {
   reinterpret_cast<double2*>(p)[1] = make_double2(v[2], v[3]);
 }
 
+// IWB 27-point update of a consumer thread's 4 consecutive x nodes (no
+// counterpart in the reference).  The 3 planes x 3 rows x 6 values around
+// the nodes come from the stage ring: the box's 16-byte x halo and one-row y
+// halo hold every edge and corner neighbour.  At the grid's x edges the
+// neighbour x-1 (x = 0) or x+4 (x+4 = X) is read from global memory at its
+// flat index, so the wrap across rows matches k_update_iwb (stencil.cu),
+// whose boundary closure (closed neighbours contribute the node's value),
+// canonical summation order (dz, dy, dx) and rounding this follows
+// operation for operation.
+template <typename S, typename C, typename Lay>
+__device__ __forceinline__ void iwb_consumer(const S* Pm, const S* Pc, const S* Pn, const S* Pq,
+                                             const C* Cl, const S* __restrict__ P,
+                                             S* __restrict__ Pp, int64_t idx, int si, int ci,
+                                             int x, int X, int64_t XY,
+                                             const PackedCoef<float>* stab,
+                                             const ClassTab<float>& tab, uint4 mk4, float l2) {
+  using R = Rn<float>;
+  using St = Store<S>;
+  constexpr int PW = Lay::PW;
+  constexpr bool kSmemTab = sizeof(C) == 1;
+  const S* pl[3] = {Pm, Pc, Pn};
+  // v[plane][row][i]: plane dz+1, row dy+1, i = 0 for x-1, 1..4 for x..x+3, 5 for x+4
+  float v[3][3][6];
+#pragma unroll
+  for (int a = 0; a < 3; ++a)
+#pragma unroll
+    for (int b = 0; b < 3; ++b) {
+      const S* row = pl[a] + si + (b - 1) * PW;
+      const V4<S> mid = lds4(row);
+#pragma unroll
+      for (int e = 0; e < 4; ++e) v[a][b][e + 1] = St::load(mid.v[e]);
+      const int64_t g = idx + (int64_t)(a - 1) * XY + (int64_t)(b - 1) * X;
+      v[a][b][0] = x == 0 ? St::load(P[g - 1]) : St::load(row[-1]);
+      v[a][b][5] = x + kVec == X ? St::load(P[g + kVec]) : St::load(row[kVec]);
+    }
+  const V4<S> vpp = lds4(Pq + ci);
+  const uint32_t mks[kVec] = {mk4.x, mk4.y, mk4.z, mk4.w};
+  unsigned cid[kVec];
+  if (sizeof(C) == 1) {
+    const uint32_t w = *reinterpret_cast<const uint32_t*>(Cl + ci);
+#pragma unroll
+    for (int e = 0; e < kVec; ++e) cid[e] = (w >> (8 * e)) & 0xFFu;
+  } else {
+    const uint2 w = *reinterpret_cast<const uint2*>(Cl + ci);
+    cid[0] = w.x & 0xFFFFu; cid[1] = w.x >> 16; cid[2] = w.y & 0xFFFFu; cid[3] = w.y >> 16;
+  }
+  S res[kVec];
+#pragma unroll
+  for (int e = 0; e < kVec; ++e) {
+    PackedCoef<float> k;
+    if (kSmemTab) k = stab[cid[e]];
+    else
+      k = PackedCoef<float>{__ldg(tab.a + cid[e]), __ldg(tab.b + cid[e]), __ldg(tab.c + cid[e]),
+                            __ldg(tab.pos + cid[e])};
+    float m[3][3][3];
+#pragma unroll
+    for (int a = 0; a < 3; ++a)
+#pragma unroll
+      for (int b = 0; b < 3; ++b)
+#pragma unroll
+        for (int c = 0; c < 3; ++c) m[a][b][c] = v[a][b][e + c];
+    const uint32_t mk = mks[e];
+    if (mk) {
+      int kk = 0;
+#pragma unroll
+      for (int a = 0; a < 3; ++a)
+#pragma unroll
+        for (int b = 0; b < 3; ++b)
+#pragma unroll
+          for (int c = 0; c < 3; ++c) {
+            if (a == 1 && b == 1 && c == 1) continue;
+            if ((mk >> kk) & 1u) m[a][b][c] = v[1][1][e + 1];
+            ++kk;
+          }
+    }
+    float s1 = 0.f, s2 = 0.f, s3 = 0.f;
+    bool f1 = true, f2 = true, f3 = true;
+#pragma unroll
+    for (int a = 0; a < 3; ++a)
+#pragma unroll
+      for (int b = 0; b < 3; ++b)
+#pragma unroll
+        for (int c = 0; c < 3; ++c) {
+          const int n = (a != 1) + (b != 1) + (c != 1);
+          if (n == 0) continue;
+          const float w = m[a][b][c];
+          if (n == 1) { s1 = f1 ? w : R::add(s1, w); f1 = false; }
+          else if (n == 2) { s2 = f2 ? w : R::add(s2, w); f2 = false; }
+          else { s3 = f3 ? w : R::add(s3, w); f3 = false; }
+        }
+    const float sw = R::mul(
+        l2, R::add(R::add(R::mul(s1, 0.25f), R::mul(s2, 0.125f)), R::mul(s3, 0.0625f)));
+    const float out = R::mul(k.a, R::sub(R::add(sw, R::mul(k.b, v[1][1][e + 1])),
+                                         R::mul(k.c, St::load(vpp.v[e]))));
+    res[e] = St::store(out);
+  }
+  stg4(Pp + idx, res);
+}
+
+// Producer of the stage ring (one thread): stage k receives the P^n plane
+// z0-1+k of the tile with its halo and, from k = 2 on, the P^{n-1} plane and
+// the class ids of plane z0+k-2.  Every wait is bounded; on expiry it raises
+// the error flag and the abort flag, then waits (bounded) for the loads it
+// already issued before returning.
+template <typename Lay>
+__device__ __forceinline__ void tma_producer(const CUtensorMap* map_cur,
+                                             const CUtensorMap* map_past,
+                                             const CUtensorMap* map_cls, unsigned char* smem,
+                                             uint32_t bar_full, uint32_t bar_empty,
+                                             volatile int* abort_flag, int x0, int y0, int z0,
+                                             int Y, int K, int kshift, int* err) {
+  constexpr int NS = Lay::NS, H = Lay::H;
+  int issued = 0;
+  for (int k = 0; k < K; ++k) {
+    const int slot = k % NS;
+    if (k >= NS) {
+      if (!mbar_wait(bar_empty + 8 * slot, (uint32_t)((k / NS - 1) & 1))) {
+        atomicExch(err, 1);
+        *abort_flag = 1;
+        break;
+      }
+    }
+    if (*abort_flag) break;
+    unsigned char* st = smem + slot * Lay::STAGE;
+    const uint32_t bar = bar_full + 8 * slot;
+    const int zp = z0 - 1 + k;
+    uint32_t bytes = Lay::P_BYTES;
+    if (k >= 2) bytes += Lay::PP_BYTES + (Lay::CL_BYTES >> kshift);
+    mbar_expect_tx(bar, bytes);
+    tma_load_2d(smem_u32(st + Lay::P_OFF), map_cur, x0 - H, zp * Y + y0 - 1, bar);
+    if (k >= 2) {
+      const int zc_ = z0 + k - 2;
+      tma_load_2d(smem_u32(st + Lay::PP_OFF), map_past, x0, zc_ * Y + y0, bar);
+      tma_load_2d(smem_u32(st + Lay::CL_OFF), map_cls, x0 >> kshift, zc_ * Y + y0, bar);
+    }
+    issued = k + 1;
+  }
+  // Wait (bounded) for every load still in flight before the CTA may exit.
+  for (int k = max(0, issued - NS); k < issued; ++k)
+    mbar_wait(bar_full + 8 * (k % NS), (uint32_t)((k / NS) & 1));
+}
+
 // BATCHED: the field holds K = 1 << kshift interleaved fields per node (K a
 // multiple of 4): X and XY count elements, a consumer thread's 4 elements are
 // 4 fields of one node, the x neighbours are K elements away and the class
 // ids (one per node) come in a box K times narrower.
+// (IWB: two CTAs per SM, i.e. at most 112 registers per thread with the
+// 288-thread CTAs, keeping 16 consumer warps resident.)
 template <typename S, typename C, int SCHEME, typename Lay, bool BATCHED = false>
-__global__ void __launch_bounds__(Lay::THREADS)
+__global__ void __launch_bounds__(Lay::THREADS, SCHEME == 3 ? 2 : 1)
 k_update_tma(const __grid_constant__ CUtensorMap map_cur, const __grid_constant__ CUtensorMap map_past,
              const __grid_constant__ CUtensorMap map_cls, const S* __restrict__ P,
              S* __restrict__ Pp, ClassTab<typename Store<S>::A> tab, int X, int Y, int64_t XY,
-             int z_last, int zc, typename Store<S>::A l2, int* __restrict__ err, int kshift = 0) {
+             int z_last, int zc, typename Store<S>::A l2, int* __restrict__ err, int kshift = 0,
+             const uint32_t* __restrict__ iwb_mask = nullptr) {
   using A = typename Store<S>::A;
   using R = Rn<A>;
   using St = Store<S>;
@@ -235,37 +380,9 @@ k_update_tma(const __grid_constant__ CUtensorMap map_cur, const __grid_constant_
   const int K = nplanes + 2;  // loads: planes z0-1 .. z1 of P^n
 
   if (warp == kConsumerWarps) {
-    // ---------------- producer ----------------
-    if (lane == 0) {
-      int issued = 0;
-      for (int k = 0; k < K; ++k) {
-        const int slot = k % NS;
-        if (k >= NS) {
-          if (!mbar_wait(bar_empty + 8 * slot, (uint32_t)((k / NS - 1) & 1))) {
-            atomicExch(err, 1);
-            *abort_flag = 1;
-            break;
-          }
-        }
-        if (*abort_flag) break;
-        unsigned char* st = smem + slot * Lay::STAGE;
-        const uint32_t bar = bar_full + 8 * slot;
-        const int zp = z0 - 1 + k;
-        uint32_t bytes = Lay::P_BYTES;
-        if (k >= 2) bytes += Lay::PP_BYTES + (Lay::CL_BYTES >> kshift);
-        mbar_expect_tx(bar, bytes);
-        tma_load_2d(smem_u32(st + Lay::P_OFF), &map_cur, x0 - H, zp * Y + y0 - 1, bar);
-        if (k >= 2) {
-          const int zc_ = z0 + k - 2;
-          tma_load_2d(smem_u32(st + Lay::PP_OFF), &map_past, x0, zc_ * Y + y0, bar);
-          tma_load_2d(smem_u32(st + Lay::CL_OFF), &map_cls, x0 >> kshift, zc_ * Y + y0, bar);
-        }
-        issued = k + 1;
-      }
-      // Wait (bounded) for every load still in flight before the CTA may exit.
-      for (int k = max(0, issued - NS); k < issued; ++k)
-        mbar_wait(bar_full + 8 * (k % NS), (uint32_t)((k / NS) & 1));
-    }
+    if (lane == 0)
+      tma_producer<Lay>(&map_cur, &map_past, &map_cls, smem, bar_full, bar_empty, abort_flag, x0,
+                        y0, z0, Y, K, kshift, err);
     return;
   }
 
@@ -280,13 +397,32 @@ k_update_tma(const __grid_constant__ CUtensorMap map_cur, const __grid_constant_
   const bool active = (x < X) && (y < Y);  // X is a multiple of 4: all 4 or none
   const int si = (ly + 1) * PW + lx + H;   // centre of the thread's first node
   bool ok = mbar_wait(bar_full, 0) && mbar_wait(bar_full + 8, 0);
+  // IWB: the closed-neighbour masks of the thread's 4 nodes, loaded one plane
+  // ahead of their use so the global read overlaps a plane of work
+  const int64_t node0 = (int64_t)z0 * XY + (int64_t)y * X + x;
+  uint4 mk_next = make_uint4(0, 0, 0, 0);
+  if (SCHEME == 3 && active) mk_next = __ldg(reinterpret_cast<const uint4*>(iwb_mask + node0));
   for (int j = 0; j < nplanes && ok; ++j) {
     const int sm = j % NS, sc_ = (j + 1) % NS, sp_ = (j + 2) % NS;
     if (!mbar_wait(bar_full + 8 * sp_, (uint32_t)(((j + 2) / NS) & 1))) {
       ok = false;
       break;
     }
-    if (active) {
+    if constexpr (SCHEME == 3) {
+      const uint4 mk_cur = mk_next;
+      if (active && j + 1 < nplanes)
+        mk_next = __ldg(reinterpret_cast<const uint4*>(iwb_mask + node0 + (int64_t)(j + 1) * XY));
+      if (active) {
+        const S* Pm = (const S*)(smem + sm * Lay::STAGE + Lay::P_OFF);
+        const S* Pc = (const S*)(smem + sc_ * Lay::STAGE + Lay::P_OFF);
+        const S* Pn = (const S*)(smem + sp_ * Lay::STAGE + Lay::P_OFF);
+        const S* Pq = (const S*)(smem + sp_ * Lay::STAGE + Lay::PP_OFF);
+        const C* Cl = (const C*)(smem + sp_ * Lay::STAGE + Lay::CL_OFF);
+        const int64_t idx = (int64_t)(z0 + j) * XY + (int64_t)y * X + x;
+        iwb_consumer<S, C, Lay>(Pm, Pc, Pn, Pq, Cl, P, Pp, idx, si, ly * kTX + lx, x, X, XY,
+                                stab, tab, mk_cur, (float)l2);
+      }
+    } else if (active) {
       const S* Pm = (const S*)(smem + sm * Lay::STAGE + Lay::P_OFF);
       const S* Pc = (const S*)(smem + sc_ * Lay::STAGE + Lay::P_OFF);
       const S* Pn = (const S*)(smem + sp_ * Lay::STAGE + Lay::P_OFF);
@@ -424,16 +560,23 @@ int launch_tma_t(pfdtd_domain* d, const void* cur, void* past, cudaStream_t s) {
   const int64_t nz = d->Z - 2;
   if (nz <= 0) return PFDTD_OK;
   TmaState& ts = d->tma;
-  const int cur_i = (cur == d->field(0)) ? 0 : 1;
-  const int64_t key[4] = {(int64_t)(intptr_t)d->d_cls, d->cls_bytes, d->precision * 100 + d->K,
-                          (int64_t)Lay::TX * 10000 + Lay::TY * 10 + (Lay::XHALO ? 1 : 0)};
+  int cur_i = -1, past_i = -1;
+  for (int f = 0; f < 4; ++f) {
+    if (d->field_base[f] && cur == d->field(f)) cur_i = f;
+    if (d->field_base[f] && past == d->field(f)) past_i = f;
+  }
+  if (cur_i < 0 || past_i < 0) return fail(PFDTD_ERR_ARG, "update fields are not domain buffers");
+  const int64_t key[5] = {(int64_t)(intptr_t)d->d_cls, d->cls_bytes, d->precision * 100 + d->K,
+                          (int64_t)Lay::TX * 10000 + Lay::TY * 10 + (Lay::XHALO ? 1 : 0),
+                          (int64_t)(intptr_t)d->field_base[2]};
   if (!ts.ready || std::memcmp(key, ts.key, sizeof(key)) != 0) {
     const CUtensorMapDataType dt = TmaType<S>::value;
     const CUtensorMapDataType ct =
         sizeof(C) == 1 ? CU_TENSOR_MAP_DATA_TYPE_UINT8 : CU_TENSOR_MAP_DATA_TYPE_UINT16;
     const int64_t rows = d->Y * d->Z;
     bool ok = true;
-    for (int f = 0; f < 2; ++f) {
+    for (int f = 0; f < 4; ++f) {
+      if (!d->field_base[f]) continue;
       ok = ok && make_map(&ts.halo[f], dt, sizeof(S), d->field(f), XE, rows, Lay::PW, Lay::TY + 2);
       ok = ok && make_map(&ts.tile[f], dt, sizeof(S), d->field(f), XE, rows, kTX, Lay::TY);
     }
@@ -442,11 +585,13 @@ int launch_tma_t(pfdtd_domain* d, const void* cur, void* past, cudaStream_t s) {
     std::memcpy(ts.key, key, sizeof(key));
     ts.ready = true;
   }
-  static bool attr_done = false;  // one instantiation, one attribute (per process)
-  if (!attr_done) {
+  // the shared-memory opt-in, once per instantiation and device
+  static bool attr_done[64] = {};
+  if (d->device >= 64) return fail(PFDTD_ERR_UNSUPPORTED, "device index above 63");
+  if (!attr_done[d->device]) {
     PFDTD_CK(cudaFuncSetAttribute(k_update_tma<S, C, SCHEME, Lay, BATCHED>,
                                   cudaFuncAttributeMaxDynamicSharedMemorySize, Lay::SMEM));
-    attr_done = true;
+    attr_done[d->device] = true;
   }
   const int gx = (int)((XE + kTX - 1) / kTX);
   const int gy = (int)((d->Y + Lay::TY - 1) / Lay::TY);
@@ -473,8 +618,9 @@ int launch_tma_t(pfdtd_domain* d, const void* cur, void* past, cudaStream_t s) {
                   (const A*)(tb + 2 * as * d->n_classes),
                   (const uint32_t*)(tb + 3 * as * d->n_classes), d->n_classes};
   k_update_tma<S, C, SCHEME, Lay, BATCHED><<<dim3(gx, gy, gz), Lay::THREADS, Lay::SMEM, s>>>(
-      ts.halo[cur_i], ts.tile[1 - cur_i], ts.cls, (const S*)cur, (S*)past, tab, (int)XE,
-      (int)d->Y, d->XY * d->K, (int)(d->Z - 1), (int)zc, (A)d->params[1], d->d_err, d->kshift);
+      ts.halo[cur_i], ts.tile[past_i], ts.cls, (const S*)cur, (S*)past, tab, (int)XE,
+      (int)d->Y, d->XY * d->K, (int)(d->Z - 1), (int)zc, (A)d->params[1], d->d_err, d->kshift,
+      d->d_iwb_mask);
   count_launch();
   PFDTD_CK(cudaGetLastError());
   return PFDTD_OK;
@@ -581,7 +727,38 @@ int launch_tma_s<double>(pfdtd_domain* d, const void* cur, void* past, cudaStrea
       d, cur, past, s);
 }
 
+// IWB on the stage ring: FP32, FP16 and BF16 storage, one field per node,
+// tiles with the x halo in the box (128 x 8 when X is a multiple of 128,
+// else 64 x 16).
+template <typename S>
+int launch_iwb_tma_s(pfdtd_domain* d, const void* cur, void* past, cudaStream_t s) {
+  if (sizeof(S) == 4 && d->X % 128 == 0) {
+    if (d->cls_bytes == 1)
+      return launch_tma_t<S, uint8_t, 3, Layout<S, uint8_t, 128, 8, 8, true>>(d, cur, past, s);
+    return launch_tma_t<S, uint16_t, 3, Layout<S, uint16_t, 128, 8, 8, true>>(d, cur, past, s);
+  }
+  if (d->cls_bytes == 1)
+    return launch_tma_t<S, uint8_t, 3, Layout<S, uint8_t, 64, 16, 8, true>>(d, cur, past, s);
+  return launch_tma_t<S, uint16_t, 3, Layout<S, uint16_t, 64, 16, 8, true>>(d, cur, past, s);
+}
+
 }  // namespace
+
+int launch_iwb_tma(pfdtd_domain* d, const void* cur, void* past, cudaStream_t s) {
+  switch (d->precision) {
+    case PFDTD_F32: return launch_iwb_tma_s<float>(d, cur, past, s);
+    case PFDTD_F16: return launch_iwb_tma_s<__half>(d, cur, past, s);
+    case PFDTD_BF16: return launch_iwb_tma_s<__nv_bfloat16>(d, cur, past, s);
+  }
+  return fail(PFDTD_ERR_UNSUPPORTED, "IWB on the TMA path needs FP32, FP16 or BF16 fields");
+}
+
+// Whether the next update runs a TMA kernel (7-point or IWB).
+bool uses_tma(const pfdtd_domain* d) {
+  if (d->kernel_variant == PFDTD_KERNEL_ZMARCH || !tma_supported(d)) return false;
+  if (d->class_scheme == PFDTD_IWB) return d->K == 1 && d->precision != PFDTD_F64;
+  return true;
+}
 
 // The TMA path needs 16-byte aligned rows for the fields and class ids.
 int tma_tile_count() { return 9; }

@@ -32,11 +32,12 @@ def arith_dtype(precision: int):
     return np.float64 if precision == L.F64 else np.float32
 
 
-def default_params(octave: int = 0, scheme="forward") -> np.ndarray:
+def default_params(octave: int = 0, scheme="forward", lam: Optional[float] = None) -> np.ndarray:
     """[lambda, lambda^2, 1/3, octave] at lambda = 1/sqrt(3), as the reference's
     SimulationParameters::getParameterPtrDouble (SimulationParameters.cpp:389-396);
-    lambda = 1 for the IWB scheme."""
-    lam = 1.0 if scheme_code(scheme) == L.IWB else 1.0 / math.sqrt(3.0)
+    lambda = 1 (its stability limit) for the IWB scheme unless `lam` is given."""
+    if lam is None:
+        lam = 1.0 if scheme_code(scheme) == L.IWB else 1.0 / math.sqrt(3.0)
     return np.array([lam, lam * lam, 1.0 / 3.0, float(octave)], dtype=np.float64)
 
 

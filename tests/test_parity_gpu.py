@@ -461,7 +461,71 @@ def test_16bit_storage_bit_identical(gpu, O, variant, prec, centred):
     assert err < (1e-2 if prec == "f16" else 1e-1), err
 
 
-@pytest.mark.parametrize("prec", ["f32", "f64", "f16"])
+@pytest.mark.parametrize("prec", ["f32", "bf16"])
+@pytest.mark.parametrize("variant", ["auto", "zmarch"])
+def test_iwb_open_x_faces(gpu, O, prec, variant):
+    """IWB with inside nodes on the x and y faces, where the flat-index
+    neighbours x-1 / x+1 wrap to the neighbouring row (the TMA kernel reads
+    them from global memory at the grid's x edges): equal to the oracle."""
+    room = rooms.boxes_room((64, 48, 40), n_boxes=4, edge=(5, 12), n_materials=6, seed=14)
+    bid = room.bid.copy().reshape(room.dims[2], room.dims[1], room.dims[0])
+    bid[5:30, 6:40, 0] = 26   # open strips on both x faces and one y face
+    bid[8:25, 3:30, -1] = 22
+    bid[10:20, 0, 10:50] = 21
+    steps = 120
+    srcs = [(1, 20, 15), (62, 10, 12)]
+    rec = [(0, 20, 15), (63, 12, 14), (30, 0, 15), (20, 20, 20)]
+    pulse = rooms.gaussian_pulse(steps, 3.0)
+    params = default_params(scheme="iwb")
+    with Domain(room.dims, prec) as d:
+        d.set_voxels(bid.reshape(-1), room.mat, centred=True)
+        d.set_materials(room.admittance)
+        d.set_params(params)
+        d.set_scheme("iwb")
+        d.set_kernel(variant)
+        d.set_sources(srcs, [1, 1], np.stack([pulse, -0.5 * pulse]))
+        d.set_receivers(rec)
+        g, _, _ = d.run(steps)
+        assert d.kernel() == ("tma" if variant == "auto" else "zmarch")
+    pos, mat = O.encode_nodes(bid.reshape(-1), room.mat, True)
+    r, _, _ = O.run(pos, mat, room.dims, room.admittance, params, [room.flat(*x) for x in srcs],
+                    [1, 1], np.stack([pulse, -0.5 * pulse]), [room.flat(*x) for x in rec], steps,
+                    scheme=3, storage=(prec if prec == "bf16" else None))
+    assert np.abs(r).max() > 1e-3
+    assert np.array_equal(g, r)
+
+
+@pytest.mark.parametrize("prec", ["f32", "bf16"])
+def test_iwb_below_the_stability_limit(gpu, O, prec):
+    """IWB at lambda = 0.95 (weights lambda^2 (1/4, 1/8, 1/16), centre
+    2 - 7/2 lambda^2) with frequency-dependent walls: equal to the oracle."""
+    from parallelfdtd_gb300 import materials
+    room = rooms.boxes_room((64, 48, 40), n_boxes=5, edge=(5, 12), n_materials=6, seed=15)
+    steps = 150
+    srcs = room.random_air_nodes(2, seed=1)
+    rec = room.random_air_nodes(4, seed=2)
+    pulse = rooms.gaussian_pulse(steps, 3.0)
+    params = default_params(scheme="iwb", lam=0.95)
+    flags = np.array([m % 2 for m in range(6)], np.int32)
+    table = materials.dif_table(materials.positive_real_filters(6, 3, seed=2), 3)
+    with Domain(room.dims, prec) as d:
+        d.set_voxels(room.bid, room.mat, centred=True)
+        d.set_materials(room.admittance)
+        d.set_params(params)
+        d.set_scheme("iwb")
+        d.set_dif_filters(flags, table)
+        d.set_sources(srcs, [1, 1], np.stack([pulse, -0.5 * pulse]))
+        d.set_receivers(rec)
+        g, _, _ = d.run(steps)
+    pos, mat = O.encode_nodes(room.bid, room.mat, True)
+    r, _, _ = O.run(pos, mat, room.dims, room.admittance, params, [room.flat(*s) for s in srcs],
+                    [1, 1], np.stack([pulse, -0.5 * pulse]), [room.flat(*x) for x in rec], steps,
+                    scheme=3, storage=(prec if prec == "bf16" else None), dif=(flags, table))
+    assert np.abs(r).max() > 1e-4
+    assert np.array_equal(g, r)
+
+
+@pytest.mark.parametrize("prec", ["f32", "f64", "f16", "bf16"])
 def test_iwb_bit_identical(gpu, O, prec):
     """IWB 27-point scheme (specification in the oracle): the CUDA path equals
     the oracle bit for bit on a room with boxes (faces, edges, corners)."""
@@ -483,9 +547,10 @@ def test_iwb_bit_identical(gpu, O, prec):
     pos, mat = O.encode_nodes(room.bid, room.mat, True)
     r, rP, _ = O.run(pos, mat, room.dims, room.admittance, params, [room.flat(*s) for s in srcs],
                      [1, 1], np.stack([pulse, -0.5 * pulse]), [room.flat(*x) for x in rec], steps,
-                     scheme=3, double=(prec == "f64"), storage=(prec if prec == "f16" else None))
+                     scheme=3, double=(prec == "f64"),
+                     storage=(prec if prec in ("f16", "bf16") else None))
     assert np.abs(r).max() > 1e-4
-    if prec == "f16":
+    if prec in ("f16", "bf16"):
         assert np.array_equal(g, r) and np.array_equal(P.view(np.uint16), rP.view(np.uint16))
     else:
         assert_parity(g, r, prec)

@@ -217,3 +217,21 @@ def test_autotune_restores_fields_and_keeps_results(gpu):
         assert st == 0
         assert np.array_equal(g1, g0)
         assert np.array_equal(values(d.download_field(L.FIELD_CURRENT), "f32"), P0)
+
+
+@pytest.mark.parametrize("prec", ["f32", "f16"])
+def test_blocked_then_per_step_on_the_other_buffer_pair(gpu, prec):
+    """A run whose blocked launches end on the second buffer pair and then
+    takes per-step TMA updates there (X a multiple of 16 selects TMA)."""
+    room = rooms.boxes_room((128, 96, 60), n_boxes=6, edge=(6, 16), n_materials=6, seed=33)
+    pts = room.random_air_nodes(6, seed=9)
+    srcs = [(tuple(pts[0]), 1), (tuple(pts[1]), 0)]
+    recs = [tuple(p) for p in pts[2:]]
+    steps = 48 + 3  # one chunk, one blocked launch (odd), one per-step update
+    pulse = rooms.gaussian_pulse(steps, 3.0)
+    samples = np.stack([pulse, 0.5 * pulse])
+    g0, P0, Pp0, _ = run(room, prec, "forward", 0, srcs, recs, samples, steps)
+    g1, P1, Pp1, info = run(room, prec, "forward", 2, srcs, recs, samples, steps)
+    assert info[1], info[2]
+    assert np.array_equal(g1, g0)
+    assert np.array_equal(P1, P0) and np.array_equal(Pp1, Pp0)
