@@ -329,10 +329,8 @@ __device__ __forceinline__ void tma_producer(const CUtensorMap* map_cur,
 // multiple of 4): X and XY count elements, a consumer thread's 4 elements are
 // 4 fields of one node, the x neighbours are K elements away and the class
 // ids (one per node) come in a box K times narrower.
-// (IWB: two CTAs per SM, i.e. at most 112 registers per thread with the
-// 288-thread CTAs, keeping 16 consumer warps resident.)
 template <typename S, typename C, int SCHEME, typename Lay, bool BATCHED = false>
-__global__ void __launch_bounds__(Lay::THREADS, SCHEME == 3 ? 2 : 1)
+__global__ void __launch_bounds__(Lay::THREADS)
 k_update_tma(const __grid_constant__ CUtensorMap map_cur, const __grid_constant__ CUtensorMap map_past,
              const __grid_constant__ CUtensorMap map_cls, const S* __restrict__ P,
              S* __restrict__ Pp, ClassTab<typename Store<S>::A> tab, int X, int Y, int64_t XY,
@@ -728,18 +726,33 @@ int launch_tma_s<double>(pfdtd_domain* d, const void* cur, void* past, cudaStrea
 }
 
 // IWB on the stage ring: FP32, FP16 and BF16 storage, one field per node,
-// tiles with the x halo in the box (128 x 8 when X is a multiple of 128,
-// else 64 x 16).
+// tiles with the x halo in the box.  Shapes (d->tma_tile for IWB, -1 auto):
+// 0 = 64 x 16, 1 = 128 x 8, 2 = 128 x 4 (12 stages), 3 = 64 x 8 (12
+// stages, the default): with the 27-point gather's register use (about 120
+// per thread) 160-thread CTAs keep three CTAs on an SM (measured on the
+// 512 x 384 x 256 room, FP32: 0.297 ms per step against 0.387 ms for the
+// 288-thread 64 x 16 and 128 x 8 tiles).
+template <typename S, typename C, int TX, int TY, int NS>
+int launch_iwb_l(pfdtd_domain* d, const void* cur, void* past, cudaStream_t s) {
+  return launch_tma_t<S, C, 3, Layout<S, C, TX, TY, NS, true>>(d, cur, past, s);
+}
+
+template <typename S, typename C>
+int launch_iwb_c(pfdtd_domain* d, const void* cur, void* past, cudaStream_t s) {
+  int tile = d->tma_tile;
+  if (tile < 0 || tile > 3) tile = 3;
+  switch (tile) {
+    case 0: return launch_iwb_l<S, C, 64, 16, 8>(d, cur, past, s);
+    case 1: return launch_iwb_l<S, C, 128, 8, 8>(d, cur, past, s);
+    case 2: return launch_iwb_l<S, C, 128, 4, 12>(d, cur, past, s);
+    default: return launch_iwb_l<S, C, 64, 8, 12>(d, cur, past, s);
+  }
+}
+
 template <typename S>
 int launch_iwb_tma_s(pfdtd_domain* d, const void* cur, void* past, cudaStream_t s) {
-  if (sizeof(S) == 4 && d->X % 128 == 0) {
-    if (d->cls_bytes == 1)
-      return launch_tma_t<S, uint8_t, 3, Layout<S, uint8_t, 128, 8, 8, true>>(d, cur, past, s);
-    return launch_tma_t<S, uint16_t, 3, Layout<S, uint16_t, 128, 8, 8, true>>(d, cur, past, s);
-  }
-  if (d->cls_bytes == 1)
-    return launch_tma_t<S, uint8_t, 3, Layout<S, uint8_t, 64, 16, 8, true>>(d, cur, past, s);
-  return launch_tma_t<S, uint16_t, 3, Layout<S, uint16_t, 64, 16, 8, true>>(d, cur, past, s);
+  return d->cls_bytes == 1 ? launch_iwb_c<S, uint8_t>(d, cur, past, s)
+                           : launch_iwb_c<S, uint16_t>(d, cur, past, s);
 }
 
 }  // namespace
