@@ -214,10 +214,19 @@ __device__ __forceinline__ void iwb_consumer(const S* Pm, const S* Pc, const S* 
       const V4<S> mid = lds4(row);
 #pragma unroll
       for (int e = 0; e < 4; ++e) v[a][b][e + 1] = St::load(mid.v[e]);
-      const int64_t g = idx + (int64_t)(a - 1) * XY + (int64_t)(b - 1) * X;
-      v[a][b][0] = x == 0 ? St::load(P[g - 1]) : St::load(row[-1]);
-      v[a][b][5] = x + kVec == X ? St::load(P[g + kVec]) : St::load(row[kVec]);
+      v[a][b][0] = St::load(row[-1]);
+      v[a][b][5] = St::load(row[kVec]);
     }
+  if (x == 0 || x + kVec == X) {  // grid x edge: the flat neighbour wraps to the next row
+#pragma unroll
+    for (int a = 0; a < 3; ++a)
+#pragma unroll
+      for (int b = 0; b < 3; ++b) {
+        const int64_t g = idx + (int64_t)(a - 1) * XY + (int64_t)(b - 1) * X;
+        if (x == 0) v[a][b][0] = St::load(P[g - 1]);
+        if (x + kVec == X) v[a][b][5] = St::load(P[g + kVec]);
+      }
+  }
   const V4<S> vpp = lds4(Pq + ci);
   const uint32_t mks[kVec] = {mk4.x, mk4.y, mk4.z, mk4.w};
   unsigned cid[kVec];
