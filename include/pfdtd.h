@@ -328,6 +328,34 @@ int pfdtd_encode_nodes(int centred, uint8_t* d_pos, uint8_t* d_mat, int64_t n, i
 /* The same translation on host arrays (no device work). */
 int pfdtd_encode_nodes_host(int centred, uint8_t* pos, uint8_t* mat, int64_t n);
 
+/* Solid voxelization of a closed triangle mesh (the room's boundary, closed
+ * obstacles inside) into the voxelizer's node bytes: boundary id 0..27 and
+ * material byte per node, flat x-fastest (replaces the external voxelizer
+ * the reference calls from voxelizationUtils.cu:55-136; that library is not
+ * vendored, so its exact output is not pinned).  vertices [n_vertices * 3],
+ * indices [n_triangles * 3], tri_materials [n_triangles] (null: 0).  Node i
+ * at bbox_min + (i - 1) * voxel_edge (the reference's element coordinates,
+ * ROUND(p/dx) + 1), one outside layer on every side; dims and origin (the
+ * position of node 0) are returned; with both
+ * output arrays null only dims/origin are computed, else both must hold
+ * dims[0]*dims[1]*dims[2] bytes.  Inside = odd number of crossings of a +z
+ * ray; a solid node next to air takes the material of the triangle between
+ * it and its first air neighbour (-x,+x,-y,+y,-z,+z); a boundary node the
+ * material of its first solid neighbour; air nodes with solid on both sides
+ * of an axis are closed first.  At most 64 crossings per column. */
+int pfdtd_voxelize(const float* vertices, int64_t n_vertices, const uint32_t* indices,
+                   int64_t n_triangles, const uint8_t* tri_materials, double voxel_edge,
+                   int device, uint32_t dims[3], double origin[3], uint8_t* bid_out,
+                   uint8_t* mat_out);
+
+/* Transparent source vector on the device (SimulationParameters.cpp:300-310,
+ * which evaluates it per step on the host, O(steps^2) for a whole run):
+ * out[n] = samples[n] - sum_{i<n} grid_ir[n-i] * samples[i] in float, in the
+ * reference's order (ascending i), grid_ir[k] = 0 for k >= n_ir.  Host arrays
+ * of `steps` floats; out may alias nothing. */
+int pfdtd_transparent_source(const float* samples, int64_t steps, const float* grid_ir,
+                             int64_t n_ir, float* out, int device);
+
 /* Count air and boundary nodes (calcBoundaries, cudaMesh.cu:500-514). */
 int pfdtd_count_boundaries(const uint8_t* d_pos, int64_t n, uint8_t air_value,
                            uint8_t outside_value, int device, uint32_t* air,

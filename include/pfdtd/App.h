@@ -138,6 +138,8 @@ class App {
   unsigned int num_elements_;
   // geometry
   unsigned int number_of_triangles_ = 0;
+  std::vector<float> mesh_vertices_;        // triangle mesh for the voxelizer
+  std::vector<unsigned int> mesh_indices_;
   std::vector<unsigned char> voxel_ids_;
   std::vector<unsigned char> voxel_mats_;
   uint3 voxel_dims_ = {0, 0, 0};

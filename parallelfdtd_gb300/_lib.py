@@ -91,6 +91,9 @@ _SIGNATURES = {
     "pfdtd_query": (_i32, [_vp, C.POINTER(_i32)]),
     "pfdtd_fetch_receivers": (_i32, [_vp, _vp]),
     "pfdtd_encode_nodes_host": (_i32, [_i32, _vp, _vp, _i64]),
+    "pfdtd_transparent_source": (_i32, [_vp, _i64, _vp, _i64, _vp, _i32]),
+    "pfdtd_voxelize": (_i32, [_vp, _i64, _vp, _i64, _vp, C.c_double, _i32,
+                              C.POINTER(C.c_uint32), C.POINTER(C.c_double), _vp, _vp]),
     # request loop (pfdtd_server.h)
     "pfdtd_request_create": (_i32, [_i64, _i64, _i64, _i32, _i32, _i32, _i64, C.POINTER(_vp)]),
     "pfdtd_request_set_voxels": (_i32, [_vp, _vp, _vp]),

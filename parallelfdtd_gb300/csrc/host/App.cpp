@@ -91,11 +91,17 @@ void App::initializeDevices() {
   g_current_app = this;
 }
 
+// The triangle mesh (App.cpp:141-145); voxelized on the device by
+// initializeMesh unless voxels were given with initializeVoxels.
 void App::initializeGeometry(unsigned int* indices, float* vertices,
                              unsigned int number_of_indices, unsigned int number_of_vertices) {
-  (void)vertices;
-  (void)number_of_vertices;
   number_of_triangles_ = indices ? number_of_indices / 3 : 0;
+  mesh_indices_.assign(indices, indices + (indices ? number_of_indices : 0));
+  // number_of_vertices counts floats, as GeometryHandler::initialize
+  // (GeometryHandler.cpp:87-100)
+  mesh_vertices_.assign(vertices, vertices + (vertices ? (size_t)number_of_vertices : 0));
+  voxel_ids_.clear();
+  voxel_mats_.clear();
 }
 
 void App::initializeVoxels(const unsigned char* ids, const unsigned char* mats, uint3 dims) {
@@ -112,10 +118,40 @@ void App::setUniformMaterial(float R) {
 // Voxel upload, mesh set-up and the reference's partition decision
 // (App.cpp:147-234); every partition count maps to one domain.
 void App::initializeMesh(unsigned int number_of_partitions) {
+  if (voxel_ids_.empty() && !mesh_indices_.empty()) {
+    // voxelizeGeometry (App.cpp:181-191): voxel edge = dx, one material byte
+    // per triangle from the material handler
+    uint32_t dims[3];
+    double origin[3];
+    const unsigned char* tri_mat = m_materials.getMaterialIdxPtr();
+    std::vector<unsigned char> zeros;
+    if (!tri_mat || m_materials.getNumberOfSurfaces() < number_of_triangles_) {
+      zeros.assign(number_of_triangles_, 0);
+      tri_mat = zeros.data();
+    }
+    int dev = 0;
+    cudaGetDevice(&dev);
+    const int64_t nv = (int64_t)mesh_vertices_.size() / 3, nt = (int64_t)number_of_triangles_;
+    const double dx = (double)m_parameters.getDx();
+    if (pfdtd_voxelize(mesh_vertices_.data(), nv, mesh_indices_.data(), nt, tri_mat, dx, dev,
+                       dims, origin, nullptr, nullptr) != PFDTD_OK) {
+      c_log_msg(LOG_ERROR, "App::initializeMesh - voxelization: %s", pfdtd_last_error());
+      throw(-1);
+    }
+    const size_t n = (size_t)dims[0] * dims[1] * dims[2];
+    voxel_ids_.assign(n, 0);
+    voxel_mats_.assign(n, 0);
+    if (pfdtd_voxelize(mesh_vertices_.data(), nv, mesh_indices_.data(), nt, tri_mat, dx, dev,
+                       dims, origin, voxel_ids_.data(), voxel_mats_.data()) != PFDTD_OK) {
+      c_log_msg(LOG_ERROR, "App::initializeMesh - voxelization: %s", pfdtd_last_error());
+      throw(-1);
+    }
+    voxel_dims_ = make_uint3(dims[0], dims[1], dims[2]);
+  }
   if (voxel_ids_.empty()) {
     c_log_msg(LOG_ERROR,
-              "App::initializeMesh - no voxelized geometry: the triangle voxelizer is not part "
-              "of this library, call initializeVoxels first");
+              "App::initializeMesh - no geometry: call initializeGeometry (triangle mesh) or "
+              "initializeVoxels first");
     throw(-1);
   }
   if (m_materials.getNumberOfUniqueMaterials() == 0) {

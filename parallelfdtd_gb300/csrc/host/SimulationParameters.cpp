@@ -9,6 +9,9 @@
 #include <atomic>
 
 #include "logger.h"
+#include "pfdtd.h"
+
+#include <cuda_runtime.h>
 
 unsigned long long SimulationParameters::nextVersion() {
   static std::atomic<unsigned long long> counter{0};
@@ -252,6 +255,25 @@ float SimulationParameters::getDx() const {
 float* SimulationParameters::getSourceVectorAt(unsigned int source_idx) {
   std::vector<float> v(getNumSteps(), 0.f);
   source_output_data_.resize(getNumSources());
+  int n_dev = 0;
+  if (getSource(source_idx).getSourceType() == SRC_TRANSPARENT && getNumSteps() > 0 &&
+      pfdtd_device_count(&n_dev) == PFDTD_OK && n_dev > 0) {
+    // The whole transparent vector on the device: O(steps * IR length) in
+    // parallel instead of the per-step host sum.
+    std::vector<float> regular(getNumSteps());
+    for (unsigned int i = 0; i < getNumSteps(); ++i)
+      regular[i] = getRegularSourceSample(source_idx, i);
+    int dev = 0;
+    cudaGetDevice(&dev);
+    if (pfdtd_transparent_source(regular.data(), (int64_t)regular.size(),
+                                 grid_ir_.empty() ? nullptr : grid_ir_.data(),
+                                 (int64_t)grid_ir_.size(), v.data(), dev) != PFDTD_OK) {
+      c_log_msg(LOG_ERROR, "SimulationParameters::getSourceVectorAt - %s", pfdtd_last_error());
+      throw(-1);
+    }
+    source_output_data_.at(source_idx) = v;
+    return &(source_output_data_.at(source_idx)[0]);
+  }
   for (unsigned int i = 0; i < getNumSteps(); ++i) v[i] = getSourceSample(source_idx, i);
   source_output_data_.at(source_idx) = v;
   return &(source_output_data_.at(source_idx)[0]);

@@ -222,3 +222,56 @@ int pfdtd_capture_slice(pfdtd_domain* d, int orientation, int64_t slice, float* 
 }
 
 }  // extern "C"
+
+// ---------------------------------------------------------------------------
+// Transparent source (SimulationParameters.cpp:300-310): out[n] = s[n] -
+// sum_{i<n} h[n-i] * s[i] in float, every product and sum rounded on its own,
+// terms added in ascending i as the reference's loop.  The terms with
+// n - i >= n_ir (h = 0 there) are skipped, which can change the sign of a zero
+// result only.  One thread per output sample.
+namespace pfdtd {
+namespace {
+__global__ void k_transparent(const float* __restrict__ s, const float* __restrict__ h,
+                              int64_t n_ir, int64_t steps, float* __restrict__ out) {
+  for (int64_t n = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; n < steps;
+       n += (int64_t)gridDim.x * blockDim.x) {
+    float acc = 0.f;
+    const int64_t i0 = n_ir > 0 ? (n - (n_ir - 1) > 0 ? n - (n_ir - 1) : 0) : n;
+    for (int64_t i = i0; i < n; ++i) acc = __fadd_rn(acc, __fmul_rn(h[n - i], s[i]));
+    out[n] = __fsub_rn(s[n], acc);
+  }
+}
+}  // namespace
+}  // namespace pfdtd
+
+extern "C" int pfdtd_transparent_source(const float* samples, int64_t steps, const float* grid_ir,
+                                        int64_t n_ir, float* out, int device) {
+  using namespace pfdtd;
+  if (steps < 0 || n_ir < 0 || (steps > 0 && (!samples || !out)) || (n_ir > 0 && !grid_ir))
+    return fail(PFDTD_ERR_ARG, "invalid transparent source arrays");
+  if (steps == 0) return PFDTD_OK;
+  DevGuard g(device);
+  cudaStream_t s = nullptr;
+  PFDTD_CK(cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking));
+  float *d_s = nullptr, *d_h = nullptr, *d_o = nullptr;
+  cudaError_t e = cudaMallocAsync((void**)&d_s, steps * sizeof(float), s);
+  if (e == cudaSuccess) e = cudaMallocAsync((void**)&d_o, steps * sizeof(float), s);
+  if (e == cudaSuccess) e = cudaMallocAsync((void**)&d_h, std::max<int64_t>(n_ir, 1) * sizeof(float), s);
+  if (e == cudaSuccess) e = cudaMemcpyAsync(d_s, samples, steps * sizeof(float), cudaMemcpyHostToDevice, s);
+  if (e == cudaSuccess && n_ir > 0)
+    e = cudaMemcpyAsync(d_h, grid_ir, n_ir * sizeof(float), cudaMemcpyHostToDevice, s);
+  if (e == cudaSuccess) {
+    k_transparent<<<grid_for(steps), 256, 0, s>>>(d_s, d_h, n_ir, steps, d_o);
+    count_launch();
+    e = cudaGetLastError();
+  }
+  if (e == cudaSuccess) e = cudaMemcpyAsync(out, d_o, steps * sizeof(float), cudaMemcpyDeviceToHost, s);
+  if (d_s) cudaFreeAsync(d_s, s);
+  if (d_o) cudaFreeAsync(d_o, s);
+  if (d_h) cudaFreeAsync(d_h, s);
+  const cudaError_t e2 = cudaStreamSynchronize(s);
+  cudaStreamDestroy(s);
+  if (e == cudaSuccess) e = e2;
+  if (e != cudaSuccess) return cuda_fail(e, "transparent source", __FILE__, __LINE__);
+  return PFDTD_OK;
+}

@@ -41,6 +41,18 @@ def default_params(octave: int = 0, scheme="forward", lam: Optional[float] = Non
     return np.array([lam, lam * lam, 1.0 / 3.0, float(octave)], dtype=np.float64)
 
 
+def transparent_source(samples: np.ndarray, grid_ir: np.ndarray, device: int = 0) -> np.ndarray:
+    """Transparent source vector computed on the device:
+    out[n] = s[n] - sum_{i<n} h[n-i] s[i] in float, in the reference's order
+    (SimulationParameters.cpp:300-310)."""
+    s = np.ascontiguousarray(samples, dtype=np.float32).reshape(-1)
+    h = np.ascontiguousarray(grid_ir, dtype=np.float32).reshape(-1)
+    out = np.empty_like(s)
+    L.call("pfdtd_transparent_source", s.ctypes.data, s.size, h.ctypes.data if h.size else None,
+           h.size, out.ctypes.data, int(device))
+    return out
+
+
 def _ptr(a: np.ndarray) -> C.c_void_p:
     return C.c_void_p(a.ctypes.data)
 

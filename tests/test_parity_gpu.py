@@ -637,3 +637,18 @@ def test_batched_fields_equal_independent_runs(gpu, O, fields, prec, scheme, var
                         scheme=code, double=(prec == "f64"),
                         storage=(prec if prec in ("f16", "bf16") else None), dif=(flags, table))
         assert np.array_equal(g[2 * f:2 * f + 2], r), f"field {f}"
+
+
+@pytest.mark.parametrize("input_type,steps,n_ir", [(1, 600, 1000), (0, 900, 250), (3, 400, 0)])
+def test_transparent_source_on_device(gpu, O, input_type, steps, n_ir):
+    """The device transparent-source vector equals the oracle's per-step
+    restatement of SimulationParameters::getTransparentSourceSample."""
+    from parallelfdtd_gb300.domain import transparent_source
+    rng = np.random.default_rng(3)
+    h = (rng.standard_normal(n_ir) * 0.05).astype(np.float32) if n_ir else np.zeros(0, np.float32)
+    data = rng.standard_normal(steps).astype(np.float32)
+    regular = O.source_vector(1, input_type, steps, data=data if input_type == 3 else None)
+    ref = O.source_vector(2, input_type, steps, data=data if input_type == 3 else None,
+                          grid_ir=h if n_ir else None)
+    got = transparent_source(regular, h)
+    assert np.array_equal(got, ref)
