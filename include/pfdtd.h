@@ -252,6 +252,23 @@ int pfdtd_capture_slice_noalloc(pfdtd_domain* d, int orientation, int64_t slice,
  * of the last asynchronous run to the host.  No call waits for other
  * domains' work. */
 int pfdtd_run_async(pfdtd_domain* d, int64_t steps);
+/* Run `steps` steps from step 0 and capture slices on the way
+ * (App::runCapture / captureSliceFast, App.cpp:407-436 and
+ * visualizationUtils.cu:130-254, which step one at a time and gather and
+ * copy each slice synchronously): capture i is the slice cap_slice[i] of
+ * orientation cap_orientation[i] (0 xy, 1 xz, 2 yz, as pfdtd_capture_slice)
+ * of the field after cap_step[i] steps (0 <= cap_step[i] <= steps).  The
+ * run is split at the capture steps, whole chunks still replay their CUDA
+ * graphs, and each capture is a gather kernel and an asynchronous copy into
+ * p_out[i] (floats) and pos_out[i] (node bytes) on the domain's stream
+ * (either array, or one of its entries, may be null).  Pinned host buffers
+ * (pfdtd_host_alloc) keep the copies asynchronous.  Receivers as pfdtd_run. */
+int pfdtd_run_captures(pfdtd_domain* d, int64_t steps, void* out, int n_cap,
+                       const int64_t* cap_step, const int32_t* cap_orientation,
+                       const int64_t* cap_slice, float* const* p_out, uint8_t* const* pos_out);
+/* Page-locked host memory for asynchronous copies. */
+int pfdtd_host_alloc(size_t bytes, void** ptr);
+int pfdtd_host_free(void* ptr);
 int pfdtd_query(pfdtd_domain* d, int* done);
 int pfdtd_fetch_receivers(pfdtd_domain* d, void* out);
 
@@ -347,6 +364,16 @@ int pfdtd_voxelize(const float* vertices, int64_t n_vertices, const uint32_t* in
                    int64_t n_triangles, const uint8_t* tri_materials, double voxel_edge,
                    int device, uint32_t dims[3], double origin[3], uint8_t* bid_out,
                    uint8_t* mat_out);
+
+/* Receiver post-processing (python/FDTDfilter.py:13-19,
+ * matlab/functions/FDTDpostFilter.m:1-31) on the device: each of n_channels
+ * traces of n_samples (row-major, float or double) is convolved with the
+ * causal FIR `taps` (lfilter(taps, 1, x)), then, with dc_block != 0, passed
+ * through y[n] = x[n] - x[n-1] + dc_coef * y[n-1].  Arithmetic in double.
+ * Host arrays. */
+int pfdtd_post_filter(const void* x, int64_t n_channels, int64_t n_samples, int is_double,
+                      const double* taps, int n_taps, int dc_block, double dc_coef, void* out,
+                      int device);
 
 /* Transparent source vector on the device (SimulationParameters.cpp:300-310,
  * which evaluates it per step on the host, O(steps^2) for a whole run):

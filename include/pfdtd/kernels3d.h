@@ -23,4 +23,14 @@ void launchFDTD3dStep(CudaMesh* d_mesh, SimulationParameters* sp, float* h_retur
                       unsigned int step, int step_direction,
                       void (*progressCallback)(int, int, float));
 
+// All sp->getNumSteps() single-precision steps in one queued run, with the
+// slice captures (step, orientation, slice) gathered on the device and copied
+// into the caller's pinned buffers p_out[i] / pos_out[i] when their step is
+// reached (no counterpart in the reference, whose capture loop steps and
+// copies synchronously: App.cpp:407-436).
+void launchFDTD3dCaptures(CudaMesh* d_mesh, SimulationParameters* sp, float* h_return_ptr,
+                          int n_capture, const int64_t* capture_step,
+                          const int32_t* capture_orientation, const int64_t* capture_slice,
+                          float* const* p_out, uint8_t* const* pos_out);
+
 #endif

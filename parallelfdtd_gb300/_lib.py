@@ -88,10 +88,16 @@ _SIGNATURES = {
     "pfdtd_get_kernel": (_i32, [_vp, C.POINTER(_i32)]),
     "pfdtd_set_temporal_block": (_i32, [_vp, _i32]),
     "pfdtd_run_async": (_i32, [_vp, _i64]),
+    "pfdtd_run_captures": (_i32, [_vp, _i64, _vp, _i32, C.POINTER(_i64), C.POINTER(C.c_int32),
+                                  C.POINTER(_i64), C.POINTER(_vp), C.POINTER(_vp)]),
+    "pfdtd_host_alloc": (_i32, [C.c_size_t, C.POINTER(_vp)]),
+    "pfdtd_host_free": (_i32, [_vp]),
     "pfdtd_query": (_i32, [_vp, C.POINTER(_i32)]),
     "pfdtd_fetch_receivers": (_i32, [_vp, _vp]),
     "pfdtd_encode_nodes_host": (_i32, [_i32, _vp, _vp, _i64]),
     "pfdtd_transparent_source": (_i32, [_vp, _i64, _vp, _i64, _vp, _i32]),
+    "pfdtd_post_filter": (_i32, [_vp, _i64, _i64, _i32, C.POINTER(C.c_double), _i32, _i32,
+                                 C.c_double, _vp, _i32]),
     "pfdtd_voxelize": (_i32, [_vp, _i64, _vp, _i64, _vp, C.c_double, _i32,
                               C.POINTER(C.c_uint32), C.POINTER(C.c_double), _vp, _vp]),
     # request loop (pfdtd_server.h)

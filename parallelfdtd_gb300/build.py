@@ -24,7 +24,7 @@ LIB = os.path.join(PKG, "libpfdtd.so")
 
 CUDA_SOURCES = ["stencil.cu", "stencil_tma.cu", "stencil_tb.cu", "stencil_tb_f32.cu",
                 "stencil_tb_f16.cu", "stencil_tb_bf16.cu", "dif.cu", "domain.cu", "setup.cu",
-                "noalloc.cu", "voxelize.cu"]
+                "noalloc.cu", "voxelize.cu", "postfilter.cu"]
 CXX_SOURCES = [
     "classes_host.cpp",
     "host/logger.cpp",

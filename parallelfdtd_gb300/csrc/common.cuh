@@ -224,6 +224,9 @@ int build_dif(pfdtd_domain* d, const std::vector<uint16_t>& keys,
               const std::vector<uint8_t>& main_tab);
 int launch_dif(pfdtd_domain* d, const void* cur, void* past, cudaStream_t s);
 int launch_dif_init(pfdtd_domain* d, cudaStream_t s);
+// Implemented in setup.cu
+int launch_slice_gather(pfdtd_domain* d, int orientation, int64_t slice, float* dp, uint8_t* dq,
+                        cudaStream_t s);
 int tma_tile_count();
 int launch_update_tma(pfdtd_domain* d, const void* cur, void* past, cudaStream_t s);
 int launch_iwb_tma(pfdtd_domain* d, const void* cur, void* past, cudaStream_t s);

@@ -10,6 +10,7 @@
 // reports progress between chunks.
 #include "common.cuh"
 
+#include <algorithm>
 #include <chrono>
 #include <cstdlib>
 #include <cstring>
@@ -270,6 +271,27 @@ int enqueue_run(pfdtd_domain* d, int64_t steps, void* rec_out, F&& between, bool
   cudaEventDestroy(ev[1]);
   *steps_queued = queued;
   return rc;
+}
+
+// Queue `n` steps continuing from the device step counter, without host
+// waits: chunk graphs for whole chunks, then blocked launches and single
+// steps.  rec_ld / inject_end as in enqueue_run (the run's step count).
+int enqueue_steps(pfdtd_domain* d, int64_t n, void* rec_out, int64_t rec_ld, int64_t inject_end) {
+  cudaStream_t s = d->stream;
+  const int tb = tb_active(d) ? d->tb_depth : 0;
+  const int64_t chunk = tb ? kChunkTb : kChunk;
+  int64_t done = 0;
+  for (; done + chunk <= n; done += chunk) {
+    cudaGraphExec_t exec = nullptr;
+    if (int rc = get_chunk_graph(d, rec_out, rec_ld, inject_end, &exec)) return rc;
+    PFDTD_CK(cudaGraphLaunch(exec, s));
+    count_launch(tb ? 2 * (chunk / tb) : 2 * chunk);
+  }
+  for (; tb && done + tb <= n; done += tb)
+    if (int rc = launch_tb(d, rec_out, rec_ld, inject_end, s)) return rc;
+  for (; done < n; ++done)
+    if (int rc = enqueue_step(d, rec_out, rec_ld, inject_end, s)) return rc;
+  return PFDTD_OK;
 }
 
 }  // namespace
@@ -663,6 +685,97 @@ int pfdtd_run_async(pfdtd_domain* d, int64_t steps) {
   rc = enqueue_run(d, steps, d->d_rec_out, [](int64_t) { return 0; }, &stopped, &queued, false);
   if (rc == PFDTD_OK) d->async_steps = steps;
   return rc;
+}
+
+int pfdtd_run_captures(pfdtd_domain* d, int64_t steps, void* out, int n_cap,
+                       const int64_t* cap_step, const int32_t* cap_orientation,
+                       const int64_t* cap_slice, float* const* p_out, uint8_t* const* pos_out) {
+  if (int rc = check_domain(d)) return rc;
+  if (steps < 0 || n_cap < 0) return fail(PFDTD_ERR_ARG, "negative count");
+  if (n_cap > 0 && (!cap_step || !cap_orientation || !cap_slice || (!p_out && !pos_out)))
+    return fail(PFDTD_ERR_ARG, "invalid capture schedule");
+  if (d->n_rec > 0 && !out && steps > 0) return fail(PFDTD_ERR_ARG, "null output buffer");
+  std::vector<int> order(n_cap);
+  std::vector<int64_t> size(n_cap), offset(n_cap + 1, 0);
+  for (int i = 0; i < n_cap; ++i) {
+    const int o = cap_orientation[i];
+    if (o < 0 || o > 2) return fail(PFDTD_ERR_ARG, "orientation must be 0, 1 or 2");
+    const int64_t lim = o == 0 ? d->Z : (o == 1 ? d->Y : d->X);
+    if (cap_slice[i] < 0 || cap_slice[i] >= lim) return fail(PFDTD_ERR_ARG, "slice outside the grid");
+    if (cap_step[i] < 0 || cap_step[i] > steps) return fail(PFDTD_ERR_ARG, "capture step outside the run");
+    size[i] = (o == 2 ? d->Y : d->X) * (o == 0 ? d->Y : d->Z);
+    offset[i + 1] = offset[i] + size[i];
+    order[i] = i;
+  }
+  std::stable_sort(order.begin(), order.end(),
+                   [&](int a, int b) { return cap_step[a] < cap_step[b]; });
+  DeviceGuard g(d->device);
+  int rc = prepare_run(d);
+  if (rc) return rc;
+  rc = ensure_rec_out(d, std::max<int64_t>(steps, 1));
+  if (rc) return rc;
+  cudaStream_t s = d->stream;
+  const size_t rec_bytes = (size_t)d->n_rec * (size_t)steps * d->arith_size();
+  if (rec_bytes) PFDTD_CK(cudaMemsetAsync(d->d_rec_out, 0, rec_bytes, s));
+  // device staging for every capture: floats, then node bytes
+  void* stage = nullptr;
+  const int64_t total = offset[n_cap];
+  if (total > 0 && d->alloc(&stage, (size_t)total * 5) != cudaSuccess)
+    return fail(PFDTD_ERR_NOMEM, "capture staging allocation failed");
+  float* sp = (float*)stage;
+  uint8_t* sq = (uint8_t*)stage + (size_t)total * 4;
+  PFDTD_CK(cudaMemsetAsync(d->d_step, 0, sizeof(int64_t), s));
+  rc = launch_dif_init(d, s);
+  int64_t at = 0;
+  for (int k = 0; k < n_cap && rc == PFDTD_OK; ++k) {
+    const int i = order[k];
+    rc = enqueue_steps(d, cap_step[i] - at, d->d_rec_out, steps, steps);
+    at = cap_step[i];
+    if (rc) break;
+    float* dp = p_out && p_out[i] ? sp + offset[i] : nullptr;
+    uint8_t* dq = pos_out && pos_out[i] ? sq + offset[i] : nullptr;
+    rc = launch_slice_gather(d, cap_orientation[i], cap_slice[i], dp, dq, s);
+    if (rc) break;
+    cudaError_t e = cudaSuccess;
+    if (dp) e = cudaMemcpyAsync(p_out[i], dp, size[i] * sizeof(float), cudaMemcpyDeviceToHost, s);
+    if (e == cudaSuccess && dq) e = cudaMemcpyAsync(pos_out[i], dq, size[i], cudaMemcpyDeviceToHost, s);
+    if (e != cudaSuccess) rc = cuda_fail(e, "capture copy", __FILE__, __LINE__);
+  }
+  if (rc == PFDTD_OK) rc = enqueue_steps(d, steps - at, d->d_rec_out, steps, steps);
+  // record the receivers of the last step; never inject
+  if (rc == PFDTD_OK && steps > 0) rc = launch_io(d, d->cur_field(), d->d_rec_out, steps, 0, s);
+  if (rc == PFDTD_OK) {
+    const size_t row = (size_t)steps * d->arith_size();
+    for (int r = 0; r < d->n_rec && rc == PFDTD_OK && steps > 0; ++r)
+      if (d->rec_idx_h[r] >= 0) {
+        cudaError_t e = cudaMemcpyAsync((char*)out + r * row, (char*)d->d_rec_out + r * row, row,
+                                        cudaMemcpyDeviceToHost, s);
+        if (e != cudaSuccess) rc = cuda_fail(e, "receiver copy", __FILE__, __LINE__);
+      }
+  }
+  d->release(stage);
+  const cudaError_t e = cudaStreamSynchronize(s);
+  if (rc) return rc;
+  if (e != cudaSuccess) return cuda_fail(e, "captured run", __FILE__, __LINE__);
+  return check_pipeline(d);
+}
+
+int pfdtd_host_alloc(size_t bytes, void** ptr) {
+  if (!ptr) return fail(PFDTD_ERR_ARG, "null output");
+  *ptr = nullptr;
+  if (bytes == 0) return PFDTD_OK;
+  cudaError_t e = cudaHostAlloc(ptr, bytes, cudaHostAllocDefault);
+  if (e != cudaSuccess) {
+    cudaGetLastError();
+    *ptr = nullptr;
+    return fail(PFDTD_ERR_NOMEM, "pinned host allocation failed");
+  }
+  return PFDTD_OK;
+}
+
+int pfdtd_host_free(void* ptr) {
+  if (ptr) PFDTD_CK(cudaFreeHost(ptr));
+  return PFDTD_OK;
 }
 
 int pfdtd_query(pfdtd_domain* d, int* done) {

@@ -211,11 +211,69 @@ void App::runVisualization() {
   throw(-1);
 }
 
+// App.cpp:385-405: the reference steps one at a time, capturing the
+// scheduled slices and meshes after each step.  Forward runs from step 0
+// with slice captures only take the asynchronous captured run instead (one
+// run, graph-replayed chunks, device gathers and asynchronous copies; the
+// interrupt callback is polled once, before the run); the bitmaps are the
+// same.
 void App::runCapture() {
   m_mesh.setDouble(false);
   initializeMesh(2);
   const unsigned steps = m_parameters.getNumSteps();
   responses_.assign((size_t)steps * m_parameters.getNumReceivers(), 0.f);
+  if (step_direction_ == 1 && current_step_ == 0 && mesh_to_capture_.empty()) {
+    if (m_interrupt && m_interrupt()) return;
+    std::vector<int64_t> cs, sl;
+    std::vector<int32_t> co;
+    std::vector<unsigned> w, h;
+    for (size_t i = 0; i < step_to_capture_.size(); ++i) {
+      const unsigned st = step_to_capture_[i], slice = slice_to_capture_[i];
+      const unsigned o = slice_orientation_[i];
+      const unsigned lim = o == 0 ? m_mesh.getDimZ() : (o == 1 ? m_mesh.getDimY() : m_mesh.getDimX());
+      if (st < 1 || st > steps || o > 2) continue;  // never reached by the stepping loop
+      if (slice >= lim) {
+        c_log_msg(LOG_INFO, "captureSliceFast - slice %u out of bounds, no capture made", slice);
+        continue;
+      }
+      cs.push_back(st);
+      co.push_back((int32_t)o);
+      sl.push_back(slice);
+      w.push_back(o == 2 ? m_mesh.getDimY() : m_mesh.getDimX());
+      h.push_back(o == 0 ? m_mesh.getDimY() : m_mesh.getDimZ());
+    }
+    const size_t n = cs.size();
+    std::vector<float*> pp(n, nullptr);
+    std::vector<uint8_t*> qq(n, nullptr);
+    int rc = PFDTD_OK;
+    for (size_t i = 0; i < n && rc == PFDTD_OK; ++i) {
+      rc = pfdtd_host_alloc((size_t)w[i] * h[i] * sizeof(float), (void**)&pp[i]);
+      if (rc == PFDTD_OK) rc = pfdtd_host_alloc((size_t)w[i] * h[i], (void**)&qq[i]);
+    }
+    auto free_all = [&]() {
+      for (size_t i = 0; i < n; ++i) {
+        pfdtd_host_free(pp[i]);
+        pfdtd_host_free(qq[i]);
+      }
+    };
+    if (rc != PFDTD_OK) {
+      free_all();
+      c_log_msg(LOG_ERROR, "App::runCapture - %s", pfdtd_last_error());
+      throw(-1);
+    }
+    try {
+      launchFDTD3dCaptures(&m_mesh, &m_parameters, responses_.empty() ? nullptr : responses_.data(),
+                           (int)n, cs.data(), co.data(), sl.data(), pp.data(), qq.data());
+    } catch (...) {
+      free_all();
+      throw;
+    }
+    for (size_t i = 0; i < n; ++i)
+      saveBitmap(pp[i], qq[i], w[i], h[i], (unsigned)sl[i], (unsigned)co[i], (unsigned)cs[i]);
+    free_all();
+    current_step_ = steps;
+    return;
+  }
   for (unsigned i = 0; i < steps; ++i) {
     executeStep();
     if (m_interrupt && m_interrupt()) break;

@@ -106,6 +106,17 @@ float launchFDTD3dDouble(CudaMesh* d_mesh, SimulationParameters* sp, double* h_r
   return run(d_mesh, sp, h_return_ptr, interruptCallback, progressCallback, true);
 }
 
+void launchFDTD3dCaptures(CudaMesh* d_mesh, SimulationParameters* sp, float* h_return_ptr,
+                          int n_capture, const int64_t* capture_step,
+                          const int32_t* capture_orientation, const int64_t* capture_slice,
+                          float* const* p_out, uint8_t* const* pos_out) {
+  configure(d_mesh, sp, false);
+  check(pfdtd_run_captures(d_mesh->getDomain(), sp->getNumSteps(), h_return_ptr, n_capture,
+                           capture_step, capture_orientation, capture_slice, p_out, pos_out),
+        "launchFDTD3dCaptures");
+  d_mesh->syncViews();
+}
+
 void launchFDTD3dStep(CudaMesh* d_mesh, SimulationParameters* sp, float* h_return_ptr,
                       unsigned int step, int step_direction,
                       void (*progressCallback)(int, int, float)) {

@@ -1,0 +1,100 @@
+// Post-processing of receiver traces (python/FDTDfilter.py:13-19,
+// matlab/functions/FDTDpostFilter.m:1-31): a causal FIR low-pass, then an
+// optional DC blocker y[n] = x[n] - x[n-1] + a y[n-1], over many channels.
+// Arithmetic in double; float or double input and output.
+#include "common.cuh"
+
+#include <algorithm>
+
+namespace pfdtd {
+namespace {
+
+// y[c][n] = sum_{k <= min(n, nb-1)} b[k] x[c][n-k]; one thread per output.
+template <typename T>
+__global__ void k_fir(const T* __restrict__ x, int64_t n_ch, int64_t n, const double* __restrict__ b,
+                      int nb, T* __restrict__ y) {
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n_ch * n;
+       i += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t c = i / n, t = i - c * n;
+    const T* xc = x + c * n;
+    double acc = 0.0;
+    const int kmax = t < (int64_t)(nb - 1) ? (int)t : nb - 1;
+    for (int k = 0; k <= kmax; ++k) acc += b[k] * (double)xc[t - k];
+    y[i] = (T)acc;
+  }
+}
+
+// DC blocker in place, one thread per channel (the recursion is sequential).
+template <typename T>
+__global__ void k_dc_block(T* __restrict__ y, int64_t n_ch, int64_t n, double a) {
+  const int64_t c = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (c >= n_ch) return;
+  T* yc = y + c * n;
+  double xp = 0.0, yp = 0.0;
+  for (int64_t t = 0; t < n; ++t) {
+    const double xv = (double)yc[t];
+    const double v = xv - xp + a * yp;
+    xp = xv;
+    yp = v;
+    yc[t] = (T)v;
+  }
+}
+
+template <typename T>
+int post_filter_t(const T* x, int64_t n_ch, int64_t n, const double* b, int nb, int dc, double a,
+                  T* out, int device) {
+  int prev = -1;
+  cudaGetDevice(&prev);
+  if (prev != device) cudaSetDevice(device);
+  struct Restore {
+    int p;
+    ~Restore() { if (p >= 0) cudaSetDevice(p); }
+  } restore{prev};
+  cudaStream_t s = nullptr;
+  PFDTD_CK(cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking));
+  const size_t bytes = (size_t)n_ch * (size_t)n * sizeof(T);
+  T *dx = nullptr, *dy = nullptr;
+  double* db = nullptr;
+  cudaError_t e = cudaMallocAsync((void**)&dx, bytes, s);
+  if (e == cudaSuccess) e = cudaMallocAsync((void**)&dy, bytes, s);
+  if (e == cudaSuccess) e = cudaMallocAsync((void**)&db, sizeof(double) * nb, s);
+  if (e == cudaSuccess) e = cudaMemcpyAsync(dx, x, bytes, cudaMemcpyHostToDevice, s);
+  if (e == cudaSuccess) e = cudaMemcpyAsync(db, b, sizeof(double) * nb, cudaMemcpyHostToDevice, s);
+  if (e == cudaSuccess) {
+    const int64_t tot = n_ch * n;
+    const int grid = (int)std::max<int64_t>(1, std::min<int64_t>((tot + 255) / 256, 152 * 32));
+    k_fir<T><<<grid, 256, 0, s>>>(dx, n_ch, n, db, nb, dy);
+    count_launch();
+    if (dc) {
+      k_dc_block<T><<<(int)((n_ch + 127) / 128), 128, 0, s>>>(dy, n_ch, n, a);
+      count_launch();
+    }
+    e = cudaGetLastError();
+  }
+  if (e == cudaSuccess) e = cudaMemcpyAsync(out, dy, bytes, cudaMemcpyDeviceToHost, s);
+  for (void* p : {(void*)dx, (void*)dy, (void*)db})
+    if (p) cudaFreeAsync(p, s);
+  const cudaError_t e2 = cudaStreamSynchronize(s);
+  cudaStreamDestroy(s);
+  if (e == cudaSuccess) e = e2;
+  if (e != cudaSuccess) return cuda_fail(e, "post filter", __FILE__, __LINE__);
+  return PFDTD_OK;
+}
+
+}  // namespace
+}  // namespace pfdtd
+
+using namespace pfdtd;
+
+extern "C" int pfdtd_post_filter(const void* x, int64_t n_channels, int64_t n_samples,
+                                 int is_double, const double* taps, int n_taps, int dc_block,
+                                 double dc_coef, void* out, int device) {
+  if (n_channels < 0 || n_samples < 0 || n_taps < 1 || !taps ||
+      (n_channels * n_samples > 0 && (!x || !out)))
+    return fail(PFDTD_ERR_ARG, "invalid filter arguments");
+  if (n_channels * n_samples == 0) return PFDTD_OK;
+  return is_double ? post_filter_t<double>((const double*)x, n_channels, n_samples, taps, n_taps,
+                                           dc_block, dc_coef, (double*)out, device)
+                   : post_filter_t<float>((const float*)x, n_channels, n_samples, taps, n_taps,
+                                          dc_block, dc_coef, (float*)out, device);
+}

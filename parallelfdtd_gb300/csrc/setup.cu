@@ -111,6 +111,26 @@ struct DevGuard {
 };
 
 }  // namespace
+
+// Slice gather of the domain's current field into device buffers (either may
+// be null), queued on stream s; no allocation, no synchronisation.
+int launch_slice_gather(pfdtd_domain* d, int orientation, int64_t slice, float* dp, uint8_t* dq,
+                        cudaStream_t s) {
+  const int64_t w = orientation == 2 ? d->Y : d->X;
+  const int64_t h = orientation == 0 ? d->Y : d->Z;
+  const int64_t n = w * h;
+  const void* cur = d->cur_field();
+  switch (d->precision) {
+    case PFDTD_F32: k_slice<float><<<grid_for(n), 256, 0, s>>>((const float*)cur, d->d_pos, (int)d->X, (int)d->Y, (int)d->Z, orientation, slice, dp, dq, d->K); break;
+    case PFDTD_F64: k_slice<double><<<grid_for(n), 256, 0, s>>>((const double*)cur, d->d_pos, (int)d->X, (int)d->Y, (int)d->Z, orientation, slice, dp, dq, d->K); break;
+    case PFDTD_F16: k_slice<__half><<<grid_for(n), 256, 0, s>>>((const __half*)cur, d->d_pos, (int)d->X, (int)d->Y, (int)d->Z, orientation, slice, dp, dq, d->K); break;
+    default: k_slice<__nv_bfloat16><<<grid_for(n), 256, 0, s>>>((const __nv_bfloat16*)cur, d->d_pos, (int)d->X, (int)d->Y, (int)d->Z, orientation, slice, dp, dq, d->K); break;
+  }
+  count_launch();
+  PFDTD_CK(cudaGetLastError());
+  return PFDTD_OK;
+}
+
 }  // namespace pfdtd
 
 using namespace pfdtd;

@@ -267,6 +267,46 @@ class Domain:
         L.call("pfdtd_get_kernel", self.handle, C.byref(v))
         return {L.KERNEL_ZMARCH: "zmarch", L.KERNEL_TMA: "tma", L.KERNEL_TB: "tb"}[v.value]
 
+    def run_captures(self, steps: int, captures: Sequence[Tuple[int, int, int]]):
+        """Run `steps` steps from step 0 capturing slices on the way:
+        captures = [(step, orientation, slice), ...]; returns (receivers
+        [n_rec, steps], [(pressure [h, w] float32, node bytes [h, w]), ...]),
+        each capture the field after its step.  The copies go to pinned host
+        buffers, asynchronously on the domain's stream."""
+        n = len(captures)
+        X, Y, Z = self.dims
+        shape = lambda o: (Y, X) if o == 0 else ((Z, X) if o == 1 else (Z, Y))
+        st = np.array([c[0] for c in captures], np.int64)
+        ori = np.array([c[1] for c in captures], np.int32)
+        sl = np.array([c[2] for c in captures], np.int64)
+        sizes = [int(np.prod(shape(int(o)))) for o in ori]
+        ptrs = []
+        try:
+            pp = (C.c_void_p * max(n, 1))()
+            qq = (C.c_void_p * max(n, 1))()
+            for i, sz in enumerate(sizes):
+                a, b = C.c_void_p(), C.c_void_p()
+                L.call("pfdtd_host_alloc", C.c_size_t(4 * sz), C.byref(a))
+                ptrs.append(a)
+                L.call("pfdtd_host_alloc", C.c_size_t(sz), C.byref(b))
+                ptrs.append(b)
+                pp[i], qq[i] = a, b
+            out = np.zeros((max(self.n_rec, 0), steps), dtype=arith_dtype(self.precision))
+            L.call("pfdtd_run_captures", self.handle, int(steps), out.ctypes.data, n,
+                   st.ctypes.data_as(C.POINTER(C.c_int64)),
+                   ori.ctypes.data_as(C.POINTER(C.c_int32)),
+                   sl.ctypes.data_as(C.POINTER(C.c_int64)), pp, qq)
+            caps = []
+            for i, o in enumerate(ori):
+                h, w = shape(int(o))
+                p = np.ctypeslib.as_array((C.c_float * sizes[i]).from_address(pp[i])).copy()
+                q = np.ctypeslib.as_array((C.c_uint8 * sizes[i]).from_address(qq[i])).copy()
+                caps.append((p.reshape(h, w), q.reshape(h, w)))
+            return out, caps
+        finally:
+            for a in ptrs:
+                L.load().pfdtd_host_free(a)
+
     def set_temporal_block(self, depth: int) -> None:
         """Steps per update kernel: 0 (one kernel per step) or 2, 3, 4."""
         L.call("pfdtd_set_temporal_block", self.handle, int(depth))

@@ -652,3 +652,59 @@ def test_transparent_source_on_device(gpu, O, input_type, steps, n_ir):
                           grid_ir=h if n_ir else None)
     got = transparent_source(regular, h)
     assert np.array_equal(got, ref)
+
+
+@pytest.mark.parametrize("prec,depth", [("f32", 0), ("f16", 0), ("f32", 2)])
+def test_run_with_slice_captures(gpu, prec, depth):
+    """Slices captured asynchronously during one run equal run(s) followed by
+    capture_slice, and the receivers equal a plain run."""
+    room = rooms.boxes_room((64, 48, 40), n_boxes=4, edge=(5, 12), n_materials=6, seed=12)
+    steps = 163
+    pulse = rooms.gaussian_pulse(steps, 3.0)
+    src = [tuple(p) for p in room.random_air_nodes(2, seed=1)]
+    rec = [tuple(p) for p in room.random_air_nodes(3, seed=2)]
+    caps = [(0, 0, 10), (37, 1, 20), (50, 2, 30), (100, 0, 25), (100, 2, 5), (163, 1, 47)]
+
+    def make():
+        d = Domain(room.dims, prec)
+        d.set_voxels(room.bid, room.mat, centred=False)
+        d.set_materials(room.admittance)
+        d.set_params(default_params())
+        d.set_sources(src, [1, 1], np.stack([pulse, -pulse]))
+        d.set_receivers(rec)
+        d.set_temporal_block(depth)
+        return d
+
+    with make() as d:
+        g, got = d.run_captures(steps, caps)
+    with make() as d:
+        g0, _, _ = d.run(steps)
+    assert np.array_equal(g, g0)
+    for (s, o, sl), (p, q) in zip(caps, got):
+        with make() as d:
+            if s:
+                d.run(s)
+            rp, rq = d.capture_slice(o, sl)
+        assert np.array_equal(p, rp), (s, o, sl)
+        assert np.array_equal(q, rq)
+    assert np.abs(got[3][0]).max() > 0
+
+
+def test_post_filter_matches_scipy(gpu):
+    """Receiver post-processing on the device against scipy's lfilter."""
+    from scipy.signal import lfilter
+    from parallelfdtd_gb300 import postfilter
+    rng = np.random.default_rng(4)
+    x = rng.standard_normal((16, 3000))
+    y = postfilter.fdtd_filter(x, 8000.0, 0.2)
+    from scipy.signal import firwin
+    taps = firwin(200, 8000 * 0.2 / 4000.0, window=("chebwin", 70.0))
+    ref = lfilter(taps, 1.0, x, axis=1)
+    assert np.max(np.abs(y - ref)) <= 1e-12 * np.max(np.abs(ref))
+    z = postfilter.fdtd_post_filter(x, 8000.0, 0.3)
+    t2 = firwin(201, 0.3, window="hamming")
+    a = postfilter.dc_block_coef(5.0, 8000.0)
+    ref2 = lfilter([1.0, -1.0], [1.0, -a], lfilter(t2, 1.0, x, axis=1), axis=1)
+    assert np.max(np.abs(z - ref2)) <= 1e-10 * np.max(np.abs(ref2))
+    f = postfilter.fdtd_filter(x.astype(np.float32), 8000.0, 0.2)
+    assert f.dtype == np.float32 and np.max(np.abs(f - ref)) <= 1e-5 * np.max(np.abs(ref))
