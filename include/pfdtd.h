@@ -375,6 +375,15 @@ int pfdtd_post_filter(const void* x, int64_t n_channels, int64_t n_samples, int 
                       const double* taps, int n_taps, int dc_block, double dc_coef, void* out,
                       int device);
 
+/* Rational resampling of n_channels traces of n_in samples (row-major, float
+ * or double) on the device (the resample step of matlab/testBench.m:204):
+ * out[c][j] = sum_i taps[(j + offset) * down - i * up] * x[c][i], j < n_out,
+ * over the i whose tap index lies in [0, n_taps).  The caller designs the
+ * anti-aliasing taps (scaled by up) and the delay offset.  Host arrays. */
+int pfdtd_resample(const void* x, int64_t n_channels, int64_t n_in, int is_double,
+                   const double* taps, int n_taps, int up, int down, int64_t offset,
+                   int64_t n_out, void* out, int device);
+
 /* Transparent source vector on the device (SimulationParameters.cpp:300-310,
  * which evaluates it per step on the host, O(steps^2) for a whole run):
  * out[n] = samples[n] - sum_{i<n} grid_ir[n-i] * samples[i] in float, in the

@@ -96,6 +96,8 @@ _SIGNATURES = {
     "pfdtd_fetch_receivers": (_i32, [_vp, _vp]),
     "pfdtd_encode_nodes_host": (_i32, [_i32, _vp, _vp, _i64]),
     "pfdtd_transparent_source": (_i32, [_vp, _i64, _vp, _i64, _vp, _i32]),
+    "pfdtd_resample": (_i32, [_vp, _i64, _i64, _i32, C.POINTER(C.c_double), _i32, _i32, _i32,
+                              _i64, _i64, _vp, _i32]),
     "pfdtd_post_filter": (_i32, [_vp, _i64, _i64, _i32, C.POINTER(C.c_double), _i32, _i32,
                                  C.c_double, _vp, _i32]),
     "pfdtd_voxelize": (_i32, [_vp, _i64, _vp, _i64, _vp, C.c_double, _i32,

@@ -691,20 +691,55 @@ def test_run_with_slice_captures(gpu, prec, depth):
 
 
 def test_post_filter_matches_scipy(gpu):
-    """Receiver post-processing on the device against scipy's lfilter."""
-    from scipy.signal import lfilter
-    from parallelfdtd_gb300 import postfilter
+    """Receiver post-processing on the device (python/FDTDfilter.py,
+    matlab/functions/FDTDpostFilter.m) against scipy's lfilter; double
+    within 1e-12 of the largest output, float within 1e-5."""
+    from scipy.signal import firwin, lfilter
+    from parallelfdtd_gb300 import postfilter as pf
     rng = np.random.default_rng(4)
-    x = rng.standard_normal((16, 3000))
-    y = postfilter.fdtd_filter(x, 8000.0, 0.2)
-    from scipy.signal import firwin
+    x = rng.standard_normal((3000, 16))  # [samples, channels], as FDTDfilter.py
+    y = pf.FDTDfilter(x, 8000.0, 48000.0, 0.2)
     taps = firwin(200, 8000 * 0.2 / 4000.0, window=("chebwin", 70.0))
-    ref = lfilter(taps, 1.0, x, axis=1)
-    assert np.max(np.abs(y - ref)) <= 1e-12 * np.max(np.abs(ref))
-    z = postfilter.fdtd_post_filter(x, 8000.0, 0.3)
-    t2 = firwin(201, 0.3, window="hamming")
-    a = postfilter.dc_block_coef(5.0, 8000.0)
-    ref2 = lfilter([1.0, -1.0], [1.0, -a], lfilter(t2, 1.0, x, axis=1), axis=1)
-    assert np.max(np.abs(z - ref2)) <= 1e-10 * np.max(np.abs(ref2))
-    f = postfilter.fdtd_filter(x.astype(np.float32), 8000.0, 0.2)
+    ref = lfilter(taps, 1.0, x, axis=0)
+    assert y.shape == x.shape and np.max(np.abs(y - ref)) <= 1e-12 * np.max(np.abs(ref))
+    a = pf.dcblock(5.0, 8000.0)
+    ref2 = lfilter([1.0, -1.0], [1.0, -a], lfilter(firwin(201, 0.3, window="hamming"), 1.0,
+                                                     x, axis=0), axis=0)
+    for inp in (x, x.T):  # column or row traces: columns out
+        z = pf.FDTDpostFilter(inp, 8000.0, 0.3)
+        assert z.shape == x.shape and np.max(np.abs(z - ref2)) <= 1e-10 * np.max(np.abs(ref2))
+    z1 = pf.FDTDpostFilter(x[:, 3], 8000.0, 0.3)
+    assert np.max(np.abs(z1 - ref2[:, 3])) <= 1e-10 * np.max(np.abs(ref2))
+    f = pf.FDTDfilter(x.astype(np.float32), 8000.0, 48000.0, 0.2)
     assert f.dtype == np.float32 and np.max(np.abs(f - ref)) <= 1e-5 * np.max(np.abs(ref))
+
+
+@pytest.mark.parametrize("p,q,n", [(6, 1, 1000), (48000, 7350, 2001), (3, 4, 999), (1, 5, 400)])
+def test_resample_matches_scipy(gpu, p, q, n):
+    """Polyphase resampling on the device against scipy's resample_poly with
+    the same taps (output alignment and length as MATLAB's resample)."""
+    from scipy.signal import resample_poly
+    from parallelfdtd_gb300 import postfilter as pf
+    rng = np.random.default_rng(p + q)
+    x = rng.standard_normal((n, 3))
+    h = pf.resample_taps(p, q)
+    y = pf.resample(x, p, q)
+    ref = resample_poly(x, p, q, axis=0, window=h)
+    assert y.shape == ref.shape == (-(-n * p // q), 3)
+    assert np.max(np.abs(y - ref)) <= 1e-12 * np.max(np.abs(ref))
+
+
+def test_render_pipeline(gpu):
+    """matlab/testBench.m:203-204 on a simulated response: post-filter, then
+    resample to 48 kHz; equal to the scipy composition."""
+    from scipy.signal import firwin, lfilter, resample_poly
+    from parallelfdtd_gb300 import postfilter as pf
+    fs = 7350
+    rng = np.random.default_rng(9)
+    p = rng.standard_normal((900, 2)) * np.exp(-np.arange(900) / 200.0)[:, None]
+    y = pf.render(p, fs, 0.2, 48000)
+    a = pf.dcblock(5.0, fs)
+    f = lfilter([1.0, -1.0], [1.0, -a], lfilter(firwin(201, 0.2, window="hamming"), 1.0, p,
+                                                  axis=0), axis=0)
+    ref = resample_poly(f, 48000, fs, axis=0, window=pf.resample_taps(48000, fs))
+    assert y.shape == ref.shape and np.max(np.abs(y - ref)) <= 1e-12 * np.max(np.abs(ref))
