@@ -220,28 +220,39 @@ T geometric_factor(int scheme, unsigned pos, T lambda) {
 // beta = lambda * Y * W, W = W16/16 the summed weight of its closed
 // neighbours:
 //   p+ = s * (d1*S1' + d2*S2' + d3*S3' + d4*p - (1 - beta)*p-) / (1 + beta).
-// Canonical evaluation order (shared with the CUDA kernel): offsets visited
-// for dz, dy, dx in -1, 0, 1 (skipping the centre), each added to its class
-// sum in that order; then ((l2 * ((S1/4 + S2/8) + S3/16) + d4*p) - c*p-) * a.
+// Canonical evaluation order (shared with the CUDA kernels), built from
+// in-plane sums so that a z-marching kernel can compute each plane's sums
+// once and use them for the three planes next to it.  With m(dz, dy, dx) the
+// neighbour values after the closure substitution and, per plane dz,
+//   c0(dz) = m(dz, 0, 0)
+//   c1(dz) = ((m(dz,-1,0) + m(dz,0,-1)) + m(dz,0,1)) + m(dz,1,0)
+//   c2(dz) = ((m(dz,-1,-1) + m(dz,-1,1)) + m(dz,1,-1)) + m(dz,1,1),
+// S1 = (c1(0) + c0(-1)) + c0(1), S2 = (c2(0) + c1(-1)) + c1(1),
+// S3 = c2(-1) + c2(1); then ((l2 * ((S1/4 + S2/8) + S3/16) + d4*p) - c*p-) * a.
+// The closed mask's bit k is the k-th offset in (dz, dy, dx) row-major order
+// with the centre left out.
 template <typename T, typename St>
 T iwb_node(const St* P, int64_t N, int64_t c, int64_t X, int64_t XY, uint32_t mask, T pp, T a,
            T cc, T l2) {
   const T p = (T)to_float(P[c]);
-  T s1 = 0, s2 = 0, s3 = 0;
-  bool f1 = true, f2 = true, f3 = true;
+  T m[3][3][3];
   int k = 0;
   for (int dz = -1; dz <= 1; ++dz)
     for (int dy = -1; dy <= 1; ++dy)
       for (int dx = -1; dx <= 1; ++dx) {
-        const int n = (dx != 0) + (dy != 0) + (dz != 0);
-        if (n == 0) continue;
-        const int64_t i = c + dz * XY + dy * X + dx;
-        const T v = ((mask >> k) & 1u) ? p : (T)to_float(P[i]);
-        ++k;
-        if (n == 1) { s1 = f1 ? v : s1 + v; f1 = false; }
-        else if (n == 2) { s2 = f2 ? v : s2 + v; f2 = false; }
-        else { s3 = f3 ? v : s3 + v; f3 = false; }
+        T v = p;
+        if (dx != 0 || dy != 0 || dz != 0) {
+          const int64_t i = c + dz * XY + dy * X + dx;
+          if (!((mask >> k) & 1u)) v = (T)to_float(P[i]);
+          ++k;
+        }
+        m[dz + 1][dy + 1][dx + 1] = v;
       }
+  auto c1 = [&](int z) { return ((m[z][0][1] + m[z][1][0]) + m[z][1][2]) + m[z][2][1]; };
+  auto c2 = [&](int z) { return ((m[z][0][0] + m[z][0][2]) + m[z][2][0]) + m[z][2][2]; };
+  const T s1 = (c1(1) + m[0][1][1]) + m[2][1][1];
+  const T s2 = (c2(1) + c1(0)) + c1(2);
+  const T s3 = c2(0) + c2(2);
   const T sw = l2 * (s1 * (T)0.25 + s2 * (T)0.125 + s3 * (T)0.0625);
   const T d4 = (T)2 - (T)3.5 * l2;
   return a * ((sw + d4 * p) - cc * pp);

@@ -46,6 +46,32 @@ template <> struct Rn<double> {
   static __device__ __forceinline__ double sub(double a, double b) { return __dsub_rn(a, b); }
 };
 
+// IWB 27-point sums of one node from its 3 x 3 x 3 neighbourhood
+// m[dz+1][dy+1][dx+1] after the closure substitution (centre unused), in the
+// scheme's canonical order, built from in-plane sums so that a z-march can
+// share them between planes:
+//   c1(dz) = ((m(dz,-1,0) + m(dz,0,-1)) + m(dz,0,1)) + m(dz,1,0)
+//   c2(dz) = ((m(dz,-1,-1) + m(dz,-1,1)) + m(dz,1,-1)) + m(dz,1,1)
+//   S1 = (c1(0) + m(-1,0,0)) + m(1,0,0),  S2 = (c2(0) + c1(-1)) + c1(1),
+//   S3 = c2(-1) + c2(1).
+template <typename A>
+__device__ __forceinline__ A iwb_c1(const A (&q)[3][3]) {
+  using R = Rn<A>;
+  return R::add(R::add(R::add(q[0][1], q[1][0]), q[1][2]), q[2][1]);
+}
+template <typename A>
+__device__ __forceinline__ A iwb_c2(const A (&q)[3][3]) {
+  using R = Rn<A>;
+  return R::add(R::add(R::add(q[0][0], q[0][2]), q[2][0]), q[2][2]);
+}
+template <typename A>
+__device__ __forceinline__ void iwb_sums(const A (&m)[3][3][3], A& s1, A& s2, A& s3) {
+  using R = Rn<A>;
+  s1 = R::add(R::add(iwb_c1(m[1]), m[0][1][1]), m[2][1][1]);
+  s2 = R::add(R::add(iwb_c2(m[1]), iwb_c1(m[0])), iwb_c1(m[2]));
+  s3 = R::add(iwb_c2(m[0]), iwb_c2(m[2]));
+}
+
 // Storage type -> arithmetic type.
 template <typename S> struct Store;
 template <> struct Store<float> {
@@ -91,7 +117,8 @@ struct TmaState {
   CUtensorMap halo[4];
   CUtensorMap tile[4];
   CUtensorMap cls;
-  int64_t key[5] = {0, 0, 0, 0, 0};
+  CUtensorMap mask;  // IWB closed-neighbour masks (4 bytes per node)
+  int64_t key[6] = {0, 0, 0, 0, 0, 0};
   bool ready = false;
   bool attr_set[2][2][2] = {{{false, false}, {false, false}}, {{false, false}, {false, false}}};
 };

@@ -138,20 +138,20 @@ __global__ void k_dif_update(const int64_t* __restrict__ list, int64_t n, int ks
     } else {
       // IWB: closed neighbours (mask bits, canonical order) contribute p
       const uint32_t mk = iwb_mask[node];
-      A f1 = (A)0, f2 = (A)0, f3 = (A)0;
-      bool n1 = true, n2 = true, n3 = true;
+      A m[3][3][3];
       int kk = 0;
       for (int dz = -1; dz <= 1; ++dz)
         for (int dy = -1; dy <= 1; ++dy)
           for (int dx = -1; dx <= 1; ++dx) {
-            const int nn = (dx != 0) + (dy != 0) + (dz != 0);
-            if (nn == 0) continue;
-            const A v = ((mk >> kk) & 1u) ? p : Sto::load(P[i + dz * XY + dy * X + dx * ks]);
-            ++kk;
-            if (nn == 1) { f1 = n1 ? v : R::add(f1, v); n1 = false; }
-            else if (nn == 2) { f2 = n2 ? v : R::add(f2, v); n2 = false; }
-            else { f3 = n3 ? v : R::add(f3, v); n3 = false; }
+            A v = p;
+            if (dx != 0 || dy != 0 || dz != 0) {
+              if (!((mk >> kk) & 1u)) v = Sto::load(P[i + dz * XY + dy * X + dx * ks]);
+              ++kk;
+            }
+            m[dz + 1][dy + 1][dx + 1] = v;
           }
+      A f1, f2, f3;
+      iwb_sums(m, f1, f2, f3);
       const A sw = R::mul(l2, R::add(R::add(R::mul(f1, (A)0.25), R::mul(f2, (A)0.125)),
                                      R::mul(f3, (A)0.0625)));
       num = R::sub(R::sub(R::add(sw, R::mul(b, p)), R::mul(cc, pp)), R::mul(g2, s1));

@@ -101,8 +101,7 @@ k_update_zmarch(const C* __restrict__ cls, const S* __restrict__ P, S* __restric
 // the read-only cache.  Boundary closure (finite volume on the voxel grid): a
 // neighbour whose bit is set in the node's closed mask (k_iwb_geometry)
 // contributes the node's own value.  Sums follow the canonical order of the
-// oracle: offsets for dz, dy, dx in -1, 0, 1 into the face, edge and corner
-// sums.
+// oracle (iwb_sums: in-plane sums of each plane, then combined).
 template <typename S, typename C>
 __global__ void __launch_bounds__(kBX * kBY)
 k_update_iwb(const C* __restrict__ cls, const uint32_t* __restrict__ mask,
@@ -155,21 +154,8 @@ k_update_iwb(const C* __restrict__ cls, const uint32_t* __restrict__ mask,
             ++k;
           }
     }
-    A s1 = (A)0, s2 = (A)0, s3 = (A)0;
-    bool f1 = true, f2 = true, f3 = true;
-#pragma unroll
-    for (int a = 0; a < 3; ++a)
-#pragma unroll
-      for (int b = 0; b < 3; ++b)
-#pragma unroll
-        for (int e = 0; e < 3; ++e) {
-          const int n = (a != 1) + (b != 1) + (e != 1);
-          if (n == 0) continue;
-          const A w = m[a][b][e];
-          if (n == 1) { s1 = f1 ? w : R::add(s1, w); f1 = false; }
-          else if (n == 2) { s2 = f2 ? w : R::add(s2, w); f2 = false; }
-          else { s3 = f3 ? w : R::add(s3, w); f3 = false; }
-        }
+    A s1, s2, s3;
+    iwb_sums(m, s1, s2, s3);
     const A sw = R::mul(l2, R::add(R::add(R::mul(s1, (A)0.25), R::mul(s2, (A)0.125)),
                                    R::mul(s3, (A)0.0625)));
     const A out = R::mul(ca, R::sub(R::add(sw, R::mul(cb, v[1][1][1])), R::mul(cc, pp)));

@@ -40,10 +40,13 @@ template <typename A> struct alignas(4 * sizeof(A)) PackedCoef { A a, b, c; uint
 __host__ __device__ constexpr int round128(int b) { return (b + 127) / 128 * 128; }
 
 // Tile shape: TX nodes along x (box inner extent TX + 2H <= 256), TY rows,
-// NS pipeline stages.
-template <typename S, typename C, int TX_, int TY_, int NS_, bool XHALO_ = true>
+// NS pipeline stages; MASK: each stage also carries the plane's IWB
+// closed-neighbour masks (4 bytes per node); MINB: CTAs per SM the register
+// allocation must allow.
+template <typename S, typename C, int TX_, int TY_, int NS_, bool XHALO_ = true, bool MASK_ = false,
+          int MINB_ = 1>
 struct Layout {
-  static constexpr int TX = TX_, TY = TY_, NS = NS_;
+  static constexpr int TX = TX_, TY = TY_, NS = NS_, MINB = MINB_;
   // With XHALO the box carries a 16-byte x halo on both sides; without it the
   // box is exactly TX wide (up to 256) and the threads at the tile's x edges
   // read their outside neighbour from global memory (an L2 hit: the
@@ -57,7 +60,10 @@ struct Layout {
   static constexpr int P_OFF = 0;
   static constexpr int PP_OFF = round128(P_BYTES);
   static constexpr int CL_OFF = PP_OFF + round128(PP_BYTES);
-  static constexpr int STAGE = CL_OFF + round128(CL_BYTES);
+  static constexpr bool MASK = MASK_;
+  static constexpr int MK_BYTES = MASK ? TX * TY * 4 : 0;
+  static constexpr int MK_OFF = CL_OFF + round128(CL_BYTES);
+  static constexpr int STAGE = MK_OFF + round128(MK_BYTES);
   static constexpr int BAR_OFF = STAGE * NS;
   // full + empty barriers + abort flag, plus 128 B to align the dynamic base
   static constexpr int SMEM = BAR_OFF + 2 * NS * 8 + 16 + 128;
@@ -183,112 +189,69 @@ __device__ __forceinline__ void stg4(double* p, const double (&v)[4]) {
   reinterpret_cast<double2*>(p)[1] = make_double2(v[2], v[3]);
 }
 
-// IWB 27-point update of a consumer thread's 4 consecutive x nodes (no
-// counterpart in the reference).  The 3 planes x 3 rows x 6 values around
-// the nodes come from the stage ring: the box's 16-byte x halo and one-row y
-// halo hold every edge and corner neighbour.  At the grid's x edges the
-// neighbour x-1 (x = 0) or x+4 (x+4 = X) is read from global memory at its
-// flat index, so the wrap across rows matches k_update_iwb (stencil.cu),
-// whose boundary closure (closed neighbours contribute the node's value),
-// canonical summation order (dz, dy, dx) and rounding this follows
-// operation for operation.
-template <typename S, typename C, typename Lay>
-__device__ __forceinline__ void iwb_consumer(const S* Pm, const S* Pc, const S* Pn, const S* Pq,
-                                             const C* Cl, const S* __restrict__ P,
-                                             S* __restrict__ Pp, int64_t idx, int si, int ci,
-                                             int x, int X, int64_t XY,
-                                             const PackedCoef<float>* stab,
-                                             const ClassTab<float>& tab, uint4 mk4, float l2) {
-  using R = Rn<float>;
+// IWB 27-point update (no counterpart in the reference), a consumer thread's
+// 4 consecutive x nodes per plane.  The rows around the nodes come from the
+// stage ring: the box's 16-byte x halo and one-row y halo hold every edge and
+// corner neighbour.  The scheme's canonical sums (iwb_sums) are built from
+// in-plane sums, so a thread computes the raw sums of each new plane z+1 once
+// and combines them with those of planes z-1 and z carried in registers; a
+// node with a closed neighbour recomputes its three planes with the closure
+// substitution.  Closure, order and rounding follow k_update_iwb
+// (stencil.cu) operation for operation.
+// Canonical index (0..25) of neighbour (dz, dy, dx) = (a-1, b-1, c-1) in the
+// closed-neighbour mask: (a, b, c) in row-major order with the centre left out.
+__host__ __device__ constexpr int iwb_bit(int a, int b, int c) {
+  return a * 9 + b * 3 + c - (a * 9 + b * 3 + c > 13 ? 1 : 0);
+}
+
+// In-plane sums of one plane (dz = a-1) for a thread's 4 nodes: the centre
+// c0, the 4 face-adjacent in-plane neighbours c1 and the 4 in-plane diagonals
+// c2, in the order of iwb_c1 / iwb_c2.  The plane's rows y-1, y, y+1, x-1 ..
+// x+4, come from the stage (pl, si) and, at the grid's x edges, from global
+// memory at their flat index (g: the flat index of (plane, y, x)), so the wrap
+// across rows matches k_update_iwb.  SUBST: neighbours whose bit is set in the
+// node's closed mask contribute the node's own value p[e].
+template <bool SUBST, int a, typename S, typename Lay>
+__device__ __forceinline__ void iwb_plane_sums(const S* pl, int si, const S* __restrict__ P,
+                                               int64_t g, int x, int X,
+                                               const uint32_t (&mk)[kVec],
+                                               const float (&p)[kVec], float (&c0)[kVec],
+                                               float (&c1)[kVec], float (&c2)[kVec]) {
   using St = Store<S>;
   constexpr int PW = Lay::PW;
-  constexpr bool kSmemTab = sizeof(C) == 1;
-  const S* pl[3] = {Pm, Pc, Pn};
-  // v[plane][row][i]: plane dz+1, row dy+1, i = 0 for x-1, 1..4 for x..x+3, 5 for x+4
-  float v[3][3][6];
+  float w[3][6];
 #pragma unroll
-  for (int a = 0; a < 3; ++a)
+  for (int b = 0; b < 3; ++b) {
+    const S* row = pl + si + (b - 1) * PW;
+    const V4<S> mid = lds4(row);
 #pragma unroll
-    for (int b = 0; b < 3; ++b) {
-      const S* row = pl[a] + si + (b - 1) * PW;
-      const V4<S> mid = lds4(row);
-#pragma unroll
-      for (int e = 0; e < 4; ++e) v[a][b][e + 1] = St::load(mid.v[e]);
-      v[a][b][0] = St::load(row[-1]);
-      v[a][b][5] = St::load(row[kVec]);
-    }
+    for (int e = 0; e < 4; ++e) w[b][e + 1] = St::load(mid.v[e]);
+    w[b][0] = St::load(row[-1]);
+    w[b][5] = St::load(row[kVec]);
+  }
   if (x == 0 || x + kVec == X) {  // grid x edge: the flat neighbour wraps to the next row
 #pragma unroll
-    for (int a = 0; a < 3; ++a)
-#pragma unroll
-      for (int b = 0; b < 3; ++b) {
-        const int64_t g = idx + (int64_t)(a - 1) * XY + (int64_t)(b - 1) * X;
-        if (x == 0) v[a][b][0] = St::load(P[g - 1]);
-        if (x + kVec == X) v[a][b][5] = St::load(P[g + kVec]);
-      }
+    for (int b = 0; b < 3; ++b) {
+      const int64_t gr = g + (int64_t)(b - 1) * X;
+      if (x == 0) w[b][0] = St::load(P[gr - 1]);
+      if (x + kVec == X) w[b][5] = St::load(P[gr + kVec]);
+    }
   }
-  const V4<S> vpp = lds4(Pq + ci);
-  const uint32_t mks[kVec] = {mk4.x, mk4.y, mk4.z, mk4.w};
-  unsigned cid[kVec];
-  if (sizeof(C) == 1) {
-    const uint32_t w = *reinterpret_cast<const uint32_t*>(Cl + ci);
-#pragma unroll
-    for (int e = 0; e < kVec; ++e) cid[e] = (w >> (8 * e)) & 0xFFu;
-  } else {
-    const uint2 w = *reinterpret_cast<const uint2*>(Cl + ci);
-    cid[0] = w.x & 0xFFFFu; cid[1] = w.x >> 16; cid[2] = w.y & 0xFFFFu; cid[3] = w.y >> 16;
-  }
-  S res[kVec];
 #pragma unroll
   for (int e = 0; e < kVec; ++e) {
-    PackedCoef<float> k;
-    if (kSmemTab) k = stab[cid[e]];
-    else
-      k = PackedCoef<float>{__ldg(tab.a + cid[e]), __ldg(tab.b + cid[e]), __ldg(tab.c + cid[e]),
-                            __ldg(tab.pos + cid[e])};
-    float m[3][3][3];
+    float q[3][3];
 #pragma unroll
-    for (int a = 0; a < 3; ++a)
+    for (int b = 0; b < 3; ++b)
 #pragma unroll
-      for (int b = 0; b < 3; ++b)
-#pragma unroll
-        for (int c = 0; c < 3; ++c) m[a][b][c] = v[a][b][e + c];
-    const uint32_t mk = mks[e];
-    if (mk) {
-      int kk = 0;
-#pragma unroll
-      for (int a = 0; a < 3; ++a)
-#pragma unroll
-        for (int b = 0; b < 3; ++b)
-#pragma unroll
-          for (int c = 0; c < 3; ++c) {
-            if (a == 1 && b == 1 && c == 1) continue;
-            if ((mk >> kk) & 1u) m[a][b][c] = v[1][1][e + 1];
-            ++kk;
-          }
-    }
-    float s1 = 0.f, s2 = 0.f, s3 = 0.f;
-    bool f1 = true, f2 = true, f3 = true;
-#pragma unroll
-    for (int a = 0; a < 3; ++a)
-#pragma unroll
-      for (int b = 0; b < 3; ++b)
-#pragma unroll
-        for (int c = 0; c < 3; ++c) {
-          const int n = (a != 1) + (b != 1) + (c != 1);
-          if (n == 0) continue;
-          const float w = m[a][b][c];
-          if (n == 1) { s1 = f1 ? w : R::add(s1, w); f1 = false; }
-          else if (n == 2) { s2 = f2 ? w : R::add(s2, w); f2 = false; }
-          else { s3 = f3 ? w : R::add(s3, w); f3 = false; }
-        }
-    const float sw = R::mul(
-        l2, R::add(R::add(R::mul(s1, 0.25f), R::mul(s2, 0.125f)), R::mul(s3, 0.0625f)));
-    const float out = R::mul(k.a, R::sub(R::add(sw, R::mul(k.b, v[1][1][e + 1])),
-                                         R::mul(k.c, St::load(vpp.v[e]))));
-    res[e] = St::store(out);
+      for (int c = 0; c < 3; ++c) {
+        q[b][c] = w[b][e + c];
+        if (SUBST && !(a == 1 && b == 1 && c == 1) && ((mk[e] >> iwb_bit(a, b, c)) & 1u))
+          q[b][c] = p[e];
+      }
+    c0[e] = q[1][1];
+    c1[e] = iwb_c1(q);
+    c2[e] = iwb_c2(q);
   }
-  stg4(Pp + idx, res);
 }
 
 // Producer of the stage ring (one thread): stage k receives the P^n plane
@@ -299,7 +262,8 @@ __device__ __forceinline__ void iwb_consumer(const S* Pm, const S* Pc, const S* 
 template <typename Lay>
 __device__ __forceinline__ void tma_producer(const CUtensorMap* map_cur,
                                              const CUtensorMap* map_past,
-                                             const CUtensorMap* map_cls, unsigned char* smem,
+                                             const CUtensorMap* map_cls,
+                                             const CUtensorMap* map_mask, unsigned char* smem,
                                              uint32_t bar_full, uint32_t bar_empty,
                                              volatile int* abort_flag, int x0, int y0, int z0,
                                              int Y, int K, int kshift, int* err) {
@@ -319,13 +283,15 @@ __device__ __forceinline__ void tma_producer(const CUtensorMap* map_cur,
     const uint32_t bar = bar_full + 8 * slot;
     const int zp = z0 - 1 + k;
     uint32_t bytes = Lay::P_BYTES;
-    if (k >= 2) bytes += Lay::PP_BYTES + (Lay::CL_BYTES >> kshift);
+    if (k >= 2) bytes += Lay::PP_BYTES + (Lay::CL_BYTES >> kshift) + Lay::MK_BYTES;
     mbar_expect_tx(bar, bytes);
     tma_load_2d(smem_u32(st + Lay::P_OFF), map_cur, x0 - H, zp * Y + y0 - 1, bar);
     if (k >= 2) {
       const int zc_ = z0 + k - 2;
       tma_load_2d(smem_u32(st + Lay::PP_OFF), map_past, x0, zc_ * Y + y0, bar);
       tma_load_2d(smem_u32(st + Lay::CL_OFF), map_cls, x0 >> kshift, zc_ * Y + y0, bar);
+      if constexpr (Lay::MASK)
+        tma_load_2d(smem_u32(st + Lay::MK_OFF), map_mask, x0, zc_ * Y + y0, bar);
     }
     issued = k + 1;
   }
@@ -339,12 +305,12 @@ __device__ __forceinline__ void tma_producer(const CUtensorMap* map_cur,
 // 4 fields of one node, the x neighbours are K elements away and the class
 // ids (one per node) come in a box K times narrower.
 template <typename S, typename C, int SCHEME, typename Lay, bool BATCHED = false>
-__global__ void __launch_bounds__(Lay::THREADS)
+__global__ void __launch_bounds__(Lay::THREADS, Lay::MINB)
 k_update_tma(const __grid_constant__ CUtensorMap map_cur, const __grid_constant__ CUtensorMap map_past,
-             const __grid_constant__ CUtensorMap map_cls, const S* __restrict__ P,
+             const __grid_constant__ CUtensorMap map_cls,
+             const __grid_constant__ CUtensorMap map_mask, const S* __restrict__ P,
              S* __restrict__ Pp, ClassTab<typename Store<S>::A> tab, int X, int Y, int64_t XY,
-             int z_last, int zc, typename Store<S>::A l2, int* __restrict__ err, int kshift = 0,
-             const uint32_t* __restrict__ iwb_mask = nullptr) {
+             int z_last, int zc, typename Store<S>::A l2, int* __restrict__ err, int kshift = 0) {
   using A = typename Store<S>::A;
   using R = Rn<A>;
   using St = Store<S>;
@@ -388,8 +354,8 @@ k_update_tma(const __grid_constant__ CUtensorMap map_cur, const __grid_constant_
 
   if (warp == kConsumerWarps) {
     if (lane == 0)
-      tma_producer<Lay>(&map_cur, &map_past, &map_cls, smem, bar_full, bar_empty, abort_flag, x0,
-                        y0, z0, Y, K, kshift, err);
+      tma_producer<Lay>(&map_cur, &map_past, &map_cls, &map_mask, smem, bar_full, bar_empty,
+                        abort_flag, x0, y0, z0, Y, K, kshift, err);
     return;
   }
 
@@ -404,11 +370,19 @@ k_update_tma(const __grid_constant__ CUtensorMap map_cur, const __grid_constant_
   const bool active = (x < X) && (y < Y);  // X is a multiple of 4: all 4 or none
   const int si = (ly + 1) * PW + lx + H;   // centre of the thread's first node
   bool ok = mbar_wait(bar_full, 0) && mbar_wait(bar_full + 8, 0);
-  // IWB: the closed-neighbour masks of the thread's 4 nodes, loaded one plane
-  // ahead of their use so the global read overlaps a plane of work
-  const int64_t node0 = (int64_t)z0 * XY + (int64_t)y * X + x;
-  uint4 mk_next = make_uint4(0, 0, 0, 0);
-  if (SCHEME == 3 && active) mk_next = __ldg(reinterpret_cast<const uint4*>(iwb_mask + node0));
+  // IWB: raw in-plane sums of planes z-1 (m) and z (c) carried along the
+  // z-march; each plane's sums are computed once and used for three planes.
+  float cm0[kVec], cm1[kVec], cm2[kVec], cc0[kVec], cc1[kVec], cc2[kVec];
+  if constexpr (SCHEME == 3) {
+    if (ok && active) {
+      const uint32_t no_mask[kVec] = {0u, 0u, 0u, 0u};
+      const int64_t g0 = (int64_t)(z0 - 1) * XY + (int64_t)y * X + x;
+      iwb_plane_sums<false, 0, S, Lay>((const S*)(smem + Lay::P_OFF), si, P, g0, x, X, no_mask,
+                                       cm0, cm0, cm1, cm2);
+      iwb_plane_sums<false, 0, S, Lay>((const S*)(smem + Lay::STAGE + Lay::P_OFF), si, P,
+                                       g0 + XY, x, X, no_mask, cc0, cc0, cc1, cc2);
+    }
+  }
   for (int j = 0; j < nplanes && ok; ++j) {
     const int sm = j % NS, sc_ = (j + 1) % NS, sp_ = (j + 2) % NS;
     if (!mbar_wait(bar_full + 8 * sp_, (uint32_t)(((j + 2) / NS) & 1))) {
@@ -416,18 +390,83 @@ k_update_tma(const __grid_constant__ CUtensorMap map_cur, const __grid_constant_
       break;
     }
     if constexpr (SCHEME == 3) {
-      const uint4 mk_cur = mk_next;
-      if (active && j + 1 < nplanes)
-        mk_next = __ldg(reinterpret_cast<const uint4*>(iwb_mask + node0 + (int64_t)(j + 1) * XY));
+      static_assert(Lay::MASK, "IWB tiles carry the closed-neighbour masks");
       if (active) {
-        const S* Pm = (const S*)(smem + sm * Lay::STAGE + Lay::P_OFF);
-        const S* Pc = (const S*)(smem + sc_ * Lay::STAGE + Lay::P_OFF);
-        const S* Pn = (const S*)(smem + sp_ * Lay::STAGE + Lay::P_OFF);
-        const S* Pq = (const S*)(smem + sp_ * Lay::STAGE + Lay::PP_OFF);
-        const C* Cl = (const C*)(smem + sp_ * Lay::STAGE + Lay::CL_OFF);
+        using R = Rn<float>;
+        using St = Store<S>;
+        const int ci = ly * kTX + lx;
         const int64_t idx = (int64_t)(z0 + j) * XY + (int64_t)y * X + x;
-        iwb_consumer<S, C, Lay>(Pm, Pc, Pn, Pq, Cl, P, Pp, idx, si, ly * kTX + lx, x, X, XY,
-                                stab, tab, mk_cur, (float)l2);
+        const S* Pn = (const S*)(smem + sp_ * Lay::STAGE + Lay::P_OFF);
+        const uint32_t no_mask[kVec] = {0u, 0u, 0u, 0u};
+        // raw sums of plane z+1
+        float n0[kVec], n1[kVec], n2[kVec];
+        iwb_plane_sums<false, 2, S, Lay>(Pn, si, P, idx + XY, x, X, no_mask, cc0, n0, n1, n2);
+        // the closed-neighbour masks of the thread's 4 nodes (stage of plane z)
+        const uint4 mk4 = *reinterpret_cast<const uint4*>(smem + sp_ * Lay::STAGE + Lay::MK_OFF +
+                                                          4 * ci);
+        float s1[kVec], s2[kVec], s3[kVec];
+        if ((mk4.x | mk4.y | mk4.z | mk4.w) != 0u) {
+          // next to a closed neighbour (walls, obstacle surfaces): the sums of
+          // this node's substituted neighbourhood, plane by plane
+          const uint32_t mk[kVec] = {mk4.x, mk4.y, mk4.z, mk4.w};
+          const S* Pm = (const S*)(smem + sm * Lay::STAGE + Lay::P_OFF);
+          const S* Pc = (const S*)(smem + sc_ * Lay::STAGE + Lay::P_OFF);
+          float a0[kVec], a1[kVec], a2[kVec], b0[kVec], b1[kVec], b2[kVec];
+          iwb_plane_sums<true, 0, S, Lay>(Pm, si, P, idx - XY, x, X, mk, cc0, a0, a1, a2);
+          iwb_plane_sums<true, 1, S, Lay>(Pc, si, P, idx, x, X, mk, cc0, b0, b1, b2);
+#pragma unroll
+          for (int e = 0; e < kVec; ++e) {
+            s1[e] = R::add(b1[e], a0[e]);
+            s2[e] = R::add(b2[e], a1[e]);
+            s3[e] = a2[e];
+          }
+          iwb_plane_sums<true, 2, S, Lay>(Pn, si, P, idx + XY, x, X, mk, cc0, a0, a1, a2);
+#pragma unroll
+          for (int e = 0; e < kVec; ++e) {
+            s1[e] = R::add(s1[e], a0[e]);
+            s2[e] = R::add(s2[e], a1[e]);
+            s3[e] = R::add(s3[e], a2[e]);
+          }
+        } else {
+#pragma unroll
+          for (int e = 0; e < kVec; ++e) {
+            s1[e] = R::add(R::add(cc1[e], cm0[e]), n0[e]);
+            s2[e] = R::add(R::add(cc2[e], cm1[e]), n1[e]);
+            s3[e] = R::add(cm2[e], n2[e]);
+          }
+        }
+        const C* Cl = (const C*)(smem + sp_ * Lay::STAGE + Lay::CL_OFF);
+        unsigned cid[kVec];
+        if (sizeof(C) == 1) {
+          const uint32_t w = *reinterpret_cast<const uint32_t*>(Cl + ci);
+#pragma unroll
+          for (int e = 0; e < kVec; ++e) cid[e] = (w >> (8 * e)) & 0xFFu;
+        } else {
+          const uint2 w = *reinterpret_cast<const uint2*>(Cl + ci);
+          cid[0] = w.x & 0xFFFFu; cid[1] = w.x >> 16; cid[2] = w.y & 0xFFFFu; cid[3] = w.y >> 16;
+        }
+        const V4<S> vpp = lds4((const S*)(smem + sp_ * Lay::STAGE + Lay::PP_OFF) + ci);
+        S res[kVec];
+#pragma unroll
+        for (int e = 0; e < kVec; ++e) {
+          PackedCoef<A> k;
+          if (kSmemTab) k = stab[cid[e]];
+          else
+            k = PackedCoef<A>{__ldg(tab.a + cid[e]), __ldg(tab.b + cid[e]),
+                              __ldg(tab.c + cid[e]), __ldg(tab.pos + cid[e])};
+          const float sw = R::mul((float)l2, R::add(R::add(R::mul(s1[e], 0.25f),
+                                                           R::mul(s2[e], 0.125f)),
+                                                    R::mul(s3[e], 0.0625f)));
+          const float out = R::mul(k.a, R::sub(R::add(sw, R::mul(k.b, cc0[e])),
+                                               R::mul(k.c, St::load(vpp.v[e]))));
+          res[e] = St::store(out);
+        }
+        stg4(Pp + idx, res);
+#pragma unroll
+        for (int e = 0; e < kVec; ++e) {
+          cm0[e] = cc0[e]; cm1[e] = cc1[e]; cm2[e] = cc2[e];
+          cc0[e] = n0[e]; cc1[e] = n1[e]; cc2[e] = n2[e];
+        }
       }
     } else if (active) {
       const S* Pm = (const S*)(smem + sm * Lay::STAGE + Lay::P_OFF);
@@ -573,9 +612,10 @@ int launch_tma_t(pfdtd_domain* d, const void* cur, void* past, cudaStream_t s) {
     if (d->field_base[f] && past == d->field(f)) past_i = f;
   }
   if (cur_i < 0 || past_i < 0) return fail(PFDTD_ERR_ARG, "update fields are not domain buffers");
-  const int64_t key[5] = {(int64_t)(intptr_t)d->d_cls, d->cls_bytes, d->precision * 100 + d->K,
+  const int64_t key[6] = {(int64_t)(intptr_t)d->d_cls, d->cls_bytes, d->precision * 100 + d->K,
                           (int64_t)Lay::TX * 10000 + Lay::TY * 10 + (Lay::XHALO ? 1 : 0),
-                          (int64_t)(intptr_t)d->field_base[2]};
+                          (int64_t)(intptr_t)d->field_base[2],
+                          Lay::MASK ? (int64_t)(intptr_t)d->d_iwb_mask : 0};
   if (!ts.ready || std::memcmp(key, ts.key, sizeof(key)) != 0) {
     const CUtensorMapDataType dt = TmaType<S>::value;
     const CUtensorMapDataType ct =
@@ -588,23 +628,37 @@ int launch_tma_t(pfdtd_domain* d, const void* cur, void* past, cudaStream_t s) {
       ok = ok && make_map(&ts.tile[f], dt, sizeof(S), d->field(f), XE, rows, kTX, Lay::TY);
     }
     ok = ok && make_map(&ts.cls, ct, sizeof(C), d->d_cls, d->X, rows, kTX >> d->kshift, Lay::TY);
+    if (Lay::MASK) {
+      if (!d->d_iwb_mask) return fail(PFDTD_ERR_STATE, "IWB masks not built");
+      ok = ok && make_map(&ts.mask, CU_TENSOR_MAP_DATA_TYPE_UINT32, 4, d->d_iwb_mask, d->X, rows,
+                          kTX, Lay::TY);
+    }
     if (!ok) return fail(PFDTD_ERR_UNSUPPORTED, "tensor map encoding failed");
     std::memcpy(ts.key, key, sizeof(key));
     ts.ready = true;
   }
   // the shared-memory opt-in, once per instantiation and device
+  // (IWB: and its resident CTAs per SM, which registers limit as well)
   static bool attr_done[64] = {};
+  static int occupancy[64] = {};
   if (d->device >= 64) return fail(PFDTD_ERR_UNSUPPORTED, "device index above 63");
   if (!attr_done[d->device]) {
     PFDTD_CK(cudaFuncSetAttribute(k_update_tma<S, C, SCHEME, Lay, BATCHED>,
                                   cudaFuncAttributeMaxDynamicSharedMemorySize, Lay::SMEM));
+    if (SCHEME == 3)
+      PFDTD_CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(
+          &occupancy[d->device], k_update_tma<S, C, SCHEME, Lay, BATCHED>, Lay::THREADS,
+          Lay::SMEM));
     attr_done[d->device] = true;
   }
   const int gx = (int)((XE + kTX - 1) / kTX);
   const int gy = (int)((d->Y + Lay::TY - 1) / Lay::TY);
   // z-chunks: several per tile so that the grid fills the machine in whole
   // waves of (SMs x resident CTAs), each chunk at least 16 planes long.
-  const int64_t per_sm = std::max<int64_t>(1, (228 * 1024) / (Lay::SMEM + 1024 + 8192));
+  const int64_t per_sm =
+      occupancy[d->device] > 0
+          ? occupancy[d->device]
+          : std::max<int64_t>(1, (228 * 1024) / (Lay::SMEM + 1024 + 8192));
   const int64_t resident = (int64_t)d->sm_count * per_sm;
   const int64_t tiles = (int64_t)gx * gy;
   int64_t best_c = 1;
@@ -625,9 +679,9 @@ int launch_tma_t(pfdtd_domain* d, const void* cur, void* past, cudaStream_t s) {
                   (const A*)(tb + 2 * as * d->n_classes),
                   (const uint32_t*)(tb + 3 * as * d->n_classes), d->n_classes};
   k_update_tma<S, C, SCHEME, Lay, BATCHED><<<dim3(gx, gy, gz), Lay::THREADS, Lay::SMEM, s>>>(
-      ts.halo[cur_i], ts.tile[past_i], ts.cls, (const S*)cur, (S*)past, tab, (int)XE,
-      (int)d->Y, d->XY * d->K, (int)(d->Z - 1), (int)zc, (A)d->params[1], d->d_err, d->kshift,
-      d->d_iwb_mask);
+      ts.halo[cur_i], ts.tile[past_i], ts.cls, Lay::MASK ? ts.mask : ts.cls, (const S*)cur,
+      (S*)past, tab, (int)XE, (int)d->Y, d->XY * d->K, (int)(d->Z - 1), (int)zc,
+      (A)d->params[1], d->d_err, d->kshift);
   count_launch();
   PFDTD_CK(cudaGetLastError());
   return PFDTD_OK;
@@ -735,26 +789,29 @@ int launch_tma_s<double>(pfdtd_domain* d, const void* cur, void* past, cudaStrea
 }
 
 // IWB on the stage ring: FP32, FP16 and BF16 storage, one field per node,
-// tiles with the x halo in the box.  Shapes (d->tma_tile for IWB, -1 auto):
-// 0 = 64 x 16, 1 = 128 x 8, 2 = 128 x 4 (12 stages), 3 = 64 x 8 (12
-// stages, the default): with the 27-point gather's register use (about 120
-// per thread) 160-thread CTAs keep three CTAs on an SM (measured on the
-// 512 x 384 x 256 room, FP32: 0.297 ms per step against 0.387 ms for the
-// 288-thread 64 x 16 and 128 x 8 tiles).
-template <typename S, typename C, int TX, int TY, int NS>
+// tiles with the x halo in the box; every stage also carries the plane's
+// closed-neighbour masks.  Shapes (d->tma_tile for IWB, -1 auto): 0 = 64 x
+// 16 and 1 = 128 x 8 (288 threads, 8 stages), 2 = 128 x 4 (5 stages), and
+// 160-thread 64 x 8 tiles: 3 = 8 stages, three CTAs per SM (the default), 4 =
+// 6 stages, four CTAs, 5 = 5 stages, five CTAs (registers capped to fit, with
+// spills).  Measured on the 512 x 384 x 256 room, FP32: 248, 180 and 122 G
+// node-updates/s for shapes 3, 4 and 5.
+template <typename S, typename C, int TX, int TY, int NS, int MINB = 1>
 int launch_iwb_l(pfdtd_domain* d, const void* cur, void* past, cudaStream_t s) {
-  return launch_tma_t<S, C, 3, Layout<S, C, TX, TY, NS, true>>(d, cur, past, s);
+  return launch_tma_t<S, C, 3, Layout<S, C, TX, TY, NS, true, true, MINB>>(d, cur, past, s);
 }
 
 template <typename S, typename C>
 int launch_iwb_c(pfdtd_domain* d, const void* cur, void* past, cudaStream_t s) {
   int tile = d->tma_tile;
-  if (tile < 0 || tile > 3) tile = 3;
+  if (tile < 0 || tile > 5) tile = 3;
   switch (tile) {
     case 0: return launch_iwb_l<S, C, 64, 16, 8>(d, cur, past, s);
     case 1: return launch_iwb_l<S, C, 128, 8, 8>(d, cur, past, s);
-    case 2: return launch_iwb_l<S, C, 128, 4, 12>(d, cur, past, s);
-    default: return launch_iwb_l<S, C, 64, 8, 12>(d, cur, past, s);
+    case 2: return launch_iwb_l<S, C, 128, 4, 5>(d, cur, past, s);
+    case 4: return launch_iwb_l<S, C, 64, 8, 6, 4>(d, cur, past, s);
+    case 5: return launch_iwb_l<S, C, 64, 8, 5, 5>(d, cur, past, s);
+    default: return launch_iwb_l<S, C, 64, 8, 8, 3>(d, cur, past, s);
   }
 }
 
