@@ -209,10 +209,31 @@ def cpu_baseline(room, src, rec, budget_s: float, fields=1):
     t0 = time.perf_counter()
     O.run(*args, rooms.impulse(n)[None], rec_idx, n, threads=threads)
     dt = time.perf_counter() - t0
+    # the same rule on one thread, a short sample
+    n1 = 2
+    t0 = time.perf_counter()
+    O.run(*args, rooms.impulse(n1)[None], rec_idx, n1, threads=1)
+    dt1 = time.perf_counter() - t0
     return {"value": X * Y * (Z - 2) * n / dt, "unit": METRIC, "cores": threads,
             "kind": "port",
             "sample": f"{X}x{Y}x{Z} room, {n} leapfrog steps of one field, FP32 "
-                      f"SRL forward, {threads} OpenMP threads"}
+                      f"SRL forward, {threads} OpenMP threads",
+            "one_thread": {"value": X * Y * (Z - 2) * n1 / dt1, "sample": f"{n1} steps"},
+            "cpu_model": cpu_model()}
+
+
+def cpu_model() -> str:
+    """The host CPU's model name (lscpu), else the machine type."""
+    import platform
+    import subprocess
+    try:
+        out = subprocess.run(["lscpu"], capture_output=True, text=True, timeout=10).stdout
+        for line in out.splitlines():
+            if line.startswith("Model name:"):
+                return line.split(":", 1)[1].strip()
+    except Exception:
+        pass
+    return platform.processor() or platform.machine()
 
 
 def run_reference_arm(a, world, rank):
