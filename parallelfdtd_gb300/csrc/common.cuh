@@ -177,6 +177,10 @@ struct pfdtd_domain {
   // that stands for the position byte in the IWB class key (stencil.cu)
   uint32_t* d_iwb_mask = nullptr;
   uint8_t* d_iwb_code = nullptr;
+  // IWB with DIF walls on the TMA path: the weighted neighbour sum sw of each
+  // DIF node (classes flagged by bit 31 of their pos word), written by the
+  // update kernel and read by the DIF pass instead of a second 27-point gather
+  float* d_iwb_sw = nullptr;
   int64_t class_version = 0;
 
   // sources / receivers

@@ -14,9 +14,13 @@
 // P^n and overwrites them.  Because the main kernel has by then overwritten
 // P^{n-1} at those nodes, each DIF node keeps its own previous value in its
 // state (re-read from the past field at the start of every run or step).
+// For IWB on the TMA path the update kernel stores each DIF node's weighted
+// neighbour sum sw (d_iwb_sw), so this pass reads one value per node instead
+// of gathering the 26 neighbours again.
 #include "common.cuh"
 
 #include <algorithm>
+#include <cstring>
 #include <vector>
 
 namespace pfdtd {
@@ -100,7 +104,8 @@ __global__ void k_dif_update(const int64_t* __restrict__ list, int64_t n, int ks
                              const typename Store<S>::A* __restrict__ dtab, const S* __restrict__ P,
                              S* __restrict__ Pp, typename Store<S>::A* __restrict__ st, int64_t X,
                              int64_t XY, typename Store<S>::A l2, const uint32_t* __restrict__ cpos,
-                             const uint32_t* __restrict__ iwb_mask) {
+                             const uint32_t* __restrict__ iwb_mask,
+                             const float* __restrict__ iwb_sw) {
   using A = typename Store<S>::A;
   using R = Rn<A>;
   using Sto = Store<S>;
@@ -136,24 +141,31 @@ __global__ void k_dif_update(const int64_t* __restrict__ list, int64_t n, int ks
       const A s7 = R::add(R::add(R::add(R::add(R::add(R::add(xm, xp), ym), yp), zp), zm), sb6);
       num = R::sub(R::add(R::sub(R::mul(s7, l2), R::mul(b, p)), R::mul(cc, pp)), R::mul(g2, s1));
     } else {
-      // IWB: closed neighbours (mask bits, canonical order) contribute p
-      const uint32_t mk = iwb_mask[node];
-      A m[3][3][3];
-      int kk = 0;
-      for (int dz = -1; dz <= 1; ++dz)
-        for (int dy = -1; dy <= 1; ++dy)
-          for (int dx = -1; dx <= 1; ++dx) {
-            A v = p;
-            if (dx != 0 || dy != 0 || dz != 0) {
-              if (!((mk >> kk) & 1u)) v = Sto::load(P[i + dz * XY + dy * X + dx * ks]);
-              ++kk;
+      // IWB: closed neighbours (mask bits, canonical order) contribute p.
+      // The TMA update kernel has already formed sw for this node (same
+      // sums, same rounding) when iwb_sw is given.
+      A sw;
+      if (iwb_sw != nullptr) {
+        sw = (A)iwb_sw[node];
+      } else {
+        const uint32_t mk = iwb_mask[node];
+        A m[3][3][3];
+        int kk = 0;
+        for (int dz = -1; dz <= 1; ++dz)
+          for (int dy = -1; dy <= 1; ++dy)
+            for (int dx = -1; dx <= 1; ++dx) {
+              A v = p;
+              if (dx != 0 || dy != 0 || dz != 0) {
+                if (!((mk >> kk) & 1u)) v = Sto::load(P[i + dz * XY + dy * X + dx * ks]);
+                ++kk;
+              }
+              m[dz + 1][dy + 1][dx + 1] = v;
             }
-            m[dz + 1][dy + 1][dx + 1] = v;
-          }
-      A f1, f2, f3;
-      iwb_sums(m, f1, f2, f3);
-      const A sw = R::mul(l2, R::add(R::add(R::mul(f1, (A)0.25), R::mul(f2, (A)0.125)),
-                                     R::mul(f3, (A)0.0625)));
+        A f1, f2, f3;
+        iwb_sums(m, f1, f2, f3);
+        sw = R::mul(l2, R::add(R::add(R::mul(f1, (A)0.25), R::mul(f2, (A)0.125)),
+                               R::mul(f3, (A)0.0625)));
+      }
       num = R::sub(R::sub(R::add(sw, R::mul(b, p)), R::mul(cc, pp)), R::mul(g2, s1));
     }
     const A out = R::mul(a, num);
@@ -215,24 +227,26 @@ int launch_dif_t(pfdtd_domain* d, const void* cur, void* past, cudaStream_t s) {
   const int64_t n = d->n_dif * d->K;
   const int64_t XE = d->X * d->K, XYE = d->XY * d->K;
   const int g = grid_for(n);
+  const float* iwb_sw =
+      (d->class_scheme == PFDTD_IWB && d->d_iwb_sw && uses_tma(d)) ? d->d_iwb_sw : nullptr;
   switch (d->class_scheme) {
     case PFDTD_SRL:
       k_dif_update<S, 1><<<g, 256, 0, s>>>(d->d_dif_list, n, d->kshift, d->d_cls, d->cls_bytes,
                                            (const A*)d->d_dif_tab, (const S*)cur, (S*)past,
                                            (A*)d->d_dif_state, XE, XYE, l2, cpos,
-                                           d->d_iwb_mask);
+                                           d->d_iwb_mask, iwb_sw);
       break;
     case PFDTD_IWB:
       k_dif_update<S, 2><<<g, 256, 0, s>>>(d->d_dif_list, n, d->kshift, d->d_cls, d->cls_bytes,
                                            (const A*)d->d_dif_tab, (const S*)cur, (S*)past,
                                            (A*)d->d_dif_state, XE, XYE, l2, cpos,
-                                           d->d_iwb_mask);
+                                           d->d_iwb_mask, iwb_sw);
       break;
     default:
       k_dif_update<S, 0><<<g, 256, 0, s>>>(d->d_dif_list, n, d->kshift, d->d_cls, d->cls_bytes,
                                            (const A*)d->d_dif_tab, (const S*)cur, (S*)past,
                                            (A*)d->d_dif_state, XE, XYE, l2, cpos,
-                                           d->d_iwb_mask);
+                                           d->d_iwb_mask, iwb_sw);
   }
   count_launch();
   PFDTD_CK(cudaGetLastError());
@@ -307,6 +321,18 @@ int build_dif(pfdtd_domain* d, const std::vector<uint16_t>& keys,
     const size_t sbytes = (size_t)total * d->K * 4 * d->arith_size();
     PFDTD_CK(d->alloc(&d->d_dif_state, sbytes));
     PFDTD_CK(cudaMemsetAsync(d->d_dif_state, 0, sbytes, s));
+    if (d->class_scheme == PFDTD_IWB && d->K == 1 && d->precision != PFDTD_F64) {
+      // flag the DIF classes (bit 31 of the pos word, unused by the IWB
+      // kernels) so that the TMA update stores their sw for the DIF pass
+      const size_t n = keys.size(), as = d->arith_size();
+      std::vector<uint32_t> pos(n);
+      std::memcpy(pos.data(), main_tab.data() + 3 * n * as, n * sizeof(uint32_t));
+      for (size_t i = 0; i < n; ++i)
+        if (is_dif[i]) pos[i] |= 0x80000000u;
+      PFDTD_CK(cudaMemcpyAsync((char*)d->d_ctab + 3 * n * as, pos.data(), n * sizeof(uint32_t),
+                               cudaMemcpyHostToDevice, s));
+      if (!d->d_iwb_sw) PFDTD_CK(d->alloc((void**)&d->d_iwb_sw, (size_t)d->N * sizeof(float)));
+    }
   }
   PFDTD_CK(cudaStreamSynchronize(s));
   d->release(d_is);

@@ -310,7 +310,8 @@ k_update_tma(const __grid_constant__ CUtensorMap map_cur, const __grid_constant_
              const __grid_constant__ CUtensorMap map_cls,
              const __grid_constant__ CUtensorMap map_mask, const S* __restrict__ P,
              S* __restrict__ Pp, ClassTab<typename Store<S>::A> tab, int X, int Y, int64_t XY,
-             int z_last, int zc, typename Store<S>::A l2, int* __restrict__ err, int kshift = 0) {
+             int z_last, int zc, typename Store<S>::A l2, int* __restrict__ err, int kshift = 0,
+             float* __restrict__ iwb_sw = nullptr) {
   using A = typename Store<S>::A;
   using R = Rn<A>;
   using St = Store<S>;
@@ -457,6 +458,7 @@ k_update_tma(const __grid_constant__ CUtensorMap map_cur, const __grid_constant_
           const float sw = R::mul((float)l2, R::add(R::add(R::mul(s1[e], 0.25f),
                                                            R::mul(s2[e], 0.125f)),
                                                     R::mul(s3[e], 0.0625f)));
+          if (iwb_sw != nullptr && (k.pos >> 31)) iwb_sw[idx + e] = sw;  // a DIF node
           const float out = R::mul(k.a, R::sub(R::add(sw, R::mul(k.b, cc0[e])),
                                                R::mul(k.c, St::load(vpp.v[e]))));
           res[e] = St::store(out);
@@ -681,7 +683,7 @@ int launch_tma_t(pfdtd_domain* d, const void* cur, void* past, cudaStream_t s) {
   k_update_tma<S, C, SCHEME, Lay, BATCHED><<<dim3(gx, gy, gz), Lay::THREADS, Lay::SMEM, s>>>(
       ts.halo[cur_i], ts.tile[past_i], ts.cls, Lay::MASK ? ts.mask : ts.cls, (const S*)cur,
       (S*)past, tab, (int)XE, (int)d->Y, d->XY * d->K, (int)(d->Z - 1), (int)zc,
-      (A)d->params[1], d->d_err, d->kshift);
+      (A)d->params[1], d->d_err, d->kshift, SCHEME == 3 ? d->d_iwb_sw : nullptr);
   count_launch();
   PFDTD_CK(cudaGetLastError());
   return PFDTD_OK;
