@@ -308,12 +308,15 @@ int pfdtd_get_kernel(pfdtd_domain* d, int* variant);
 int pfdtd_set_temporal_block(pfdtd_domain* d, int depth);
 int pfdtd_get_temporal_block(pfdtd_domain* d, int* depth, int* active, char* why,
                              size_t why_len);
-/* Tile shape of the blocked kernel, -1 (default) or 0..2:
+/* Tile shape of the blocked kernel, -1 (default) or 0..3:
  *   one field per node: 0 = 64 x 32 nodes, 256 threads of two rows;
  *     1 = 64 x 32, 512 threads of one row; 2 = 64 x 64, 512 threads of two
  *     rows (depths 2, 3); depth 4 has only shape 1;
  *   batched fields: 0 = 32 x 32 nodes of 4 fields, 512 threads of two rows;
- *     1 = one row per thread (FP32 depth 4: 32 x 24); depth 4 only shape 1.
+ *     1 = one row per thread (FP32 depth 4: 32 x 24); depth 4 only shape 1;
+ *     2 and 3 = 32 x 32 nodes of 4 fields with packed two-field arithmetic,
+ *     512 threads of two rows (2) or 1024 threads of one row (3); SRL
+ *     forward scheme, depths 2 and 3, fewer than 256 node classes.
  * A shape that does not exist for the depth makes the next run fail with
  * PFDTD_ERR_ARG. */
 int pfdtd_set_tb_shape(pfdtd_domain* d, int shape);

@@ -1058,7 +1058,7 @@ int pfdtd_get_temporal_block(pfdtd_domain* d, int* depth, int* active, char* why
 
 int pfdtd_set_tb_shape(pfdtd_domain* d, int shape) {
   if (int rc = check_domain(d)) return rc;
-  if (shape < -1 || shape > 2) return fail(PFDTD_ERR_ARG, "blocked tile shape must be -1..2");
+  if (shape < -1 || shape > 3) return fail(PFDTD_ERR_ARG, "blocked tile shape must be -1..3");
   d->tb_shape = shape;
   if (d->graph.exec) {
     cudaGraphExecDestroy(d->graph.exec);
@@ -1131,7 +1131,7 @@ int pfdtd_autotune(pfdtd_domain* d, int max_depth, int iters, int* best_depth, i
   struct Cand { int depth, shape; };
   std::vector<Cand> cands{{0, -1}};
   for (int depth = 2; depth <= max_depth; ++depth)
-    for (int shape = 0; shape < 3; ++shape) cands.push_back({depth, shape});
+    for (int shape = 0; shape < 4; ++shape) cands.push_back({depth, shape});
   for (const Cand& c : cands) {
     d->tb_depth = c.depth;
     d->tb_shape = c.shape;

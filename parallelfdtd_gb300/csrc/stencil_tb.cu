@@ -107,7 +107,9 @@ int launch_tb(pfdtd_domain* d, void* rec_out, int64_t rec_ld, int64_t inject_end
 bool tb_shape_valid(const pfdtd_domain* d, int shape) {
   if (shape < 0) return true;
   if (d->tb_depth == 4) return shape == 1;
-  return shape < (d->K == 1 ? 3 : 2);
+  if (d->K > 1 && (shape == 2 || shape == 3))  // packed pair kernel: forward, a free class slot
+    return d->class_scheme == PFDTD_SRL_FORWARD && d->n_classes < 256;
+  return shape < 3;
 }
 
 }  // namespace pfdtd

@@ -45,6 +45,7 @@
 #include <algorithm>
 #include <cstring>
 #include <mutex>
+#include <type_traits>
 
 namespace pfdtd {
 namespace tb {
@@ -590,12 +591,17 @@ int launch_tb_t(pfdtd_domain* d, void* rec_out, int64_t rec_ld, int64_t inject_e
   return PFDTD_OK;
 }
 
+#include "stencil_tb_packed.cuh"
+
 // Tile shapes (x nodes x rows), selected by index (d->tb_shape, -1 = 0):
 //  unbatched  0: 64 x 32 from 256 threads of two rows
 //             1: 64 x 32 from 512 threads of one row
 //             2: 64 x 64 from 512 threads of two rows (depth 2, 3)
 //  batched    0: 32 x 32 nodes of 4 fields from 512 threads of two rows
 //             1: 32 x 32 (FP32 depth 4: 32 x 24) from one row per thread
+//             2: 32 x 32 nodes of 4 fields, packed pair arithmetic, two rows
+//                per thread (stencil_tb_packed.cuh; forward scheme, depth 2, 3)
+//             3: as 2 with one row per thread (1024 threads)
 // Depth 4 has only shape 1; other combinations report PFDTD_ERR_ARG.
 template <typename S, int SCHEME, int T>
 int launch_tb_d(pfdtd_domain* d, void* rec_out, int64_t rec_ld, int64_t inject_end,
@@ -630,6 +636,10 @@ int launch_tb_d(pfdtd_domain* d, void* rec_out, int64_t rec_ld, int64_t inject_e
       if (shape == 1)
         return launch_tb_t<S, SCHEME, TbShape<S, 32, 32, 1, T, true>>(d, rec_out, rec_ld,
                                                                       inject_end, s);
+      if constexpr (SCHEME == 0) {
+        if (shape == 2) return launch_tb_packed<S, T, 2>(d, rec_out, rec_ld, inject_end, s);
+        if (shape == 3) return launch_tb_packed<S, T, 1>(d, rec_out, rec_ld, inject_end, s);
+      }
     }
   }
   return fail(PFDTD_ERR_ARG, "blocked tile shape not available for this depth and batching");

@@ -312,7 +312,8 @@ class Domain:
         L.call("pfdtd_set_temporal_block", self.handle, int(depth))
 
     def set_tb_shape(self, shape: int) -> None:
-        """Tile shape of the blocked kernel (-1 default, 0..2)."""
+        """Tile shape of the blocked kernel (-1 default, 0..3; 2 and 3 are the
+        packed two-field kernels for batched fields)."""
         L.call("pfdtd_set_tb_shape", self.handle, int(shape))
 
     def autotune(self, max_depth: int = 4, iters: int = 10):

@@ -235,3 +235,36 @@ def test_blocked_then_per_step_on_the_other_buffer_pair(gpu, prec):
     assert info[1], info[2]
     assert np.array_equal(g1, g0)
     assert np.array_equal(P1, P0) and np.array_equal(Pp1, Pp0)
+
+
+# The packed-pair kernel for batched fields (tile shapes 2 and 3, two rows
+# or one row per thread): 32 x 32 node
+# tiles with cores of 32 - 2T, so this room (not a multiple of the core in x
+# or y) has partial tiles on both far edges; sources and receivers sit on
+# and next to core boundaries.
+@pytest.mark.parametrize("fields,prec,depth,shape", [
+    (4, "f32", 2, 2), (4, "f32", 3, 2), (16, "f32", 3, 2), (8, "f16", 3, 2), (16, "bf16", 2, 2),
+    (4, "f32", 2, 3), (4, "f32", 3, 3), (16, "f32", 3, 3), (8, "f16", 3, 3), (16, "f16", 2, 3),
+    (8, "bf16", 3, 3), (16, "bf16", 2, 3)])
+def test_blocked_batched_packed(gpu, fields, prec, depth, shape):
+    room = rooms.boxes_room((100, 76, 46), n_boxes=6, edge=(5, 14), n_materials=7, seed=41)
+    steps = 101
+    pulse = rooms.gaussian_pulse(steps, 3.0)
+    air = set(map(tuple, room.random_air_nodes(6000, seed=5)))
+    core = 32 - 2 * depth
+    want = [(core - 1 + depth, core + depth, 20), (core + depth, core - 1 + depth, 21),
+            (2 * core + depth, core + depth, 3), (30, 40, 44), (97, 73, 30)]
+    edge = [p for p in want if p in air]
+    pts = edge + [tuple(p) for p in room.random_air_nodes(3 * fields, seed=8)]
+    srcs = [(pts[i], 1) for i in range(fields)]
+    recs = pts[:3 * fields]
+    src_f = list(range(fields))
+    rec_f = [i % fields for i in range(3 * fields)]
+    samples = np.stack([pulse * (1 + 0.1 * f) for f in range(fields)])
+    g0, P0, Pp0, _ = run(room, prec, "forward", 0, srcs, recs, samples, steps, fields, src_f, rec_f)
+    g1, P1, Pp1, info = run(room, prec, "forward", depth, srcs, recs, samples, steps, fields,
+                            src_f, rec_f, shape=shape)
+    assert info[1], info[2]
+    assert np.abs(g0).max() > 1e-3
+    assert np.array_equal(g1, g0), f"receivers differ, max |d| {np.abs(g1 - g0).max():.3e}"
+    assert np.array_equal(P1, P0) and np.array_equal(Pp1, Pp0)
