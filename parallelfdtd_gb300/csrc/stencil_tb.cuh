@@ -193,7 +193,9 @@ k_update_tb(const S* __restrict__ Pa, const S* __restrict__ Pb, S* __restrict__ 
   constexpr bool BATCHED = Sh::BATCHED;
   using Rf = Rn<float>;
   extern __shared__ __align__(128) unsigned char smem_raw[];
-  unsigned char* smem = (unsigned char*)(((uintptr_t)smem_raw + 127) & ~(uintptr_t)127);
+  // 128-byte aligned base, derived within the shared window (an integer
+  // round trip would make every access through it a generic one)
+  unsigned char* smem = smem_raw + ((128u - (smem_u32(smem_raw) & 127u)) & 127u);
   __shared__ PackedCoef<float> stab[256];
   __shared__ int s_nsrc, s_nrec;
   ListEntry* src_list = (ListEntry*)(smem + Sh::LIST_OFF);

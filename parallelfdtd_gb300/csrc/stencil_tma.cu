@@ -321,7 +321,9 @@ k_update_tma(const __grid_constant__ CUtensorMap map_cur, const __grid_constant_
   constexpr bool kSmemTab = (sizeof(C) == 1);
   extern __shared__ __align__(128) unsigned char smem_raw[];
   // TMA destinations: 128-byte aligned stage buffers.
-  unsigned char* smem = (unsigned char*)(((uintptr_t)smem_raw + 127) & ~(uintptr_t)127);
+  // 128-byte aligned base, derived within the shared window (an integer
+  // round trip would make every access through it a generic one)
+  unsigned char* smem = smem_raw + ((128u - (smem_u32(smem_raw) & 127u)) & 127u);
   __shared__ PackedCoef<A> stab[kSmemTab ? 256 : 1];
 
   // A launch after one whose pipeline failed does nothing: the run is
