@@ -46,6 +46,45 @@ template <> struct Rn<double> {
   static __device__ __forceinline__ double sub(double a, double b) { return __dsub_rn(a, b); }
 };
 
+// Packed pairs of floats (two fields of one node) and the sm_100-family
+// f32x2 operations on them.  Each lane of add/sub/mul.rn.f32x2 rounds as the
+// scalar __fadd_rn/__fsub_rn/__fmul_rn.  ptxas may contract a packed multiply
+// into a following packed add even with .rn, so kernels that must not fuse
+// form products as fma2(x, y, nz) with nz = (-0, -0) taken from a kernel
+// argument: one rounding of the exact product, and an addend the compiler
+// cannot fold away.
+namespace px {
+typedef unsigned long long f2;  // the lower field in the low word
+__device__ __forceinline__ f2 add2(f2 a, f2 b) {
+  f2 d;
+  asm("add.rn.f32x2 %0, %1, %2;" : "=l"(d) : "l"(a), "l"(b));
+  return d;
+}
+__device__ __forceinline__ f2 sub2(f2 a, f2 b) {
+  f2 d;
+  asm("sub.rn.f32x2 %0, %1, %2;" : "=l"(d) : "l"(a), "l"(b));
+  return d;
+}
+__device__ __forceinline__ f2 mul2(f2 a, f2 b) {
+  f2 d;
+  asm("mul.rn.f32x2 %0, %1, %2;" : "=l"(d) : "l"(a), "l"(b));
+  return d;
+}
+__device__ __forceinline__ f2 fma2(f2 a, f2 b, f2 c) {
+  f2 d;
+  asm("fma.rn.f32x2 %0, %1, %2, %3;" : "=l"(d) : "l"(a), "l"(b), "l"(c));
+  return d;
+}
+__device__ __forceinline__ f2 pk2(float lo, float hi) {
+  f2 d;
+  asm("mov.b64 %0, {%1, %2};" : "=l"(d) : "f"(lo), "f"(hi));
+  return d;
+}
+__device__ __forceinline__ void up2(f2 v, float& lo, float& hi) {
+  asm("mov.b64 {%0, %1}, %2;" : "=f"(lo), "=f"(hi) : "l"(v));
+}
+}  // namespace px
+
 // IWB 27-point sums of one node from its 3 x 3 x 3 neighbourhood
 // m[dz+1][dy+1][dx+1] after the closure substitution (centre unused), in the
 // scheme's canonical order, built from in-plane sums so that a z-march can

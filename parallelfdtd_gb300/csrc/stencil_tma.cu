@@ -25,6 +25,7 @@
 
 #include <algorithm>
 #include <cstring>
+#include <type_traits>
 
 namespace pfdtd {
 namespace {
@@ -311,7 +312,7 @@ k_update_tma(const __grid_constant__ CUtensorMap map_cur, const __grid_constant_
              const __grid_constant__ CUtensorMap map_mask, const S* __restrict__ P,
              S* __restrict__ Pp, ClassTab<typename Store<S>::A> tab, int X, int Y, int64_t XY,
              int z_last, int zc, typename Store<S>::A l2, int* __restrict__ err, int kshift = 0,
-             float* __restrict__ iwb_sw = nullptr) {
+             float* __restrict__ iwb_sw = nullptr, float nzf = -0.0f) {
   using A = typename Store<S>::A;
   using R = Rn<A>;
   using St = Store<S>;
@@ -511,6 +512,67 @@ k_update_tma(const __grid_constant__ CUtensorMap map_cur, const __grid_constant_
         const uint2 w = *reinterpret_cast<const uint2*>(Cl + ly * kTX + lx);
         cid[0] = w.x & 0xFFFFu; cid[1] = w.x >> 16; cid[2] = w.y & 0xFFFFu; cid[3] = w.y >> 16;
       }
+      if constexpr (SCHEME == 0 && sizeof(A) == 4) {
+        // Forward update of the thread's 4 elements as two packed pairs: the
+        // same operations and rounding as the scalar loop below, with every
+        // product formed as fma(x, y, -0) so that none is contracted.
+        // Batched: the pairs are fields of one node (one class); otherwise
+        // adjacent x nodes (a class each).
+        using namespace px;
+        auto coef = [&](int e) -> PackedCoef<A> {
+          if (kSmemTab) return stab[cid[e]];
+          return PackedCoef<A>{__ldg(tab.a + cid[e]), __ldg(tab.b + cid[e]),
+                               __ldg(tab.c + cid[e]), __ldg(tab.pos + cid[e])};
+        };
+        const f2 l22 = pk2(l2, l2), nz = pk2(nzf, nzf);
+        auto pr = [](const V4<S>& v, int h) -> f2 {
+          return pk2(St::load(v.v[2 * h]), St::load(v.v[2 * h + 1]));
+        };
+        f2 aa[2], bb[2], cc[2], xm2[2], xp2[2];
+        if constexpr (BATCHED) {
+          const PackedCoef<A> k = coef(0);
+          aa[0] = aa[1] = pk2(k.a, k.a);
+          bb[0] = bb[1] = pk2(k.b, k.b);
+          cc[0] = cc[1] = pk2(k.c, k.c);
+          xm2[0] = pr(vxm, 0); xm2[1] = pr(vxm, 1);
+          xp2[0] = pr(vxp, 0); xp2[1] = pr(vxp, 1);
+        } else {
+#pragma unroll
+          for (int h = 0; h < 2; ++h) {
+            const PackedCoef<A> k0 = coef(2 * h), k1 = coef(2 * h + 1);
+            aa[h] = pk2(k0.a, k1.a);
+            bb[h] = pk2(k0.b, k1.b);
+            cc[h] = pk2(k0.c, k1.c);
+          }
+          const A c0 = St::load(vc.v[0]), c1 = St::load(vc.v[1]), c2 = St::load(vc.v[2]),
+                  c3 = St::load(vc.v[3]);
+          xm2[0] = pk2(left, c0); xm2[1] = pk2(c1, c2);
+          xp2[0] = pk2(c1, c2); xp2[1] = pk2(c3, right);
+        }
+        S res[kVec];
+#pragma unroll
+        for (int h = 0; h < 2; ++h) {
+          const f2 s6 = add2(add2(add2(add2(add2(pr(vzp, h), pr(vzm, h)), pr(vyp, h)),
+                                      pr(vym, h)), xp2[h]), xm2[h]);
+          const f2 o = mul2(aa[h], sub2(add2(fma2(bb[h], pr(vc, h), nz), fma2(l22, s6, nz)),
+                                        fma2(cc[h], pr(vpp, h), nz)));
+          float lo, hi;
+          up2(o, lo, hi);
+          if constexpr (sizeof(S) == 4) {
+            res[2 * h] = lo;
+            res[2 * h + 1] = hi;
+          } else if constexpr (std::is_same<S, __half>::value) {
+            const __half2 t = __floats2half2_rn(lo, hi);  // each half rounded to nearest even
+            res[2 * h] = __low2half(t);
+            res[2 * h + 1] = __high2half(t);
+          } else {
+            const __nv_bfloat162 t = __floats2bfloat162_rn(lo, hi);
+            res[2 * h] = __low2bfloat16(t);
+            res[2 * h + 1] = __high2bfloat16(t);
+          }
+        }
+        stg4(Pp + idx, res);
+      } else {
       S res[kVec];
 #pragma unroll
       for (int e = 0; e < kVec; ++e) {
@@ -550,6 +612,7 @@ k_update_tma(const __grid_constant__ CUtensorMap map_cur, const __grid_constant_
         res[e] = St::store(out);
       }
       stg4(Pp + idx, res);
+      }
     }
     __syncwarp();
     if (lane == 0) mbar_arrive(bar_empty + 8 * sm);
@@ -685,7 +748,7 @@ int launch_tma_t(pfdtd_domain* d, const void* cur, void* past, cudaStream_t s) {
   k_update_tma<S, C, SCHEME, Lay, BATCHED><<<dim3(gx, gy, gz), Lay::THREADS, Lay::SMEM, s>>>(
       ts.halo[cur_i], ts.tile[past_i], ts.cls, Lay::MASK ? ts.mask : ts.cls, (const S*)cur,
       (S*)past, tab, (int)XE, (int)d->Y, d->XY * d->K, (int)(d->Z - 1), (int)zc,
-      (A)d->params[1], d->d_err, d->kshift, SCHEME == 3 ? d->d_iwb_sw : nullptr);
+      (A)d->params[1], d->d_err, d->kshift, SCHEME == 3 ? d->d_iwb_sw : nullptr, -0.0f);
   count_launch();
   PFDTD_CK(cudaGetLastError());
   return PFDTD_OK;
@@ -759,14 +822,17 @@ int auto_tile16(const pfdtd_domain* d) {
 
 template <typename S>
 int launch_tma_16(pfdtd_domain* d, const void* cur, void* past, cudaStream_t s) {
+  // Two CTAs per SM (registers capped to allow it): a 256 x 8 tile of 16-bit
+  // fields holds half the bytes of the FP32 tile, and one CTA per SM leaves
+  // too few loads in flight to stream at HBM speed.
   if (d->K > 1)
-    return launch_tma_batched<S, Layout<S, uint8_t, 256, 8, 8, false>,
-                              Layout<S, uint16_t, 256, 8, 8, false>>(d, cur, past, s);
+    return launch_tma_batched<S, Layout<S, uint8_t, 256, 8, 8, false, false, 2>,
+                              Layout<S, uint16_t, 256, 8, 8, false, false, 2>>(d, cur, past, s);
   switch (d->tma_tile < 0 ? auto_tile16(d) : d->tma_tile) {
 #define PFDTD_CASE16(id, tx, ty, ns, xh)                                                  \
   case id:                                                                                \
-    return launch_tma_l<S, Layout<S, uint8_t, tx, ty, ns, xh>,                             \
-                        Layout<S, uint16_t, tx, ty, ns, xh>>(d, cur, past, s);
+    return launch_tma_l<S, Layout<S, uint8_t, tx, ty, ns, xh, false, 2>,                   \
+                        Layout<S, uint16_t, tx, ty, ns, xh, false, 2>>(d, cur, past, s);
     PFDTD_F16_TILES(PFDTD_CASE16)
 #undef PFDTD_CASE16
   }
