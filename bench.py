@@ -89,6 +89,25 @@ def dist_env():
     return world, rank, local
 
 
+def max_over_ranks(value: float, world: int, device: str) -> float:
+    """The largest of every rank's value (replicas are timed by the slowest
+    rank); the value itself on one rank.  Needs an initialised process group
+    when world > 1 (NCCL with a CUDA device, gloo with "cpu")."""
+    if world <= 1:
+        return value
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor([value], device=device, dtype=torch.float64)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def replica_rate(units_per_rank: float, world: int, seconds: float) -> float:
+    """Whole-job rate of independent replicas: every rank's units over the
+    slowest rank's time."""
+    return units_per_rank * world / seconds
+
+
 C4_DIMS = (384, 320, 256)
 C4_STEPS = 4000
 
@@ -297,14 +316,13 @@ def run_serving(a, world, rank, local):
     if world > 1:
         import torch.distributed as dist
         dist.init_process_group("nccl" if torch.cuda.is_available() else "gloo")
-        t = torch.tensor([wall], device=f"cuda:{local}", dtype=torch.float64)
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        wall = float(t.item())
+        wall = max_over_ranks(wall, world, f"cuda:{local}")
         dist.destroy_process_group()
     st = res["stats"]
     if rank == 0:
         line = {
-            "metric": METRIC, "value": res["node_updates"] * world / wall, "unit": METRIC,
+            "metric": METRIC, "value": replica_rate(res["node_updates"], world, wall),
+            "unit": METRIC,
             "n_gpus": world, "steps": len(trace), "warmup": 0,
             "ms_per_step": wall * 1e3 / len(trace), "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": a.precision,
@@ -412,13 +430,8 @@ def main():
         barrier()
     launches = L.load().pfdtd_kernel_launches() - l0
     ms = ev0.elapsed_time(ev1) / a.steps
-    t_local = ms
-    if world > 1:
-        import torch.distributed as dist
-        t = torch.tensor([ms], device=f"cuda:{local}")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        ms = float(t.item())
-    value = updates_per_run * world / (ms * 1e-3)
+    ms = max_over_ranks(ms, world, f"cuda:{local}")
+    value = replica_rate(updates_per_run, world, ms * 1e-3)
 
     # ---- dominant kernel alone (same stream, same arguments) ---------------
     prof_iters = 50
@@ -463,12 +476,8 @@ def main():
         d.run(S, out=out_host)
     barrier()
     e2e_s = (time.perf_counter() - t0) / a.steps
-    if world > 1:
-        import torch.distributed as dist
-        t = torch.tensor([e2e_s], device=f"cuda:{local}", dtype=torch.float64)
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        e2e_s = float(t.item())
-    e2e = {"value": updates_per_run * world / e2e_s, "unit": METRIC,
+    e2e_s = max_over_ranks(e2e_s, world, f"cuda:{local}")
+    e2e = {"value": replica_rate(updates_per_run, world, e2e_s), "unit": METRIC,
            "h2d_bytes_per_step": int(2 * room.n_nodes + samples.nbytes),
            "d2h_bytes_per_step": int(n_rec * S * (8 if prec == "f64" else 4))}
 
