@@ -285,7 +285,12 @@ int pfdtd_set_kernel(pfdtd_domain* d, int variant);
 /* Tile shape of the TMA kernel for FP32 fields: 0 64x16, 1 128x8, 2 32x32,
  * 3 128x16, 4 128x4 (x halo in the TMA box); 5 128x8, 6 256x4, 7 256x8,
  * 8 256x2 (x halo read from global); -1 (default) picks the widest of
- * 256/128/64 that divides X.  FP64 always uses 64x8. */
+ * 256/128/64 that divides X.  FP64 always uses 64x8.  For the IWB scheme the
+ * same index picks the IWB shape: 0..5 carry the closed-neighbour masks and
+ * compute the closure in the kernel (0 64x16, 1 128x8, 2 128x4, 3..5 64x8
+ * with 3, 4, 5 CTAs per SM); 6..8 run the open sums in the kernel and a
+ * sparse pass for the nodes with a closed neighbour (6 64x8 with 4 CTAs per
+ * SM; 7 64x8 with 3; 8 128x8 with 2, the default). */
 int pfdtd_set_tile(pfdtd_domain* d, int tile);
 int pfdtd_get_kernel(pfdtd_domain* d, int* variant);
 

@@ -312,6 +312,10 @@ int update(const RunDesc& d, const St* P, St* Pp, const std::vector<T>& beta_tab
           ret = iwb_node<T, St>(P, XY * Z, c, X, XY, mask, pp, sw * ((T)1 / ((T)1 + beta)),
                                 (T)1 - beta, l2);
         }
+        // A node without the inside bit holds +0: its update is 0 times a
+        // finite value, whose sign would depend on neighbours that no inside
+        // node ever reads (the closure substitutes them); +0 fixes its bits.
+        if (pos == 0) ret = (T)0;
       } else if (d.scheme == 0 && slot >= 0) {
         const T position = (T)(pos & kForwardMask);
         const T sw = (T)(pos >> kInsideSwitch);

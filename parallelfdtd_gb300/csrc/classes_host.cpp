@@ -57,6 +57,10 @@ int eval(int scheme, int quirks, const double* params, const std::vector<double>
       ca[i] = swi * ((A)1 / ((A)1 + beta));
       cb[i] = (A)2 - (A)3.5 * l2;  // d4 = 2 - 7/2 lambda^2 (-3/2 at lambda = 1)
       cc[i] = (A)1 - beta;
+      // bit 30: an inside node with a closed neighbour (code >= 2), updated
+      // by the closure pass on the TMA path
+      cpos[i] = pos | (pos >= 2 ? 0x40000000u : 0u);
+      continue;
     } else if (scheme != PFDTD_SRL) {
       // kernels3d.cu:509-526
       const A position = (A)(pos & 0x7Fu);

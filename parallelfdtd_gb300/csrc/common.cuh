@@ -220,6 +220,13 @@ struct pfdtd_domain {
   // DIF node (classes flagged by bit 31 of their pos word), written by the
   // update kernel and read by the DIF pass instead of a second 27-point gather
   float* d_iwb_sw = nullptr;
+  // IWB on the TMA path: the closure nodes (inside, with a closed neighbour;
+  // classes flagged by bit 30 of their pos word) as flat-index order records
+  // {index, closed mask, class} (dif.cu).  The TMA update leaves P^{n-1} at
+  // these nodes and k_iwb_closure updates them.
+  void* d_iwb_closure = nullptr;
+  int64_t n_iwb_closure = 0;
+  bool iwb_closure_ready = false;
   int64_t class_version = 0;
 
   // sources / receivers
@@ -294,6 +301,8 @@ int build_dif(pfdtd_domain* d, const std::vector<uint16_t>& keys,
               const std::vector<uint8_t>& main_tab);
 int launch_dif(pfdtd_domain* d, const void* cur, void* past, cudaStream_t s);
 int launch_dif_init(pfdtd_domain* d, cudaStream_t s);
+int build_iwb_closure(pfdtd_domain* d, const std::vector<uint16_t>& keys);
+int launch_iwb_closure(pfdtd_domain* d, const void* cur, void* past, cudaStream_t s);
 // Implemented in setup.cu
 int launch_slice_gather(pfdtd_domain* d, int orientation, int64_t slice, float* dp, uint8_t* dq,
                         cudaStream_t s);

@@ -14,9 +14,10 @@
 // P^n and overwrites them.  Because the main kernel has by then overwritten
 // P^{n-1} at those nodes, each DIF node keeps its own previous value in its
 // state (re-read from the past field at the start of every run or step).
-// For IWB on the TMA path the update kernel stores each DIF node's weighted
-// neighbour sum sw (d_iwb_sw), so this pass reads one value per node instead
-// of gathering the 26 neighbours again.
+// For IWB on the TMA path the closure pass (k_iwb_closure, which updates every
+// node with a closed neighbour after the streaming update) stores each DIF
+// node's weighted neighbour sum sw (d_iwb_sw), so this pass reads one value
+// per node instead of gathering the 26 neighbours again.
 #include "common.cuh"
 
 #include <algorithm>
@@ -180,6 +181,125 @@ __global__ void k_dif_update(const int64_t* __restrict__ list, int64_t n, int ks
   }
 }
 
+// IWB closure nodes on the TMA path (no counterpart in the reference): the
+// update kernel has left P^{n-1} at every node whose class has a closed
+// neighbour (bit 30 of the pos word); this pass updates them with the
+// finite-volume closure, operation for operation as k_update_iwb and the
+// oracle's iwb_node: a closed neighbour (bit k of the node's mask, canonical
+// order) contributes the node's own value, the sums follow iwb_sums, and the
+// neighbours are read at their flat offsets.  For a DIF node (bit 31) it
+// also stores sw for the DIF pass that follows.
+//
+// One record per node (index, mask and class read together).  All 26
+// neighbours are loaded before the substitution so that a thread has them
+// in flight at once: the flat offsets of a node of planes 1..Z-2 stay within
+// the field's margins (at least X + 64 elements each side), and a closed
+// neighbour's value (outside the grid or in a margin) is replaced by a
+// select, never used in arithmetic.
+struct ClosureRec {
+  int64_t idx;
+  uint32_t mask;
+  uint32_t cls;
+};
+
+__global__ void k_closure_records(const int64_t* __restrict__ list, int64_t n,
+                                  const void* __restrict__ cls, int cls_bytes,
+                                  const uint32_t* __restrict__ mask, ClosureRec* __restrict__ rec) {
+  for (int64_t k = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; k < n;
+       k += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t i = list[k];
+    const unsigned c = cls_bytes == 1 ? ((const uint8_t*)cls)[i] : ((const uint16_t*)cls)[i];
+    rec[k] = ClosureRec{i, mask[i], c};
+  }
+}
+
+template <typename S>
+__global__ void __launch_bounds__(256)
+k_iwb_closure(const ClosureRec* __restrict__ recs, int64_t n, ClassTab<float> tab,
+              const S* __restrict__ P, S* __restrict__ Pp, int64_t X, int64_t XY, float l2,
+              float* __restrict__ iwb_sw) {
+  using R = Rn<float>;
+  using Sto = Store<S>;
+  for (int64_t k = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; k < n;
+       k += (int64_t)gridDim.x * blockDim.x) {
+    const ClosureRec r = recs[k];
+    const int64_t i = r.idx;
+    float m[3][3][3];
+#pragma unroll
+    for (int dz = -1; dz <= 1; ++dz)
+#pragma unroll
+      for (int dy = -1; dy <= 1; ++dy)
+#pragma unroll
+        for (int dx = -1; dx <= 1; ++dx)
+          m[dz + 1][dy + 1][dx + 1] = Sto::load(__ldg(P + i + dz * XY + dy * X + dx));
+    const float pp = Sto::load(Pp[i]);
+    const float p = m[1][1][1];
+    int kk = 0;
+#pragma unroll
+    for (int a = 0; a < 3; ++a)
+#pragma unroll
+      for (int b = 0; b < 3; ++b)
+#pragma unroll
+        for (int e = 0; e < 3; ++e) {
+          if (a == 1 && b == 1 && e == 1) continue;
+          m[a][b][e] = ((r.mask >> kk) & 1u) ? p : m[a][b][e];
+          ++kk;
+        }
+    float s1, s2, s3;
+    iwb_sums(m, s1, s2, s3);
+    const float sw = R::mul(l2, R::add(R::add(R::mul(s1, 0.25f), R::mul(s2, 0.125f)),
+                                       R::mul(s3, 0.0625f)));
+    const unsigned c = r.cls;
+    if (iwb_sw != nullptr && (__ldg(tab.pos + c) >> 31)) iwb_sw[i] = sw;
+    const float out = R::mul(__ldg(tab.a + c), R::sub(R::add(sw, R::mul(__ldg(tab.b + c), p)),
+                                                      R::mul(__ldg(tab.c + c), pp)));
+    Pp[i] = Sto::store(out);
+  }
+}
+
+// Ordered list of the nodes of planes 1..Z-2 whose class is flagged; *list
+// is allocated (stream-ordered) when there is at least one.
+int build_flagged_list(pfdtd_domain* d, const std::vector<uint8_t>& flag, int64_t** list,
+                       int64_t* count) {
+  *list = nullptr;
+  *count = 0;
+  if (std::find(flag.begin(), flag.end(), 1) == flag.end()) return PFDTD_OK;
+  cudaStream_t s = d->stream;
+  const int64_t begin = d->XY, end = d->N - d->XY;
+  if (end <= begin) return PFDTD_OK;
+  const int64_t blocks = (end - begin + kChunkNodes - 1) / kChunkNodes;
+  uint8_t* d_is = nullptr;
+  int* d_counts = nullptr;
+  PFDTD_CK(d->alloc((void**)&d_is, flag.size()));
+  PFDTD_CK(d->alloc((void**)&d_counts, sizeof(int) * (blocks + 1)));
+  PFDTD_CK(cudaMemcpyAsync(d_is, flag.data(), flag.size(), cudaMemcpyHostToDevice, s));
+  k_dif_count<<<(int)blocks, kListThreads, 0, s>>>(d->d_cls, d->cls_bytes, d_is, begin, end,
+                                                  d_counts);
+  count_launch();
+  std::vector<int> counts(blocks);
+  PFDTD_CK(cudaMemcpyAsync(counts.data(), d_counts, sizeof(int) * blocks, cudaMemcpyDeviceToHost, s));
+  PFDTD_CK(cudaStreamSynchronize(s));
+  std::vector<int> offsets(blocks);
+  int64_t total = 0;
+  for (int64_t b = 0; b < blocks; ++b) {
+    offsets[b] = (int)total;
+    total += counts[b];
+  }
+  if (total > 0) {
+    PFDTD_CK(cudaMemcpyAsync(d_counts, offsets.data(), sizeof(int) * blocks, cudaMemcpyHostToDevice, s));
+    PFDTD_CK(d->alloc((void**)list, sizeof(int64_t) * total));
+    k_dif_list<<<(int)blocks, kListThreads, 0, s>>>(d->d_cls, d->cls_bytes, d_is, begin, end,
+                                                   d_counts, *list);
+    count_launch();
+    PFDTD_CK(cudaGetLastError());
+  }
+  PFDTD_CK(cudaStreamSynchronize(s));
+  d->release(d_is);
+  d->release(d_counts);
+  *count = total;
+  return PFDTD_OK;
+}
+
 int grid_for(int64_t n) {
   return (int)std::max<int64_t>(1, std::min<int64_t>((n + 255) / 256, 152 * 16));
 }
@@ -288,33 +408,10 @@ int build_dif(pfdtd_domain* d, const std::vector<uint16_t>& keys,
     eval_dif_classes<float>(d, d->class_scheme, keys, main_tab, is_dif, t);
     tab_bytes.assign((uint8_t*)t.data(), (uint8_t*)(t.data() + t.size()));
   }
-  if (std::find(is_dif.begin(), is_dif.end(), 1) == is_dif.end()) return PFDTD_OK;
   cudaStream_t s = d->stream;
-  const int64_t begin = d->XY, end = d->N - d->XY;
-  const int64_t blocks = (end - begin + kChunkNodes - 1) / kChunkNodes;
-  uint8_t* d_is = nullptr;
-  int* d_counts = nullptr;
-  PFDTD_CK(d->alloc((void**)&d_is, is_dif.size()));
-  PFDTD_CK(d->alloc((void**)&d_counts, sizeof(int) * (blocks + 1)));
-  PFDTD_CK(cudaMemcpyAsync(d_is, is_dif.data(), is_dif.size(), cudaMemcpyHostToDevice, s));
-  k_dif_count<<<(int)blocks, kListThreads, 0, s>>>(d->d_cls, d->cls_bytes, d_is, begin, end, d_counts);
-  count_launch();
-  std::vector<int> counts(blocks);
-  PFDTD_CK(cudaMemcpyAsync(counts.data(), d_counts, sizeof(int) * blocks, cudaMemcpyDeviceToHost, s));
-  PFDTD_CK(cudaStreamSynchronize(s));
-  std::vector<int> offsets(blocks);
   int64_t total = 0;
-  for (int64_t b = 0; b < blocks; ++b) {
-    offsets[b] = (int)total;
-    total += counts[b];
-  }
+  if (int rc = build_flagged_list(d, is_dif, &d->d_dif_list, &total)) return rc;
   if (total > 0) {
-    PFDTD_CK(cudaMemcpyAsync(d_counts, offsets.data(), sizeof(int) * blocks, cudaMemcpyHostToDevice, s));
-    PFDTD_CK(d->alloc((void**)&d->d_dif_list, sizeof(int64_t) * total));
-    k_dif_list<<<(int)blocks, kListThreads, 0, s>>>(d->d_cls, d->cls_bytes, d_is, begin, end,
-                                                   d_counts, d->d_dif_list);
-    count_launch();
-    PFDTD_CK(cudaGetLastError());
     PFDTD_CK(d->alloc(&d->d_dif_tab, tab_bytes.size()));
     PFDTD_CK(cudaMemcpyAsync(d->d_dif_tab, tab_bytes.data(), tab_bytes.size(),
                              cudaMemcpyHostToDevice, s));
@@ -323,7 +420,8 @@ int build_dif(pfdtd_domain* d, const std::vector<uint16_t>& keys,
     PFDTD_CK(cudaMemsetAsync(d->d_dif_state, 0, sbytes, s));
     if (d->class_scheme == PFDTD_IWB && d->K == 1 && d->precision != PFDTD_F64) {
       // flag the DIF classes (bit 31 of the pos word, unused by the IWB
-      // kernels) so that the TMA update stores their sw for the DIF pass
+      // kernels) so that the TMA update or the closure pass stores their sw
+      // for the DIF pass
       const size_t n = keys.size(), as = d->arith_size();
       std::vector<uint32_t> pos(n);
       std::memcpy(pos.data(), main_tab.data() + 3 * n * as, n * sizeof(uint32_t));
@@ -333,12 +431,65 @@ int build_dif(pfdtd_domain* d, const std::vector<uint16_t>& keys,
                                cudaMemcpyHostToDevice, s));
       if (!d->d_iwb_sw) PFDTD_CK(d->alloc((void**)&d->d_iwb_sw, (size_t)d->N * sizeof(float)));
     }
+    PFDTD_CK(cudaStreamSynchronize(s));
   }
-  PFDTD_CK(cudaStreamSynchronize(s));
-  d->release(d_is);
-  d->release(d_counts);
   d->n_dif = total;
   return PFDTD_OK;
+}
+
+// The closure-node list of an IWB domain on the TMA path (one field per
+// node, FP32/FP16/BF16 storage): classes whose geometry code is >= 2.
+int build_iwb_closure(pfdtd_domain* d, const std::vector<uint16_t>& keys) {
+  if (d->d_iwb_closure) d->release(d->d_iwb_closure);
+  d->d_iwb_closure = nullptr;
+  d->n_iwb_closure = 0;
+  d->iwb_closure_ready = false;
+  if (d->class_scheme != PFDTD_IWB || d->K != 1 || d->precision == PFDTD_F64) return PFDTD_OK;
+  std::vector<uint8_t> flag(keys.size());
+  for (size_t i = 0; i < keys.size(); ++i) flag[i] = (keys[i] >> 8) >= 2 ? 1 : 0;
+  int64_t* list = nullptr;
+  int64_t n = 0;
+  if (int rc = build_flagged_list(d, flag, &list, &n)) return rc;
+  if (n > 0) {
+    cudaStream_t s = d->stream;
+    PFDTD_CK(d->alloc(&d->d_iwb_closure, sizeof(ClosureRec) * (size_t)n));
+    k_closure_records<<<grid_for(n), 256, 0, s>>>(list, n, d->d_cls, d->cls_bytes, d->d_iwb_mask,
+                                                  (ClosureRec*)d->d_iwb_closure);
+    count_launch();
+    PFDTD_CK(cudaGetLastError());
+    d->release(list);
+  }
+  d->n_iwb_closure = n;
+  d->iwb_closure_ready = true;
+  return PFDTD_OK;
+}
+
+template <typename S>
+int launch_closure_t(pfdtd_domain* d, const void* cur, void* past, cudaStream_t s) {
+  const int64_t n = d->n_iwb_closure;
+  const uint8_t* ctab = (const uint8_t*)d->d_ctab;
+  const int nc = d->n_classes;
+  ClassTab<float> tab{(const float*)ctab, (const float*)(ctab + (size_t)nc * 4),
+                      (const float*)(ctab + 2 * (size_t)nc * 4),
+                      (const uint32_t*)(ctab + 3 * (size_t)nc * 4), nc};
+  k_iwb_closure<S><<<grid_for(n), 256, 0, s>>>((const ClosureRec*)d->d_iwb_closure, n, tab,
+                                               (const S*)cur, (S*)past, d->X, d->XY,
+                                               (float)d->params[1],
+                                               d->n_dif > 0 ? d->d_iwb_sw : nullptr);
+  count_launch();
+  PFDTD_CK(cudaGetLastError());
+  return PFDTD_OK;
+}
+
+int launch_iwb_closure(pfdtd_domain* d, const void* cur, void* past, cudaStream_t s) {
+  if (!d->iwb_closure_ready) return fail(PFDTD_ERR_STATE, "IWB closure list not built");
+  if (d->n_iwb_closure <= 0) return PFDTD_OK;
+  switch (d->precision) {
+    case PFDTD_F32: return launch_closure_t<float>(d, cur, past, s);
+    case PFDTD_F16: return launch_closure_t<__half>(d, cur, past, s);
+    case PFDTD_BF16: return launch_closure_t<__nv_bfloat16>(d, cur, past, s);
+  }
+  return fail(PFDTD_ERR_UNSUPPORTED, "IWB closure pass needs FP32, FP16 or BF16 fields");
 }
 
 int launch_dif(pfdtd_domain* d, const void* cur, void* past, cudaStream_t s) {

@@ -410,7 +410,8 @@ int pfdtd_destroy(pfdtd_domain* d) {
   void* ptrs[] = {d->field_base[0], d->field_base[1], d->field_base[2], d->field_base[3], d->d_pos, d->d_mat, d->d_cls,
                   d->d_ctab, d->d_src_idx, d->d_src_mode, d->d_src_samples, d->d_rec_idx,
                   d->d_step, d->d_rec_out, d->d_err, d->d_dif_list, d->d_dif_tab,
-                  d->d_dif_state, d->d_iwb_mask, d->d_iwb_code, d->d_iwb_sw};
+                  d->d_dif_state, d->d_iwb_mask, d->d_iwb_code, d->d_iwb_sw,
+                  d->d_iwb_closure};
   for (void* p : ptrs)
     d->release(p);
   if (d->stream) cudaStreamDestroy(d->stream);

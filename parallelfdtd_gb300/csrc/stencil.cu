@@ -159,7 +159,7 @@ k_update_iwb(const C* __restrict__ cls, const uint32_t* __restrict__ mask,
     const A sw = R::mul(l2, R::add(R::add(R::mul(s1, (A)0.25), R::mul(s2, (A)0.125)),
                                    R::mul(s3, (A)0.0625)));
     const A out = R::mul(ca, R::sub(R::add(sw, R::mul(cb, v[1][1][1])), R::mul(cc, pp)));
-    Pp[idx] = St::store(out);
+    Pp[idx] = St::store(ca == (A)0 ? (A)0 : out);  // a node outside the room holds +0
 #pragma unroll
     for (int b = 0; b < 3; ++b)
 #pragma unroll
@@ -450,6 +450,8 @@ int build_classes(pfdtd_domain* d) {
   d->n_classes = n_classes;
   d->class_scheme = scheme;
   rc = build_dif(d, keys, tab);
+  if (rc != PFDTD_OK) return rc;
+  rc = build_iwb_closure(d, keys);
   if (rc != PFDTD_OK) return rc;
   rc = check_tb_faces(d);
   if (rc != PFDTD_OK) return rc;

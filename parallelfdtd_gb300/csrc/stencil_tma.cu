@@ -394,7 +394,11 @@ k_update_tma(const __grid_constant__ CUtensorMap map_cur, const __grid_constant_
       break;
     }
     if constexpr (SCHEME == 3) {
-      static_assert(Lay::MASK, "IWB tiles carry the closed-neighbour masks");
+      // MASK: the stage carries the closed-neighbour masks and a node next to
+      // a closed neighbour is updated here with the closure substitution.
+      // Without: every node takes the open sums, and a closure node (class
+      // flag bit 30) keeps P^{n-1} for the closure pass (k_iwb_closure) that
+      // follows, which also serves the DIF nodes' sw.
       if (active) {
         using R = Rn<float>;
         using St = Store<S>;
@@ -406,10 +410,11 @@ k_update_tma(const __grid_constant__ CUtensorMap map_cur, const __grid_constant_
         float n0[kVec], n1[kVec], n2[kVec];
         iwb_plane_sums<false, 2, S, Lay>(Pn, si, P, idx + XY, x, X, no_mask, cc0, n0, n1, n2);
         // the closed-neighbour masks of the thread's 4 nodes (stage of plane z)
-        const uint4 mk4 = *reinterpret_cast<const uint4*>(smem + sp_ * Lay::STAGE + Lay::MK_OFF +
-                                                          4 * ci);
+        uint4 mk4 = make_uint4(0u, 0u, 0u, 0u);
+        if constexpr (Lay::MASK)
+          mk4 = *reinterpret_cast<const uint4*>(smem + sp_ * Lay::STAGE + Lay::MK_OFF + 4 * ci);
         float s1[kVec], s2[kVec], s3[kVec];
-        if ((mk4.x | mk4.y | mk4.z | mk4.w) != 0u) {
+        if (Lay::MASK && (mk4.x | mk4.y | mk4.z | mk4.w) != 0u) {
           // next to a closed neighbour (walls, obstacle surfaces): the sums of
           // this node's substituted neighbourhood, plane by plane
           const uint32_t mk[kVec] = {mk4.x, mk4.y, mk4.z, mk4.w};
@@ -461,10 +466,13 @@ k_update_tma(const __grid_constant__ CUtensorMap map_cur, const __grid_constant_
           const float sw = R::mul((float)l2, R::add(R::add(R::mul(s1[e], 0.25f),
                                                            R::mul(s2[e], 0.125f)),
                                                     R::mul(s3[e], 0.0625f)));
-          if (iwb_sw != nullptr && (k.pos >> 31)) iwb_sw[idx + e] = sw;  // a DIF node
+          if (Lay::MASK && iwb_sw != nullptr && (k.pos >> 31)) iwb_sw[idx + e] = sw;  // a DIF node
           const float out = R::mul(k.a, R::sub(R::add(sw, R::mul(k.b, cc0[e])),
                                                R::mul(k.c, St::load(vpp.v[e]))));
-          res[e] = St::store(out);
+          // a closure node (maskless tiles) keeps P^{n-1} for the closure
+          // pass; a node outside the room (a = 0) holds +0
+          res[e] = (!Lay::MASK && ((k.pos >> 30) & 1u)) ? vpp.v[e]
+                                                         : St::store(k.a == 0.f ? 0.f : out);
         }
         stg4(Pp + idx, res);
 #pragma unroll
@@ -859,29 +867,46 @@ int launch_tma_s<double>(pfdtd_domain* d, const void* cur, void* past, cudaStrea
 }
 
 // IWB on the stage ring: FP32, FP16 and BF16 storage, one field per node,
-// tiles with the x halo in the box; every stage also carries the plane's
-// closed-neighbour masks.  Shapes (d->tma_tile for IWB, -1 auto): 0 = 64 x
-// 16 and 1 = 128 x 8 (288 threads, 8 stages), 2 = 128 x 4 (5 stages), and
-// 160-thread 64 x 8 tiles: 3 = 8 stages, three CTAs per SM (the default), 4 =
-// 6 stages, four CTAs, 5 = 5 stages, five CTAs (registers capped to fit, with
-// spills).  Measured on the 512 x 384 x 256 room, FP32: 248, 180 and 122 G
-// node-updates/s for shapes 3, 4 and 5.
-template <typename S, typename C, int TX, int TY, int NS, int MINB = 1>
+// tiles with the x halo in the box.  Shapes (d->tma_tile for IWB, -1 auto):
+// with the closed-neighbour masks in every stage and the closure computed in
+// the kernel: 0 = 64 x 16 and 1 = 128 x 8 (288 threads, 8 stages), 2 = 128 x
+// 4 (5 stages), and 160-thread 64 x 8 tiles: 3 = 8 stages, three CTAs per
+// SM, 4 = 6 stages, four CTAs, 5 = 5 stages, five CTAs (registers capped to
+// fit).  Without masks, every node takes the open sums in the kernel and the
+// closure nodes are updated by the sparse closure pass after it: 6 = 64 x 8,
+// 8 stages, four CTAs per SM, 7 = the same with three CTAs, 8 = 128 x 8 (288
+// threads), two CTAs (the default).  With masks a warp that holds one closure
+// node runs the substitution for all its lanes, and in the tiles along the x
+// walls that is every warp; the split keeps the streaming kernel on the open
+// path and leaves the ~2 % closure nodes to the gather pass.  Measured on the
+// 512 x 384 x 256 room, FP32 with third-order DIF walls (C3): shape 3 208 G,
+// 6 235 G, 8 249 G node-updates/s; without DIF, shape 8 317 G.
+template <typename S, typename C, int TX, int TY, int NS, int MINB = 1, bool MASK = true>
 int launch_iwb_l(pfdtd_domain* d, const void* cur, void* past, cudaStream_t s) {
-  return launch_tma_t<S, C, 3, Layout<S, C, TX, TY, NS, true, true, MINB>>(d, cur, past, s);
+  if constexpr (MASK) {
+    return launch_tma_t<S, C, 3, Layout<S, C, TX, TY, NS, true, true, MINB>>(d, cur, past, s);
+  } else {
+    if (!d->iwb_closure_ready) return fail(PFDTD_ERR_STATE, "IWB closure list not built");
+    if (int rc = launch_tma_t<S, C, 3, Layout<S, C, TX, TY, NS, true, false, MINB>>(d, cur, past, s))
+      return rc;
+    return launch_iwb_closure(d, cur, past, s);
+  }
 }
 
 template <typename S, typename C>
 int launch_iwb_c(pfdtd_domain* d, const void* cur, void* past, cudaStream_t s) {
   int tile = d->tma_tile;
-  if (tile < 0 || tile > 5) tile = 3;
+  if (tile < 0 || tile > 8) tile = 8;
   switch (tile) {
     case 0: return launch_iwb_l<S, C, 64, 16, 8>(d, cur, past, s);
     case 1: return launch_iwb_l<S, C, 128, 8, 8>(d, cur, past, s);
     case 2: return launch_iwb_l<S, C, 128, 4, 5>(d, cur, past, s);
+    case 3: return launch_iwb_l<S, C, 64, 8, 8, 3>(d, cur, past, s);
     case 4: return launch_iwb_l<S, C, 64, 8, 6, 4>(d, cur, past, s);
     case 5: return launch_iwb_l<S, C, 64, 8, 5, 5>(d, cur, past, s);
-    default: return launch_iwb_l<S, C, 64, 8, 8, 3>(d, cur, past, s);
+    case 7: return launch_iwb_l<S, C, 64, 8, 8, 3, false>(d, cur, past, s);
+    case 6: return launch_iwb_l<S, C, 64, 8, 8, 4, false>(d, cur, past, s);
+    default: return launch_iwb_l<S, C, 128, 8, 8, 2, false>(d, cur, past, s);
   }
 }
 
