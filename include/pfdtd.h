@@ -289,8 +289,8 @@ int pfdtd_set_kernel(pfdtd_domain* d, int variant);
  * same index picks the IWB shape: 0..5 carry the closed-neighbour masks and
  * compute the closure in the kernel (0 64x16, 1 128x8, 2 128x4, 3..5 64x8
  * with 3, 4, 5 CTAs per SM); 6..8 run the open sums in the kernel and a
- * sparse pass for the nodes with a closed neighbour (6 64x8 with 4 CTAs per
- * SM; 7 64x8 with 3; 8 128x8 with 2, the default). */
+ * sparse pass for the nodes with a closed neighbour (6 128x8 with 3 CTAs per
+ * SM, the default; 7 128x4 with 4; 8 128x8 with 2). */
 int pfdtd_set_tile(pfdtd_domain* d, int tile);
 int pfdtd_get_kernel(pfdtd_domain* d, int* variant);
 

@@ -873,14 +873,15 @@ int launch_tma_s<double>(pfdtd_domain* d, const void* cur, void* past, cudaStrea
 // 4 (5 stages), and 160-thread 64 x 8 tiles: 3 = 8 stages, three CTAs per
 // SM, 4 = 6 stages, four CTAs, 5 = 5 stages, five CTAs (registers capped to
 // fit).  Without masks, every node takes the open sums in the kernel and the
-// closure nodes are updated by the sparse closure pass after it: 6 = 64 x 8,
-// 8 stages, four CTAs per SM, 7 = the same with three CTAs, 8 = 128 x 8 (288
-// threads), two CTAs (the default).  With masks a warp that holds one closure
+// closure nodes are updated by the sparse closure pass after it: 6 = 128 x 8
+// (288 threads), 6 stages, three CTAs per SM (the default), 7 = 128 x 4 (160
+// threads), 8 stages, four CTAs, 8 = 128 x 8, 8 stages, two CTAs.  With masks a warp that holds one closure
 // node runs the substitution for all its lanes, and in the tiles along the x
 // walls that is every warp; the split keeps the streaming kernel on the open
 // path and leaves the ~2 % closure nodes to the gather pass.  Measured on the
 // 512 x 384 x 256 room, FP32 with third-order DIF walls (C3): shape 3 208 G,
-// 6 235 G, 8 249 G node-updates/s; without DIF, shape 8 317 G.
+// 6 267 G, 7 249 G, 8 249 G node-updates/s (64 x 8 without masks, four CTAs:
+// 235 G).
 template <typename S, typename C, int TX, int TY, int NS, int MINB = 1, bool MASK = true>
 int launch_iwb_l(pfdtd_domain* d, const void* cur, void* past, cudaStream_t s) {
   if constexpr (MASK) {
@@ -896,7 +897,7 @@ int launch_iwb_l(pfdtd_domain* d, const void* cur, void* past, cudaStream_t s) {
 template <typename S, typename C>
 int launch_iwb_c(pfdtd_domain* d, const void* cur, void* past, cudaStream_t s) {
   int tile = d->tma_tile;
-  if (tile < 0 || tile > 8) tile = 8;
+  if (tile < 0 || tile > 8) tile = 6;
   switch (tile) {
     case 0: return launch_iwb_l<S, C, 64, 16, 8>(d, cur, past, s);
     case 1: return launch_iwb_l<S, C, 128, 8, 8>(d, cur, past, s);
@@ -904,9 +905,9 @@ int launch_iwb_c(pfdtd_domain* d, const void* cur, void* past, cudaStream_t s) {
     case 3: return launch_iwb_l<S, C, 64, 8, 8, 3>(d, cur, past, s);
     case 4: return launch_iwb_l<S, C, 64, 8, 6, 4>(d, cur, past, s);
     case 5: return launch_iwb_l<S, C, 64, 8, 5, 5>(d, cur, past, s);
-    case 7: return launch_iwb_l<S, C, 64, 8, 8, 3, false>(d, cur, past, s);
-    case 6: return launch_iwb_l<S, C, 64, 8, 8, 4, false>(d, cur, past, s);
-    default: return launch_iwb_l<S, C, 128, 8, 8, 2, false>(d, cur, past, s);
+    case 7: return launch_iwb_l<S, C, 128, 4, 8, 4, false>(d, cur, past, s);
+    case 8: return launch_iwb_l<S, C, 128, 8, 8, 2, false>(d, cur, past, s);
+    default: return launch_iwb_l<S, C, 128, 8, 6, 3, false>(d, cur, past, s);
   }
 }
 
