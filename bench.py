@@ -196,12 +196,17 @@ def peak_hbm():
         return 6800.0, "fallback"
 
 
-def traffic_per_launch(prec, fields=1):
-    """DRAM bytes per update-kernel launch from the committed ncu summary."""
+def traffic_per_launch(prec, fields=1, scheme="forward"):
+    """DRAM bytes per update-kernel launch from the committed ncu summaries
+    (profiles/traffic.json); None where no capture of that kernel exists."""
     path = os.path.join(ROOT, "profiles", "traffic.json")
     try:
         with open(path) as f:
             t = json.load(f)
+        if scheme == "iwb":
+            return t.get(f"update_iwb_{prec}_bytes_per_launch") if fields == 1 else None
+        if scheme != "forward":
+            return None
         return t.get(f"update_{prec}_bytes_per_launch" if fields == 1 else
                      f"update_{prec}_k{fields}_bytes_per_launch")
     except Exception:
@@ -458,7 +463,11 @@ def main():
     achieved = algo_bytes / (kms * 1e-3) / 1e9
     effective = bpu * nodes * K * T / (kms * 1e-3) / 1e9
     peak, peak_kind = peak_hbm()
-    traffic = traffic_per_launch(prec, K)
+    traffic = traffic_per_launch(prec, K, a.scheme)
+    kernel_name = "k_update_" + d.kernel()
+    in_kernel_closure = os.environ.get("PFDTD_TMA_TILE", "-1").strip() in ("0", "1", "2", "3", "4", "5")
+    if a.scheme == "iwb" and d.kernel() == "tma" and not in_kernel_closure:
+        kernel_name += " + k_iwb_closure"  # the update of a step: both kernels, timed together
 
     # ---- end to end through the C ABI with host buffers ------------------------
     out_host = np.zeros((n_rec, S), dtype=np.float64 if prec == "f64" else np.float32)
@@ -523,7 +532,7 @@ def main():
             "e2e": e2e,
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                          "frac": achieved / peak, "traffic": traffic,
-                         "kernel": "k_update_" + d.kernel(), "kernel_ms": kms,
+                         "kernel": kernel_name, "kernel_ms": kms,
                          "algorithmic_bytes_per_launch": algo_bytes,
                          "steps_per_launch": T,
                          "effective_gbs": effective,
