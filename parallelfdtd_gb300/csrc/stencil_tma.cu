@@ -7,9 +7,13 @@
 //    kStages shared-memory stages; stage k holds the P^n plane z0-1+k of the
 //    CTA's tile with a one-row / 16-byte halo, and the P^{n-1} plane and class
 //    ids of plane z0+k-2 (the plane computed once P^n plane z+1 has arrived);
-//  * eight consumer warps compute plane z from stages z-1, z, z+1 and store
+//  * the consumer warps compute plane z from stages z-1, z, z+1 and store
 //    P^{n+1} straight to global memory; after a step the stage holding plane
 //    z-1 is released to the producer through an mbarrier;
+//  * the forward update of the 7-point scheme runs as packed f32x2 pairs
+//    (two fields of a node, or two adjacent x nodes) with every product an
+//    fma(x, y, -0) that the compiler cannot contract, so each element keeps
+//    the scalar operation order and rounding;
 //  * the tensor maps view each field as rows of the flat array (X wide,
 //    Y*Z rows), so the row above the last row of a plane is the first row of
 //    the next plane, exactly the flat +-X neighbour the reference reads; the
@@ -195,10 +199,13 @@ __device__ __forceinline__ void stg4(double* p, const double (&v)[4]) {
 // stage ring: the box's 16-byte x halo and one-row y halo hold every edge and
 // corner neighbour.  The scheme's canonical sums (iwb_sums) are built from
 // in-plane sums, so a thread computes the raw sums of each new plane z+1 once
-// and combines them with those of planes z-1 and z carried in registers; a
-// node with a closed neighbour recomputes its three planes with the closure
-// substitution.  Closure, order and rounding follow k_update_iwb
-// (stencil.cu) operation for operation.
+// and combines them with those of planes z-1 and z carried in registers.
+// With the closed-neighbour masks in the stage (tile shapes 0..5), a node
+// with a closed neighbour recomputes its three planes with the closure
+// substitution; without them (shapes 6..8, the default), such a node keeps
+// P^{n-1} here and the closure pass k_iwb_closure (dif.cu) updates it.
+// Closure, order and rounding follow k_update_iwb (stencil.cu) operation for
+// operation.
 // Canonical index (0..25) of neighbour (dz, dy, dx) = (a-1, b-1, c-1) in the
 // closed-neighbour mask: (a, b, c) in row-major order with the centre left out.
 __host__ __device__ constexpr int iwb_bit(int a, int b, int c) {
