@@ -104,6 +104,15 @@ uint64_t estimate_bytes(const pfdtd_request* r) {
   bool dif = false;
   for (int32_t f : r->dif_flags) dif |= f != 0;
   if (dif) b += (uint64_t)r->n_boundary * (K * 4 * as + 8);   // filter states + node list
+  if (r->scheme == PFDTD_IWB) {
+    b += 5 * N;  // closed-neighbour masks and geometry codes
+    if (K == 1 && r->precision != PFDTD_F64) {
+      // closure-node records (16 B; nodes closed only diagonally come on top
+      // of the face-boundary count, bounded here by the same number again)
+      b += 2 * (uint64_t)r->n_boundary * 16;
+      if (dif) b += 4 * N;  // the DIF nodes' neighbour sums, one float per node
+    }
+  }
   return b + (4u << 20);                                     // tables, graphs, scratch
 }
 

@@ -18,6 +18,17 @@ def test_request_bytes_estimate(built):
     assert r.bytes() > b + 2 * n * 4 * 4 - 1
 
 
+def test_request_bytes_iwb(built):
+    """IWB requests also hold the closed-neighbour masks and geometry codes
+    (5 B per node) and, with one field, the closure-node records."""
+    from parallelfdtd_gb300 import rooms
+    room = rooms.boxes_room((64, 48, 40), n_boxes=3, edge=(5, 10), n_materials=4, seed=3)
+    n = 64 * 48 * 40
+    f = Request(room.dims, 100, precision="f32", scheme="forward").set_voxels(room.bid, room.mat)
+    i = Request(room.dims, 100, precision="f32", scheme="iwb").set_voxels(room.bid, room.mat)
+    assert i.bytes() >= f.bytes() + 5 * n
+
+
 def test_request_validation(built):
     with pytest.raises(L.PfdtdError):
         Request((64, 48, 2), 100)
