@@ -496,6 +496,48 @@ def test_iwb_open_x_faces(gpu, O, prec, variant):
 
 
 @pytest.mark.parametrize("prec", ["f32", "bf16"])
+@pytest.mark.parametrize("shape", list(range(9)))
+def test_iwb_tile_shapes(gpu, O, prec, shape):
+    """Every IWB tile shape on the TMA path equals the oracle, with DIF walls:
+    shapes 0..5 run the closure inside the streaming kernel, 6..8 leave the
+    nodes with a closed neighbour to the closure pass (which hands the DIF
+    nodes' neighbour sums to the DIF pass).  The room is not a multiple of
+    the 64- or 128-node tiles in x or of the tile rows in y."""
+    from parallelfdtd_gb300 import materials
+    room = rooms.boxes_room((208, 44, 36), n_boxes=6, edge=(5, 12), n_materials=6, seed=16)
+    steps = 90
+    srcs = room.random_air_nodes(2, seed=1)
+    rec = room.random_air_nodes(4, seed=2)
+    pulse = rooms.gaussian_pulse(steps, 3.0)
+    params = default_params(scheme="iwb")
+    flags = np.array([m % 2 for m in range(6)], np.int32)
+    table = materials.dif_table(materials.positive_real_filters(6, 3, seed=2), 3)
+    with Domain(room.dims, prec) as d:
+        d.set_voxels(room.bid, room.mat, centred=True)
+        d.set_materials(room.admittance)
+        d.set_params(params)
+        d.set_scheme("iwb")
+        d.set_dif_filters(flags, table)
+        d.set_kernel("tma")
+        L.call("pfdtd_set_tile", d.handle, shape)
+        d.set_sources(srcs, [1, 1], np.stack([pulse, -0.5 * pulse]))
+        d.set_receivers(rec)
+        g, _, _ = d.run(steps)
+        assert d.kernel() == "tma"
+        P = d.download_field(L.FIELD_CURRENT)
+    pos, mat = O.encode_nodes(room.bid, room.mat, True)
+    r, rP, _ = O.run(pos, mat, room.dims, room.admittance, params, [room.flat(*s) for s in srcs],
+                     [1, 1], np.stack([pulse, -0.5 * pulse]), [room.flat(*x) for x in rec], steps,
+                     scheme=3, storage=(prec if prec == "bf16" else None), dif=(flags, table))
+    assert np.abs(r).max() > 1e-4
+    assert np.array_equal(g, r)
+    if prec == "bf16":
+        assert np.array_equal(P.view(np.uint16), rP.view(np.uint16))
+    else:
+        assert np.array_equal(P, rP)
+
+
+@pytest.mark.parametrize("prec", ["f32", "bf16"])
 def test_iwb_below_the_stability_limit(gpu, O, prec):
     """IWB at lambda = 0.95 (weights lambda^2 (1/4, 1/8, 1/16), centre
     2 - 7/2 lambda^2) with frequency-dependent walls: equal to the oracle."""
