@@ -108,3 +108,27 @@ def test_float_close_to_double(O):
     f, _, _ = O.run(*args, scheme=3)
     d, _, _ = O.run(*args, scheme=3, double=True)
     assert np.linalg.norm(f - d) / np.linalg.norm(d) < 1e-3
+
+
+def test_nodes_outside_the_room_hold_plus_zero(O):
+    """A node without the inside bit stores +0 every step (its update would be
+    0 times a finite value, whose zero sign depends on neighbours no inside
+    node reads); inside nodes are unaffected."""
+    room = rooms.boxes_room((40, 32, 28), n_boxes=4, edge=(4, 10), n_materials=5, seed=9)
+    pos, mat = O.encode_nodes(room.bid, room.mat, True)
+    steps = 40
+    pulse = rooms.gaussian_pulse(steps, 3.0)
+    src = room.random_air_nodes(1, seed=1)
+    for double in (False, True):
+        _, P, Pp = O.run(pos, mat, room.dims, room.admittance, iwb_params(), [room.flat(*src[0])],
+                         [1], pulse[None], [], steps, scheme=3, double=double)
+        X, Y, Z = room.dims
+        outside = (pos & 0x80) == 0
+        planes = np.zeros((Z, Y, X), bool)
+        planes[1:-1] = True  # planes 0 and Z-1 are never updated
+        sel = (outside & planes.reshape(-1))
+        for F in (P, Pp):
+            v = np.asarray(F).reshape(-1)[sel]
+            assert np.all(v == 0) and not np.any(np.signbit(v))
+        inside = ~outside & planes.reshape(-1)
+        assert np.abs(np.asarray(P).reshape(-1)[inside]).max() > 1e-6
