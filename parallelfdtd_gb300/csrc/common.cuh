@@ -27,6 +27,11 @@ int cuda_fail(cudaError_t e, const char* what, const char* file, int line);
     if (e_ != cudaSuccess) return ::pfdtd::cuda_fail(e_, #call, __FILE__, __LINE__); \
   } while (0)
 
+// GB300's SM count: the grid-stride kernels launch at most a small multiple
+// of it (any grid size is correct; this one keeps every SM busy without
+// oversubscribing).
+constexpr int kGridSMs = 152;
+
 extern std::atomic<int64_t> g_launches;
 inline void count_launch(int64_t n = 1) { g_launches.fetch_add(n, std::memory_order_relaxed); }
 

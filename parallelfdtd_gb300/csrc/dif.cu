@@ -301,7 +301,7 @@ int build_flagged_list(pfdtd_domain* d, const std::vector<uint8_t>& flag, int64_
 }
 
 int grid_for(int64_t n) {
-  return (int)std::max<int64_t>(1, std::min<int64_t>((n + 255) / 256, 152 * 16));
+  return (int)std::max<int64_t>(1, std::min<int64_t>((n + 255) / 256, kGridSMs * 16));
 }
 
 template <typename A>

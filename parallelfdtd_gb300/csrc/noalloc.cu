@@ -97,7 +97,7 @@ extern "C" int pfdtd_capture_slice_noalloc(pfdtd_domain* d, int orientation, int
   if (rc == PFDTD_OK) {
     float* dp = (float*)scratch;
     uint8_t* dq = (uint8_t*)scratch + (size_t)kNoAllocMaxSliceNodes * sizeof(float);
-    const int grid = (int)std::max<int64_t>(1, std::min<int64_t>((n + 255) / 256, 152 * 16));
+    const int grid = (int)std::max<int64_t>(1, std::min<int64_t>((n + 255) / 256, kGridSMs * 16));
     cudaStream_t s = d->stream;
     const void* cur = d->cur_field();
     const int X = (int)d->X, Y = (int)d->Y, Z = (int)d->Z;

@@ -86,7 +86,7 @@ int resample_t(const T* x, int64_t n_ch, int64_t n_in, const double* h, int nh, 
   if (e == cudaSuccess) e = cudaMemcpyAsync(dh, h, sizeof(double) * nh, cudaMemcpyHostToDevice, s);
   if (e == cudaSuccess) {
     const int64_t tot = n_ch * n_out;
-    const int grid = (int)std::max<int64_t>(1, std::min<int64_t>((tot + 255) / 256, 152 * 32));
+    const int grid = (int)std::max<int64_t>(1, std::min<int64_t>((tot + 255) / 256, kGridSMs * 32));
     k_resample<T><<<grid, 256, 0, s>>>(dx, n_ch, n_in, dh, nh, up, down, offset, n_out, dy);
     count_launch();
     e = cudaGetLastError();
@@ -123,7 +123,7 @@ int post_filter_t(const T* x, int64_t n_ch, int64_t n, const double* b, int nb, 
   if (e == cudaSuccess) e = cudaMemcpyAsync(db, b, sizeof(double) * nb, cudaMemcpyHostToDevice, s);
   if (e == cudaSuccess) {
     const int64_t tot = n_ch * n;
-    const int grid = (int)std::max<int64_t>(1, std::min<int64_t>((tot + 255) / 256, 152 * 32));
+    const int grid = (int)std::max<int64_t>(1, std::min<int64_t>((tot + 255) / 256, kGridSMs * 32));
     k_fir<T><<<grid, 256, 0, s>>>(dx, n_ch, n, db, nb, dy);
     count_launch();
     if (dc) {

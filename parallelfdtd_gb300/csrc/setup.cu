@@ -102,7 +102,7 @@ __global__ void k_slice(const S* __restrict__ P, const uint8_t* __restrict__ pos
   }
 }
 
-int grid_for(int64_t n) { return (int)std::max<int64_t>(1, std::min<int64_t>((n + 255) / 256, 152 * 16)); }
+int grid_for(int64_t n) { return (int)std::max<int64_t>(1, std::min<int64_t>((n + 255) / 256, kGridSMs * 16)); }
 
 struct DevGuard {
   int prev = -1;

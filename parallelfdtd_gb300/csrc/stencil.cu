@@ -390,7 +390,7 @@ int build_classes(pfdtd_domain* d) {
           d->alloc((void**)&d->d_iwb_code, (size_t)d->N) != cudaSuccess)
         return fail(PFDTD_ERR_NOMEM, "IWB geometry allocation failed");
     }
-    const int64_t gb = std::min<int64_t>((d->N + 255) / 256, 152 * 32);
+    const int64_t gb = std::min<int64_t>((d->N + 255) / 256, kGridSMs * 32);
     k_iwb_geometry<<<(int)gb, 256, 0, s>>>(d->d_pos, d->N, d->X, d->XY, d->d_iwb_mask,
                                            d->d_iwb_code);
     count_launch();
@@ -399,7 +399,7 @@ int build_classes(pfdtd_domain* d) {
   }
   const int64_t begin = d->XY, end = d->N - d->XY;
   if (end > begin) {
-    const int64_t blocks = std::min<int64_t>((end - begin + 255) / 256, 152 * 32);
+    const int64_t blocks = std::min<int64_t>((end - begin + 255) / 256, kGridSMs * 32);
     k_key_presence<<<(int)blocks, 256, 0, s>>>(key_bytes, d->d_mat, begin, end, d_present);
     count_launch();
     PFDTD_CK(cudaGetLastError());
@@ -436,7 +436,7 @@ int build_classes(pfdtd_domain* d) {
   uint16_t* d_lut = nullptr;
   PFDTD_CK(cudaMallocAsync((void**)&d_lut, 65536 * sizeof(uint16_t), s));
   PFDTD_CK(cudaMemcpyAsync(d_lut, lut.data(), 65536 * sizeof(uint16_t), cudaMemcpyHostToDevice, s));
-  const int64_t blocks = std::min<int64_t>((d->N + 255) / 256, 152 * 32);
+  const int64_t blocks = std::min<int64_t>((d->N + 255) / 256, kGridSMs * 32);
   if (cls_bytes == 1)
     k_map_classes<uint8_t><<<(int)blocks, 256, 0, s>>>(key_bytes, d->d_mat, d->N, d_lut,
                                                         (uint8_t*)d->d_cls);

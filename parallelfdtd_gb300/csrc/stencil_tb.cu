@@ -47,7 +47,7 @@ int check_tb_faces(pfdtd_domain* d) {
   cudaStream_t s = d->stream;
   PFDTD_CK(cudaMallocAsync((void**)&dc, sizeof(unsigned long long), s));
   PFDTD_CK(cudaMemsetAsync(dc, 0, sizeof(unsigned long long), s));
-  k_face_inside<<<152, 256, 0, s>>>(d->d_pos, (int)d->X, (int)d->Y, (int)d->Z, dc);
+  k_face_inside<<<kGridSMs, 256, 0, s>>>(d->d_pos, (int)d->X, (int)d->Y, (int)d->Z, dc);
   count_launch();
   PFDTD_CK(cudaGetLastError());
   unsigned long long h = 1;

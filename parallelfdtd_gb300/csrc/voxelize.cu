@@ -255,7 +255,7 @@ __global__ void k_ids(const uint8_t* __restrict__ solid, const uint8_t* __restri
   }
 }
 
-int grid_n(int64_t n) { return (int)std::max<int64_t>(1, std::min<int64_t>((n + 255) / 256, 152 * 32)); }
+int grid_n(int64_t n) { return (int)std::max<int64_t>(1, std::min<int64_t>((n + 255) / 256, kGridSMs * 32)); }
 
 }  // namespace
 }  // namespace pfdtd
