@@ -338,3 +338,49 @@ class Domain:
         s = C.c_void_p()
         L.call("pfdtd_get_stream", self.handle, C.byref(s))
         return s.value or 0
+
+
+def autotune_fields(dims: Sequence[int], setup: Callable[["Domain"], None], precision="f32",
+                    candidates: Sequence[int] = (1, 4, 8, 16, 32), max_depth: int = 3,
+                    iters: int = 10, device: int = 0, memory_fraction: float = 0.8):
+    """Pick the number of batched fields K for many sources in one room.
+
+    Sources in the same room can run as K fields of one domain sharing the
+    geometry, the class ids and the coefficient table (one run per K sources).
+    For every candidate K whose fields fit in `memory_fraction` of the
+    device's free memory, a K-field domain is created and prepared by
+    `setup(domain)` (geometry, materials, parameters, scheme), and
+    Domain.autotune times its per-step kernel and every blocked (depth <=
+    max_depth, tile shape) configuration and keeps the fastest.  The rate is
+    field-updates per second, X*Y*(Z-2)*K per step.
+
+    Returns (K, depth, shape, rates): the K with the highest rate, its kernel
+    configuration (depth 0 = per step), and {K: (rate, depth, shape)} for
+    every candidate timed.  No counterpart in the reference, which runs one
+    source set per simulation.
+    """
+    X, Y, Z = (int(v) for v in dims)
+    esize = {L.F32: 4, L.F64: 8, L.F16: 2, L.BF16: 2}[precision_code(precision)]
+    free = None
+    try:
+        import torch
+        if torch.cuda.is_available():
+            free = torch.cuda.mem_get_info(device)[0]
+    except Exception:
+        free = None
+    rates = {}
+    for K in candidates:
+        K = int(K)
+        if K != 1 and (K % 4 != 0 or K & (K - 1)):
+            raise ValueError("candidate field counts are 1 or powers of two from 4")
+        need = (4 if max_depth >= 2 else 2) * X * Y * Z * K * esize + 2 * X * Y * Z
+        if free is not None and need > memory_fraction * free:
+            continue
+        with Domain((X, Y, Z), precision, device=device, fields=K) as d:
+            setup(d)
+            depth, shape, ms = d.autotune(max_depth=max_depth, iters=iters)
+        rates[K] = (X * Y * (Z - 2) * K / (ms * 1e-3), depth, shape)
+    if not rates:
+        raise RuntimeError("no candidate field count fits in device memory")
+    best = max(rates, key=lambda k: rates[k][0])
+    return best, rates[best][1], rates[best][2], rates

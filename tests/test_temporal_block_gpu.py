@@ -219,6 +219,28 @@ def test_autotune_restores_fields_and_keeps_results(gpu):
         assert np.array_equal(values(d.download_field(L.FIELD_CURRENT), "f32"), P0)
 
 
+def test_autotune_fields(gpu):
+    """The field-count autotuner times every candidate K on the same room
+    (each with its own best kernel configuration) and returns the K with the
+    highest field-update rate."""
+    from parallelfdtd_gb300.domain import autotune_fields
+    room = rooms.boxes_room((128, 96, 64), n_boxes=5, edge=(6, 16), n_materials=6, seed=35)
+
+    def setup(d):
+        d.set_voxels(room.bid, room.mat, centred=False)
+        d.set_materials(room.admittance)
+        d.set_params(default_params())
+        d.set_scheme("forward")
+
+    K, depth, shape, rates = autotune_fields(room.dims, setup, "f32", candidates=(1, 4, 16),
+                                             max_depth=3, iters=3)
+    assert set(rates) == {1, 4, 16}
+    assert K in rates and rates[K][0] == max(r[0] for r in rates.values())
+    assert (depth, shape) == rates[K][1:]
+    assert all(r[0] > 0 and r[1] in (0, 2, 3) for r in rates.values())
+    print("field-update rates (G/s):", {k: round(v[0] / 1e9, 1) for k, v in rates.items()})
+
+
 @pytest.mark.parametrize("prec", ["f32", "f16"])
 def test_blocked_then_per_step_on_the_other_buffer_pair(gpu, prec):
     """A run whose blocked launches end on the second buffer pair and then
