@@ -54,3 +54,4 @@ def test_serving_trace_is_seeded_and_bounded():
     assert steps.min() >= 500 and steps.max() <= 8000
     srcs = np.array([t.n_src for t in a])
     assert srcs.min() >= 1 and srcs.max() <= 16
+
