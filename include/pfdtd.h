@@ -193,7 +193,10 @@ int pfdtd_run_device(pfdtd_domain* d, int64_t steps, void* d_out);
 
 /* Queue `iters` update-kernel launches alone (no sources, no receivers),
  * swapping the fields after each, on the domain's stream; no synchronisation.
- * Used to time the update kernel with events recorded around it. */
+ * Used to time the update kernel with events recorded around it.  The fields
+ * advance (for IWB with frequency-dependent walls on the TMA path, so do the
+ * filter states, which the closure pass updates); pfdtd_reset_fields gives a
+ * clean start again. */
 int pfdtd_profile_update(pfdtd_domain* d, int iters);
 
 /* One step in capture mode (launchFDTD3dStep, kernels3d.cu:376-482): inject

@@ -176,6 +176,7 @@ struct TmaState {
 struct GraphCache {
   cudaGraphExec_t exec = nullptr;
   int64_t key[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+  int64_t launches = 0;  // kernels in one replay (counted while capturing)
 };
 
 }  // namespace pfdtd
@@ -231,6 +232,10 @@ struct pfdtd_domain {
   // these nodes and k_iwb_closure updates them.
   void* d_iwb_closure = nullptr;
   int64_t n_iwb_closure = 0;
+  // per closure record: its DIF node slot (position in the DIF list), -1 for
+  // a node without a filter; set when every DIF node has a record, and then
+  // the closure pass also applies the DIF update (no separate DIF pass)
+  int32_t* d_iwb_closure_dif = nullptr;
   bool iwb_closure_ready = false;
   int64_t class_version = 0;
 
@@ -308,6 +313,9 @@ int launch_dif(pfdtd_domain* d, const void* cur, void* past, cudaStream_t s);
 int launch_dif_init(pfdtd_domain* d, cudaStream_t s);
 int build_iwb_closure(pfdtd_domain* d, const std::vector<uint16_t>& keys);
 int launch_iwb_closure(pfdtd_domain* d, const void* cur, void* past, cudaStream_t s);
+// Implemented in stencil_tma.cu: whether the next update runs the IWB
+// closure pass with the DIF update fused into it
+bool iwb_closure_fuses_dif(const pfdtd_domain* d);
 // Implemented in setup.cu
 int launch_slice_gather(pfdtd_domain* d, int orientation, int64_t slice, float* dp, uint8_t* dq,
                         cudaStream_t s);

@@ -213,11 +213,36 @@ __global__ void k_closure_records(const int64_t* __restrict__ list, int64_t n,
   }
 }
 
+// dif_slot (optional): per record the node's position in the DIF list, -1
+// for a node without a filter.  A DIF node then takes the DIF update here,
+// operation for operation as k_dif_update with the same sw (and its filter
+// state at dstate + 4 * slot), instead of the FI rule and the separate pass.
+// For each DIF node (flat index order), the record holding it: a binary
+// search in the records' ascending indices.  A DIF node without a record
+// (none is expected: a DIF node has a closed face neighbour) is counted.
+__global__ void k_closure_dif_slots(const int64_t* __restrict__ dif_list, int64_t n_dif,
+                                    const ClosureRec* __restrict__ recs, int64_t n_rec,
+                                    int32_t* __restrict__ slot, unsigned* __restrict__ missing) {
+  for (int64_t k = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; k < n_dif;
+       k += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t node = dif_list[k];
+    int64_t lo = 0, hi = n_rec;
+    while (lo < hi) {
+      const int64_t mid = lo + (hi - lo) / 2;
+      if (recs[mid].idx < node) lo = mid + 1;
+      else hi = mid;
+    }
+    if (lo < n_rec && recs[lo].idx == node) slot[lo] = (int32_t)k;
+    else atomicAdd(missing, 1u);
+  }
+}
+
 template <typename S>
 __global__ void __launch_bounds__(256)
 k_iwb_closure(const ClosureRec* __restrict__ recs, int64_t n, ClassTab<float> tab,
               const S* __restrict__ P, S* __restrict__ Pp, int64_t X, int64_t XY, float l2,
-              float* __restrict__ iwb_sw) {
+              float* __restrict__ iwb_sw, const int32_t* __restrict__ dif_slot,
+              const float* __restrict__ dtab, float* __restrict__ dstate) {
   using R = Rn<float>;
   using Sto = Store<S>;
   for (int64_t k = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; k < n;
@@ -250,6 +275,23 @@ k_iwb_closure(const ClosureRec* __restrict__ recs, int64_t n, ClassTab<float> ta
     const float sw = R::mul(l2, R::add(R::add(R::mul(s1, 0.25f), R::mul(s2, 0.125f)),
                                        R::mul(s3, 0.0625f)));
     const unsigned c = r.cls;
+    const int32_t slot = dif_slot != nullptr ? dif_slot[k] : -1;
+    if (slot >= 0) {
+      const float* t = dtab + (int64_t)kDifClassVals * c;
+      float* st = dstate + 4 * (int64_t)slot;
+      const float s1d = st[0], ppd = st[3];
+      const float num = R::sub(R::sub(R::add(sw, R::mul(t[1], p)), R::mul(t[2], ppd)),
+                               R::mul(t[3], s1d));
+      const float out = R::mul(t[0], num);
+      const float xx = R::mul(R::sub(out, ppd), 0.5f);
+      const float yy = R::add(R::mul(t[4], xx), s1d);
+      st[0] = R::add(R::sub(R::mul(t[5], xx), R::mul(t[8], yy)), st[1]);
+      st[1] = R::add(R::sub(R::mul(t[6], xx), R::mul(t[9], yy)), st[2]);
+      st[2] = R::sub(R::mul(t[7], xx), R::mul(t[10], yy));
+      st[3] = p;
+      Pp[i] = Sto::store(out);
+      continue;
+    }
     if (iwb_sw != nullptr && (__ldg(tab.pos + c) >> 31)) iwb_sw[i] = sw;
     const float out = R::mul(__ldg(tab.a + c), R::sub(R::add(sw, R::mul(__ldg(tab.b + c), p)),
                                                       R::mul(__ldg(tab.c + c), pp)));
@@ -442,6 +484,8 @@ int build_dif(pfdtd_domain* d, const std::vector<uint16_t>& keys,
 int build_iwb_closure(pfdtd_domain* d, const std::vector<uint16_t>& keys) {
   if (d->d_iwb_closure) d->release(d->d_iwb_closure);
   d->d_iwb_closure = nullptr;
+  if (d->d_iwb_closure_dif) d->release(d->d_iwb_closure_dif);
+  d->d_iwb_closure_dif = nullptr;
   d->n_iwb_closure = 0;
   d->iwb_closure_ready = false;
   if (d->class_scheme != PFDTD_IWB || d->K != 1 || d->precision == PFDTD_F64) return PFDTD_OK;
@@ -458,6 +502,26 @@ int build_iwb_closure(pfdtd_domain* d, const std::vector<uint16_t>& keys) {
     count_launch();
     PFDTD_CK(cudaGetLastError());
     d->release(list);
+    if (d->n_dif > 0 && d->n_dif < ((int64_t)1 << 31) && d->d_dif_list) {
+      // the DIF slot of every record, so that the closure pass applies the
+      // DIF update itself; kept only if every DIF node has a record
+      int32_t* slot = nullptr;
+      unsigned* d_missing = nullptr;
+      PFDTD_CK(d->alloc((void**)&slot, sizeof(int32_t) * (size_t)n));
+      PFDTD_CK(d->alloc((void**)&d_missing, sizeof(unsigned)));
+      PFDTD_CK(cudaMemsetAsync(slot, 0xFF, sizeof(int32_t) * (size_t)n, s));
+      PFDTD_CK(cudaMemsetAsync(d_missing, 0, sizeof(unsigned), s));
+      k_closure_dif_slots<<<grid_for(d->n_dif), 256, 0, s>>>(
+          d->d_dif_list, d->n_dif, (const ClosureRec*)d->d_iwb_closure, n, slot, d_missing);
+      count_launch();
+      PFDTD_CK(cudaGetLastError());
+      unsigned missing = 1;
+      PFDTD_CK(cudaMemcpyAsync(&missing, d_missing, sizeof(unsigned), cudaMemcpyDeviceToHost, s));
+      PFDTD_CK(cudaStreamSynchronize(s));
+      d->release(d_missing);
+      if (missing == 0) d->d_iwb_closure_dif = slot;
+      else d->release(slot);
+    }
   }
   d->n_iwb_closure = n;
   d->iwb_closure_ready = true;
@@ -472,10 +536,12 @@ int launch_closure_t(pfdtd_domain* d, const void* cur, void* past, cudaStream_t 
   ClassTab<float> tab{(const float*)ctab, (const float*)(ctab + (size_t)nc * 4),
                       (const float*)(ctab + 2 * (size_t)nc * 4),
                       (const uint32_t*)(ctab + 3 * (size_t)nc * 4), nc};
-  k_iwb_closure<S><<<grid_for(n), 256, 0, s>>>((const ClosureRec*)d->d_iwb_closure, n, tab,
-                                               (const S*)cur, (S*)past, d->X, d->XY,
-                                               (float)d->params[1],
-                                               d->n_dif > 0 ? d->d_iwb_sw : nullptr);
+  const bool fuse = iwb_closure_fuses_dif(d);
+  k_iwb_closure<S><<<grid_for(n), 256, 0, s>>>(
+      (const ClosureRec*)d->d_iwb_closure, n, tab, (const S*)cur, (S*)past, d->X, d->XY,
+      (float)d->params[1], (d->n_dif > 0 && !fuse) ? d->d_iwb_sw : nullptr,
+      fuse ? d->d_iwb_closure_dif : nullptr, fuse ? (const float*)d->d_dif_tab : nullptr,
+      fuse ? (float*)d->d_dif_state : nullptr);
   count_launch();
   PFDTD_CK(cudaGetLastError());
   return PFDTD_OK;
@@ -494,6 +560,7 @@ int launch_iwb_closure(pfdtd_domain* d, const void* cur, void* past, cudaStream_
 
 int launch_dif(pfdtd_domain* d, const void* cur, void* past, cudaStream_t s) {
   if (d->n_dif <= 0) return PFDTD_OK;
+  if (iwb_closure_fuses_dif(d)) return PFDTD_OK;  // the closure pass applied it
   switch (d->precision) {
     case PFDTD_F32: return launch_dif_t<float>(d, cur, past, s);
     case PFDTD_F64: return launch_dif_t<double>(d, cur, past, s);

@@ -141,7 +141,11 @@ int get_chunk_graph(pfdtd_domain* d, void* rec_out, int64_t rec_ld, int64_t inje
                     cudaGraphExec_t* exec) {
   const int tb = tb_active(d) ? d->tb_depth : 0;
   const int64_t chunk = tb ? kChunkTb : kChunk;
-  const int64_t key[8] = {d->cur * 16 + d->prev * 4 + tb, chunk, d->class_version, d->io_version,
+  // the kernels a chunk launches depend on the variant and the tile shape
+  // too (an IWB shape decides whether a DIF pass follows the update)
+  const int64_t cfg = chunk | ((int64_t)(d->tma_tile + 1) << 8) |
+                      ((int64_t)d->kernel_variant << 16) | ((int64_t)(d->tb_shape + 1) << 24);
+  const int64_t key[8] = {d->cur * 16 + d->prev * 4 + tb, cfg, d->class_version, d->io_version,
                           (int64_t)(intptr_t)rec_out, rec_ld, inject_end,
                           (int64_t)(intptr_t)d->d_cls};
   if (d->graph.exec && std::memcmp(key, d->graph.key, sizeof(key)) == 0) {
@@ -164,6 +168,7 @@ int get_chunk_graph(pfdtd_domain* d, void* rec_out, int64_t rec_ld, int64_t inje
     for (int64_t i = 0; i < chunk && rc == PFDTD_OK; ++i)
       rc = enqueue_step(d, rec_out, rec_ld, inject_end, s);
   }
+  const int64_t captured = g_launches.load() - before;
   g_launches.store(before);  // captured, not launched
   d->cur = cur0;
   d->prev = prev0;
@@ -178,6 +183,7 @@ int get_chunk_graph(pfdtd_domain* d, void* rec_out, int64_t rec_ld, int64_t inje
   cudaGraphDestroy(graph);
   if (e != cudaSuccess) return cuda_fail(e, "cudaGraphInstantiate", __FILE__, __LINE__);
   std::memcpy(d->graph.key, key, sizeof(key));
+  d->graph.launches = captured;
   *exec = d->graph.exec;
   return PFDTD_OK;
 }
@@ -249,7 +255,7 @@ int enqueue_run(pfdtd_domain* d, int64_t steps, void* rec_out, F&& between, bool
     if (rc) break;
     cudaError_t e = cudaGraphLaunch(exec, s);
     if (e != cudaSuccess) { rc = cuda_fail(e, "cudaGraphLaunch", __FILE__, __LINE__); break; }
-    count_launch(tb ? 2 * (chunk / tb) : 2 * chunk);
+    count_launch(d->graph.launches);
     e = cudaEventRecord(ev[k % 2], s);
     if (e != cudaSuccess) { rc = cuda_fail(e, "cudaEventRecord", __FILE__, __LINE__); break; }
     queued += chunk;
@@ -285,7 +291,7 @@ int enqueue_steps(pfdtd_domain* d, int64_t n, void* rec_out, int64_t rec_ld, int
     cudaGraphExec_t exec = nullptr;
     if (int rc = get_chunk_graph(d, rec_out, rec_ld, inject_end, &exec)) return rc;
     PFDTD_CK(cudaGraphLaunch(exec, s));
-    count_launch(tb ? 2 * (chunk / tb) : 2 * chunk);
+    count_launch(d->graph.launches);
   }
   for (; tb && done + tb <= n; done += tb)
     if (int rc = launch_tb(d, rec_out, rec_ld, inject_end, s)) return rc;
@@ -411,7 +417,7 @@ int pfdtd_destroy(pfdtd_domain* d) {
                   d->d_ctab, d->d_src_idx, d->d_src_mode, d->d_src_samples, d->d_rec_idx,
                   d->d_step, d->d_rec_out, d->d_err, d->d_dif_list, d->d_dif_tab,
                   d->d_dif_state, d->d_iwb_mask, d->d_iwb_code, d->d_iwb_sw,
-                  d->d_iwb_closure};
+                  d->d_iwb_closure, d->d_iwb_closure_dif};
   for (void* p : ptrs)
     d->release(p);
   if (d->stream) cudaStreamDestroy(d->stream);
@@ -1127,6 +1133,19 @@ int pfdtd_autotune(pfdtd_domain* d, int max_depth, int iters, int* best_depth, i
   }
   PFDTD_CK(cudaMemcpyAsync(keep[0], d->field_base[d->cur], fbytes, cudaMemcpyDeviceToDevice, s));
   PFDTD_CK(cudaMemcpyAsync(keep[1], d->field_base[d->prev], fbytes, cudaMemcpyDeviceToDevice, s));
+  // the IWB closure pass also advances the DIF filter states: keep them too
+  void* keep_dif = nullptr;
+  const size_t dbytes = d->n_dif > 0 ? (size_t)d->n_dif * d->K * 4 * d->arith_size() : 0;
+  if (dbytes) {
+    if (cudaMallocAsync(&keep_dif, dbytes, s) != cudaSuccess) {
+      cudaGetLastError();
+      cudaFreeAsync(keep[0], s);
+      cudaFreeAsync(keep[1], s);
+      d->tb_depth = depth0;
+      return fail(PFDTD_ERR_NOMEM, "autotune filter-state snapshot allocation failed");
+    }
+    PFDTD_CK(cudaMemcpyAsync(keep_dif, d->d_dif_state, dbytes, cudaMemcpyDeviceToDevice, s));
+  }
   double best = 1e300;
   int bd = 0, bs = -1;
   struct Cand { int depth, shape; };
@@ -1155,10 +1174,13 @@ int pfdtd_autotune(pfdtd_domain* d, int max_depth, int iters, int* best_depth, i
                                     cudaMemcpyDeviceToDevice, s);
     if (e == cudaSuccess)
       e = cudaMemcpyAsync(d->field_base[d->prev], keep[1], fbytes, cudaMemcpyDeviceToDevice, s);
+    if (e == cudaSuccess && keep_dif)
+      e = cudaMemcpyAsync(d->d_dif_state, keep_dif, dbytes, cudaMemcpyDeviceToDevice, s);
     if (e != cudaSuccess) rc = cuda_fail(e, "autotune field restore", __FILE__, __LINE__);
   }
   cudaFreeAsync(keep[0], s);
   cudaFreeAsync(keep[1], s);
+  if (keep_dif) cudaFreeAsync(keep_dif, s);
   cudaError_t e = cudaStreamSynchronize(s);
   if (rc == PFDTD_OK && e != cudaSuccess) rc = cuda_fail(e, "autotune", __FILE__, __LINE__);
   if (d->graph.exec) {

@@ -935,6 +935,12 @@ int launch_iwb_tma(pfdtd_domain* d, const void* cur, void* past, cudaStream_t s)
   return fail(PFDTD_ERR_UNSUPPORTED, "IWB on the TMA path needs FP32, FP16 or BF16 fields");
 }
 
+bool iwb_closure_fuses_dif(const pfdtd_domain* d) {
+  // tile shapes 0..5 run the closure inside the streaming kernel
+  return d->class_scheme == PFDTD_IWB && d->n_dif > 0 && d->iwb_closure_ready &&
+         d->d_iwb_closure_dif != nullptr && uses_tma(d) && !(d->tma_tile >= 0 && d->tma_tile <= 5);
+}
+
 // Whether the next update runs a TMA kernel (7-point or IWB).
 bool uses_tma(const pfdtd_domain* d) {
   if (d->kernel_variant == PFDTD_KERNEL_ZMARCH || !tma_supported(d)) return false;
