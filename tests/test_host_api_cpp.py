@@ -29,3 +29,17 @@ def test_host_api(built, tmp_path):
     print(r.stdout)
     assert r.returncode == 0, r.stdout + r.stderr
     assert "0 failures" in r.stdout
+
+
+def test_host_classes_equal_reference_golden(built, tmp_path):
+    """Source samples of every source and input type (float and double),
+    parameter vectors and a material table with repeated materials: this
+    library's classes against the values the reference's own classes gave
+    (tests/golden/ref_host_golden.txt, made by tests/golden/make_ref_golden.py)."""
+    exe = compile_cpp("golden_host_test.cpp", str(tmp_path))
+    gold = os.path.join(ROOT, "tests", "golden", "ref_host_golden.txt")
+    ir = os.path.join(ROOT, "tests", "golden", "grid_ir_kat.txt")
+    r = subprocess.run([exe, gold, ir], capture_output=True, text=True, cwd=str(tmp_path))
+    print(r.stdout[-3000:])
+    assert r.returncode == 0, r.stdout[-3000:] + r.stderr
+    assert " 0 failures" in r.stdout

@@ -1,0 +1,157 @@
+"""GPU parity against the reference's own code.
+
+Three checks, all through this library's C ABI (parallelfdtd_gb300.Domain):
+
+* golden: the receivers and final fields (SHA-256 of every byte) must equal
+  the values the reference's own update kernels and host classes produced
+  (tests/golden/ref_fields.npz, made by tests/golden/make_ref_golden.py from
+  src/kernels/kernels3d.cu, src/kernels/cudaMesh.cu and src/base/*.cpp compiled
+  unchanged), bit for bit.
+* the reference on this GPU: oracle/_ref holds the reference's kernels3d.cu
+  and cudaMesh.cu compiled unchanged for sm_103a, once with nvcc's default
+  floating-point contraction and once with -fmad=false.
+  oracle/ref_gpu_runner.cpp launches them with launchFDTD3d's host sequence
+  (kernels3d.cu:86-175).  Without contraction the reference must equal this
+  library bit for bit; with it, within the relative-L2 tolerance of the
+  contract (1e-5 FP32, 1e-12 FP64).
+* the same at the full 512 x 384 x 256 room for the full 2000 steps.
+
+Sources follow the reference as it runs: a soft source overwrites
+(PFDTD_QUIRK_SOFTSRC), and at octave 0 the forward kernel reads coefficient 0
+of material 0 for every node (PFDTD_QUIRK_MATIDX); at octave 1 with the same
+admittance in all 20 bands its index m*20*1 reads the value this library's
+intended index m*20+1 reads, so those cases run with no quirk.
+"""
+import hashlib
+import json
+import os
+
+import numpy as np
+import pytest
+
+from parallelfdtd_gb300 import rooms
+from parallelfdtd_gb300 import _lib as L
+from parallelfdtd_gb300.domain import Domain, default_params
+
+pytestmark = pytest.mark.gpu
+HERE = os.path.dirname(os.path.abspath(__file__))
+GOLD = os.path.join(HERE, "golden", "ref_fields.npz")
+TOL = {False: 1e-5, True: 1e-12}
+
+
+@pytest.fixture(scope="module")
+def R(built):
+    from oracle import ref
+    if not ref.gpu_available():
+        pytest.fail("oracle/_ref/*.cubin missing: run oracle/build_ref.py where the reference "
+                    "sources are mounted")
+    return ref
+
+
+def sha(a):
+    return hashlib.sha256(np.ascontiguousarray(a).tobytes()).hexdigest()
+
+
+def rel_l2(a, b):
+    return float(np.linalg.norm(np.asarray(a, np.float64) - b) / max(np.linalg.norm(b), 1e-300))
+
+
+def make_room(recipe):
+    kind, dims, n, seed = recipe
+    if kind == "shoebox":
+        return rooms.shoebox(tuple(dims), n_materials=n, seed=seed)
+    return rooms.boxes_room(tuple(dims), n_boxes=n, edge=(6, 24), n_materials=8, seed=seed)
+
+
+def run_product(room, double, scheme, quirks, params, table, srcs, types, samples, recs, steps):
+    with Domain(room.dims, "f64" if double else "f32") as d:
+        d.set_voxels(room.bid, room.mat, centred=scheme == "centred")
+        d.set_materials(np.asarray(table, np.float64).reshape(-1, 20))
+        d.set_params(np.asarray(params, np.float64))
+        d.set_scheme(scheme)
+        d.set_quirks(quirks)
+        d.set_sources(srcs, types, samples)
+        d.set_receivers(recs)
+        out, _, st = d.run(steps)
+        assert st == 0
+        return out, d.download_field(L.FIELD_CURRENT), d.download_field(L.FIELD_PAST)
+
+
+def _cases():
+    z = np.load(GOLD)
+    return json.loads(str(z["meta"]))["cases"]
+
+
+@pytest.fixture(scope="module")
+def gold():
+    return np.load(GOLD)
+
+
+@pytest.mark.parametrize("case", _cases(), ids=lambda c: c["name"])
+def test_product_equals_reference_golden(gpu, gold, case, R):
+    name = case["name"]
+    room = make_room(case["room"])
+    X, Y, _ = room.dims
+    flat = lambda c: c[2] * X * Y + c[1] * X + c[0]  # noqa: E731
+    srcs = [tuple(s[:3]) for s in case["sources"]]
+    types = [1 if s[3] == 1 else 0 for s in case["sources"]]
+    recs = [tuple(r) for r in case["receivers"]]
+    table, params, samples = gold[f"{name}__table"], gold[f"{name}__params"], gold[f"{name}__samples"]
+    want = gold[f"{name}__rec"]
+    out, P, Pp = run_product(room, case["double"], case["scheme"], case["quirks"], params, table,
+                             srcs, types, samples, recs, case["steps"])
+    err = rel_l2(out, want)
+    assert err <= TOL[case["double"]], f"relative L2 {err:.3e}"
+    assert np.array_equal(out, want), f"receivers not bit-identical (relative L2 {err:.3e})"
+    assert sha(P) == case["P_sha"] and sha(Pp) == case["Pp_sha"], "fields differ"
+
+    # the reference's own kernels on this GPU, without contraction: bit for bit
+    rr, rP, rPp, counts, _ = R.run_gpu(room.bid, room.mat, room.dims, case["scheme"], table,
+                                       params, [flat(s) for s in srcs], samples,
+                                       [flat(r) for r in recs], case["steps"],
+                                       double=case["double"], nofma=True)
+    assert list(counts) == case["counts"]
+    assert np.array_equal(rr, want)
+    assert sha(rP) == case["P_sha"] and sha(rPp) == case["Pp_sha"]
+    # ... and as nvcc compiles it by default (contracted multiply-adds)
+    rf, _, _, _, _ = R.run_gpu(room.bid, room.mat, room.dims, case["scheme"], table, params,
+                               [flat(s) for s in srcs], samples, [flat(r) for r in recs],
+                               case["steps"], double=case["double"], fields=False)
+    err = rel_l2(out, rf)
+    assert err <= TOL[case["double"]], f"vs contracted reference: relative L2 {err:.3e}"
+
+
+def c2_room():
+    return rooms.boxes_room((512, 384, 256), n_boxes=40, edge=(8, 64), n_materials=20, seed=2)
+
+
+@pytest.mark.parametrize("scheme,double", [("forward", False), ("centred", False),
+                                           ("forward", True)])
+def test_full_room_full_length_vs_reference_gpu(gpu, R, scheme, double):
+    """512 x 384 x 256, 40 boxes, 20 materials, soft impulse, 8 air receivers,
+    2000 steps (the benchmark room and length): this library and the
+    reference's own kernels on the same GPU.  Octave 1 with uniform bands, and
+    soft sources that overwrite, as the reference runs."""
+    room = c2_room()
+    steps = 2000
+    recs = room.random_air_nodes(8, seed=9)
+    src = room.random_air_nodes(1, seed=8)[0]
+    X, Y, _ = room.dims
+    flat = lambda c: c[2] * X * Y + c[1] * X + c[0]  # noqa: E731
+    dt = np.float64 if double else np.float32
+    params = default_params(octave=1).astype(dt)
+    table = room.admittance.astype(np.float32).astype(dt).reshape(-1)
+    samples = rooms.impulse(steps)[None].astype(dt)
+    out, P, Pp = run_product(room, double, scheme, L.QUIRK_SOFTSRC, params, table, [src], [1],
+                             samples, recs, steps)
+    assert np.abs(out).max() > 1e-6
+    rr, rP, rPp, _, _ = R.run_gpu(room.bid, room.mat, room.dims, scheme, table, params,
+                                  [flat(src)], samples, [flat(r) for r in recs], steps,
+                                  double=double, nofma=True)
+    assert np.array_equal(out, rr), f"receivers: relative L2 {rel_l2(out, rr):.3e}"
+    assert np.array_equal(P, rP) and np.array_equal(Pp, rPp)
+    rf, _, _, _, _ = R.run_gpu(room.bid, room.mat, room.dims, scheme, table, params, [flat(src)],
+                               samples, [flat(r) for r in recs], steps, double=double,
+                               fields=False)
+    err = rel_l2(out, rf)
+    assert err <= TOL[double], f"vs contracted reference: relative L2 {err:.3e}"
