@@ -344,6 +344,12 @@ def run_serving(a, world, rank, local):
             "e2e": {"value": res["node_updates"] * world / wall, "unit": METRIC,
                     "h2d_bytes_per_step": None, "d2h_bytes_per_step": None},
             "server": {k: st[k] for k in ("completed", "failed", "max_running", "bytes_peak")},
+            "work": {"requests": res["requests"],
+                     "node_updates": res["node_updates"],
+                     "computed_node_updates": res["computed_updates"],
+                     "note": "value counts the fields that carry a source; a request's field "
+                             "count is rounded up to a power of two and the padding fields "
+                             "are computed but not counted"},
             "clocks": clk.summary(),
         }
         print(json.dumps(line), flush=True)

@@ -176,6 +176,24 @@ int pfdtd_set_receivers_batched(pfdtd_domain* d, int n, const int64_t* xyz, cons
 /* Update scheme used by the next run/step (PFDTD_SRL_FORWARD, _SHARED, _SRL, _IWB). */
 int pfdtd_set_scheme(pfdtd_domain* d, int scheme);
 
+/* Arithmetic form of the forward (SRL_FORWARD / SHARED) update.  No
+ * counterpart in the reference.
+ * PFDTD_FORM_REFERENCE (default): the reference's expression
+ *   P+ = s/(1+b) * ((2 - K l2) P + l2 S - (1 - b) P-)   (kernels3d.cu:526),
+ *   bit for bit.
+ * PFDTD_FORM_DIFFERENCE: the same update, equal in exact arithmetic,
+ *   P+ = s/(1+b) * (((1+b) P + (1-b) (P - P-)) + l2 (S - K P)).
+ *   In float, the reference form rounds 6 l2 to 2 + 6e-8, which makes the
+ *   uniform (pressure offset) mode of a closed room grow step by step; the
+ *   difference form has no such term (S - K P is exactly 0 on a uniform
+ *   field), and its receiver error against an FP64 run drops by about two
+ *   orders of magnitude at the same memory traffic.  Float arithmetic only
+ *   (FP32, FP16, BF16 storage); no frequency-dependent boundaries and no
+ *   temporal blocking (PFDTD_ERR_UNSUPPORTED at the next run).  */
+#define PFDTD_FORM_REFERENCE 0
+#define PFDTD_FORM_DIFFERENCE 1
+int pfdtd_set_update_form(pfdtd_domain* d, int form);
+
 /* Run `steps` leapfrog steps from step index 0 (launchFDTD3d,
  * src/kernels/kernels3d.cu:31-203): per step inject sources into the current
  * field, update z = 1..Z-2 into the past field, swap, record receivers.
@@ -235,11 +253,14 @@ int pfdtd_capture_slice(pfdtd_domain* d, int orientation, int64_t slice, float* 
  * a serving loop that has given the whole HBM budget to resident domains, or
  * a per-step capture loop that must not stall on cudaFree, which synchronizes
  * the device.  The slice is gathered into a fixed 5 MiB scratch array
- * compiled into the library (held on every GPU the library is loaded on
- * until the process exits), so a slice may hold at most 1,048,576 nodes
+ * compiled into the library, so a slice may hold at most 1,048,576 nodes
  * (e.g. 1024 x 1024); larger slices return PFDTD_ERR_ARG and write nothing.
- * The first call on a device looks up the scratch's device address
- * (cudaGetSymbolAddress); make that first call before any stream capture.
+ * CUDA places such an array on a GPU only when its code is first used there;
+ * pfdtd_create / pfdtd_create_batched do that on their device (looking up
+ * the scratch's address with cudaGetSymbolAddress), so the 5 MiB are taken
+ * before the domain's buffers and stay on every GPU that has had a domain
+ * until the process exits.  Create the domain before committing the rest of
+ * the device's memory and before any stream capture.
  * Every call shares the one scratch array: calls that overlap on the GPU
  * (several host threads, or several domains on one device) race.  Each call
  * writes every element of its slice, so no earlier call's data leaks into

@@ -14,6 +14,7 @@
 #include <vector_functions.h>
 #include <vector_types.h>
 
+#include <cstdlib>
 #include <vector>
 
 #include "logger.h"
@@ -54,6 +55,7 @@ class CudaMesh {
   std::vector<double*> materials_double_;
   std::vector<unsigned int> device_list_;
   std::vector<std::vector<unsigned int> > partition_indexing_;
+  std::vector<unsigned int> memory_splits_;
   unsigned int number_of_partitions_;
   unsigned int partition_size_;
   float* h_material_coef_ptr_;
@@ -81,6 +83,12 @@ class CudaMesh {
   double* getPastPressureDoublePtrAt(unsigned int p) { return pressures_past_double_.at(p); }
   unsigned char* getPositionIdxPtrAt(unsigned int p) { return position_idx_ptr_.at(p); }
   unsigned char* getMaterialIdxPtrAt(unsigned int p) { return material_idx_ptr_.at(p); }
+  // cudaMesh.h:214-215.  The reference declares this getter but never fills
+  // the list behind it (its call throws std::out_of_range); here the list
+  // holds each partition's first global z-slice, where the mesh memory is
+  // split, and is filled by makePartition.  Out-of-range partitions throw
+  // std::out_of_range as before.
+  unsigned int getMemorySplitAt(unsigned int p) { return memory_splits_.at(p); }
   unsigned int getNumberOfElementsAt(unsigned int p) {
     return (unsigned int)partition_indexing_.at(p).size() * getDimXY();
   }
@@ -117,6 +125,18 @@ class CudaMesh {
   int getDeviceOfElement(unsigned int x, unsigned int y, unsigned int z);
   // z-slab indexing with one overlapping slice (cudaMesh.h:280-307).
   std::vector<std::vector<unsigned int> > getPartitionIndexing(int num_parts, int dim);
+
+  // Host buffers for per-partition data (cudaMesh.h:309-318): one zeroed
+  // block of slice_dim * (slices in the partition) elements of T per
+  // partition, from calloc; the caller frees each with free().
+  template <typename T>
+  std::vector<T*> splitPartitions(std::vector<std::vector<unsigned int> >& slices, int slice_dim) {
+    std::vector<T*> out;
+    out.reserve(slices.size());
+    for (const std::vector<unsigned int>& part : slices)
+      out.push_back(static_cast<T*>(std::calloc((size_t)slice_dim * part.size(), sizeof(T))));
+    return out;
+  }
 
   template <typename T>
   void setSample(T sample, unsigned int x, unsigned int y, unsigned int z) {

@@ -133,7 +133,9 @@ template <> inline double from_arith<double>(double v) { return v; }
 
 struct RunDesc {
   int scheme;   // 0 forward (Bilbao), 1 centred (Kowalczyk), 3 IWB (centred encoding)
-  int quirks;   // bit0: forward material index m*20*octave; bit1: soft source overwrites
+  int quirks;   // bit0: forward material index m*20*octave; bit1: soft source overwrites;
+                // bit8: forward update in the difference form (the library's
+                // PFDTD_FORM_DIFFERENCE, no counterpart in the reference)
   int64_t X, Y, Z;
   const uint8_t* pos;
   const uint8_t* mat;
@@ -323,6 +325,15 @@ int update(const RunDesc& d, const St* P, St* Pp, const std::vector<T>& beta_tab
                     (T)to_float(P[c - X]) + (T)to_float(P[c + 1]) + (T)to_float(P[c - 1]);
         ret = sw * ((T)1 / ((T)1 + beta)) *
               ((((T)2 - position * l2) * p + l2 * S - ((T)1 - beta) * pp) - g2 * s1);
+      } else if (d.scheme == 0 && (d.quirks & 0x100)) {
+        // Difference form of the same update (equal in exact arithmetic):
+        // s/(1+b) (((1+b) p + (1-b)(p - pp)) + l2 (S - K p)).
+        const T position = (T)(pos & kForwardMask);
+        const T sw = (T)(pos >> kInsideSwitch);
+        const T S = (T)to_float(P[c + XY]) + (T)to_float(P[c - XY]) + (T)to_float(P[c + X]) +
+                    (T)to_float(P[c - X]) + (T)to_float(P[c + 1]) + (T)to_float(P[c - 1]);
+        ret = sw * ((T)1 / ((T)1 + beta)) *
+              ((((T)1 + beta) * p + ((T)1 - beta) * (p - pp)) + l2 * (S - position * p));
       } else if (d.scheme == 0) {
         const T position = (T)(pos & kForwardMask);
         const T sw = (T)(pos >> kInsideSwitch);

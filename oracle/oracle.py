@@ -101,12 +101,14 @@ def run(pos: np.ndarray, mat: np.ndarray, dims: Sequence[int], table: np.ndarray
         samples: np.ndarray, rec_idx: Sequence[int], steps: int, scheme: int = 0,
         quirks: int = 0, double: bool = False, threads: int = 0,
         P0: Optional[np.ndarray] = None, Pp0: Optional[np.ndarray] = None,
-        storage: Optional[str] = None, dif: Optional[Tuple[np.ndarray, np.ndarray]] = None):
+        storage: Optional[str] = None, dif: Optional[Tuple[np.ndarray, np.ndarray]] = None,
+        form: str = "reference"):
     """Oracle step loop.  Returns (receivers [n_rec, steps], P, P_past).
     storage: None (FP32, or FP64 with double=True), "f16" or "bf16" (16-bit
     fields with float arithmetic; fields returned as float16 / uint16).
     dif: (flags [n_mat] int, coefs [n_mat, 7] b0..b3, a1..a3) for materials
-    with frequency-dependent admittance."""
+    with frequency-dependent admittance.  form: "reference" or "difference"
+    (the library's PFDTD_FORM_DIFFERENCE forward update)."""
     lib = load()
     dt = np.float64 if double else np.float32
     prec = 1 if double else {None: 0, "f32": 0, "f16": 2, "bf16": 3}[storage]
@@ -133,6 +135,10 @@ def run(pos: np.ndarray, mat: np.ndarray, dims: Sequence[int], table: np.ndarray
         dcoef = np.ascontiguousarray(dif[1], dtype=dt).reshape(-1, 7)
         if dflag.size != n_mat or dcoef.shape[0] != n_mat:
             raise ValueError("dif tables must have one row per material")
+    if form not in ("reference", "difference"):
+        raise ValueError("form must be 'reference' or 'difference'")
+    if form == "difference":
+        quirks = quirks | 0x100
     rc = lib.oracle_run(prec, scheme, quirks, X, Y, Z, _p(pos), _p(mat), _p(tab),
                         n_mat, _p(prm), si.size, _p(si), _p(st), _p(sm), ri.size, _p(ri),
                         steps, _p(P), _p(Pp), _p(out), threads, _p(dflag), _p(dcoef))

@@ -4,9 +4,9 @@ src/AppPy.cpp:96-133) over the C ABI of FDTD::App (include/pfdtd_app.h).
 Method names, argument order and meaning follow the boost::python module, so
 a script written for ``import libPyFDTD as pf`` runs with
 ``from parallelfdtd_gb300 import libPyFDTD as pf``.  Lists may be Python
-lists or numpy arrays.  Two additions: initializeVoxels (already voxelized
-geometry, since the triangle voxelizer is not part of this library) and
-setReferenceQuirks.
+lists or numpy arrays.  initializeGeometry voxelizes the triangle mesh on the
+device (csrc/voxelize.cu).  Two additions: initializeVoxels (geometry that is
+already voxelized, as boundary ids and materials) and setReferenceQuirks.
 """
 from __future__ import annotations
 

@@ -1,5 +1,9 @@
 // Per-class update coefficients, evaluated on the host.
 //
+// Forward classes in the difference form (PFDTD_FORM_DIFFERENCE) hold
+// a = s/(1+beta), b = K, c = 1 - beta and the float bits of 1 + beta in the
+// pos word, for P+ = a (((1+beta) P + c (P - P-)) + l2 (S - b P)).
+//
 // A class is one (position byte, material byte) pair present in the grid.
 // The terms of the reference kernels that depend only on that pair are
 // computed here in the kernel's arithmetic type, with the reference's own
@@ -19,8 +23,9 @@ int fail(int code, const std::string& msg);
 namespace {
 
 template <typename A>
-int eval(int scheme, int quirks, const double* params, const std::vector<double>& materials,
-         int n_mat, int n_coef, const std::vector<uint16_t>& keys, std::vector<uint8_t>& out) {
+int eval(int scheme, int form, int quirks, const double* params,
+         const std::vector<double>& materials, int n_mat, int n_coef,
+         const std::vector<uint16_t>& keys, std::vector<uint8_t>& out) {
   const size_t n = keys.size();
   std::vector<A> ca(n), cb(n), cc(n);
   std::vector<uint32_t> cpos(n);
@@ -61,6 +66,20 @@ int eval(int scheme, int quirks, const double* params, const std::vector<double>
       // by the closure pass on the TMA path
       cpos[i] = pos | (pos >= 2 ? 0x40000000u : 0u);
       continue;
+    } else if (scheme != PFDTD_SRL && form == PFDTD_FORM_DIFFERENCE && sizeof(A) == 4) {
+      // difference form: a = s/(1+beta), b = K, c = 1 - beta and, in the
+      // pos word, the bits of the float 1 + beta
+      const A position = (A)(pos & 0x7Fu);
+      const A beta = (A)0.5 * (Y * ((A)6 - position) * l);
+      const A onep = (A)1 + beta;
+      ca[i] = sw * ((A)1 / onep);
+      cb[i] = position;
+      cc[i] = (A)1 - beta;
+      const float e = (float)onep;
+      uint32_t bits;
+      std::memcpy(&bits, &e, 4);
+      cpos[i] = bits;
+      continue;
     } else if (scheme != PFDTD_SRL) {
       // kernels3d.cu:509-526
       const A position = (A)(pos & 0x7Fu);
@@ -89,12 +108,12 @@ int eval(int scheme, int quirks, const double* params, const std::vector<double>
 
 }  // namespace
 
-int eval_class_coefs(int precision, int scheme, int quirks, const double* params,
+int eval_class_coefs(int precision, int scheme, int form, int quirks, const double* params,
                      const std::vector<double>& materials, int n_mat, int n_coef,
                      const std::vector<uint16_t>& keys, std::vector<uint8_t>& out_tab) {
   if (precision == PFDTD_F64)
-    return eval<double>(scheme, quirks, params, materials, n_mat, n_coef, keys, out_tab);
-  return eval<float>(scheme, quirks, params, materials, n_mat, n_coef, keys, out_tab);
+    return eval<double>(scheme, form, quirks, params, materials, n_mat, n_coef, keys, out_tab);
+  return eval<float>(scheme, form, quirks, params, materials, n_mat, n_coef, keys, out_tab);
 }
 
 }  // namespace pfdtd

@@ -8,6 +8,7 @@
 #include <stdint.h>
 
 #include <atomic>
+#include <cmath>
 #include <string>
 #include <vector>
 
@@ -209,11 +210,15 @@ struct pfdtd_domain {
   // material table and parameters (host copies, arithmetic type widened to double)
   std::vector<double> materials;
   int n_mat = 0, n_coef = 20;
-  double params[4] = {0.57735026918962576, 1.0 / 3.0, 1.0 / 3.0, 0.0};
+  // lambda = sqrt(1/3) as SimulationParameters::setUpdateType sets it
+  double params[4] = {std::sqrt(1.0 / 3.0), 1.0 / 3.0, 1.0 / 3.0, 0.0};
+  // PFDTD_FORM_*: arithmetic form of the forward update
+  int update_form = 0;
 
   // class table
   bool classes_dirty = true;
   int class_scheme = -1;
+  int class_form = 0;        // update form the class table was built for
   int n_classes = 0;
   int cls_bytes = 1;
   void* d_cls = nullptr;     // per node class id (uint8 or uint16)
@@ -304,6 +309,8 @@ int launch_update(pfdtd_domain* d, const void* cur, void* past, cudaStream_t s);
 int launch_io(pfdtd_domain* d, void* cur, void* rec_out, int64_t rec_ld, int64_t inject_end,
               cudaStream_t s, int advance = 1);
 int build_classes(pfdtd_domain* d);
+// noalloc.cu: puts the no-allocation capture's scratch on `device` (current).
+int noalloc_prepare(int device);
 // Implemented in stencil_tma.cu
 bool tma_supported(const pfdtd_domain* d);
 // Implemented in dif.cu

@@ -20,6 +20,8 @@
 // per node instead of gathering the 26 neighbours again.
 #include "common.cuh"
 
+#include <cstdlib>
+
 #include <algorithm>
 #include <cstring>
 #include <vector>
@@ -479,6 +481,37 @@ int build_dif(pfdtd_domain* d, const std::vector<uint16_t>& keys,
   return PFDTD_OK;
 }
 
+// The DIF slot of every closure record, so that the closure pass applies the
+// DIF update itself.  Only an optimisation: returns nullptr (and the separate
+// DIF pass stays in use) if any DIF node has no record or anything fails, with
+// every temporary released and the CUDA error cleared.
+static int32_t* closure_dif_slots(pfdtd_domain* d, int64_t n) {
+  cudaStream_t s = d->stream;
+  int32_t* slot = nullptr;
+  unsigned* d_missing = nullptr;
+  unsigned missing = 1;
+  cudaError_t e = d->alloc((void**)&slot, sizeof(int32_t) * (size_t)n);
+  if (e == cudaSuccess) e = d->alloc((void**)&d_missing, sizeof(unsigned));
+  if (e == cudaSuccess) e = cudaMemsetAsync(slot, 0xFF, sizeof(int32_t) * (size_t)n, s);
+  if (e == cudaSuccess) e = cudaMemsetAsync(d_missing, 0, sizeof(unsigned), s);
+  if (e == cudaSuccess) {
+    k_closure_dif_slots<<<grid_for(d->n_dif), 256, 0, s>>>(
+        d->d_dif_list, d->n_dif, (const ClosureRec*)d->d_iwb_closure, n, slot, d_missing);
+    count_launch();
+    e = cudaGetLastError();
+  }
+  if (e == cudaSuccess)
+    e = cudaMemcpyAsync(&missing, d_missing, sizeof(unsigned), cudaMemcpyDeviceToHost, s);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+  if (d_missing) d->release(d_missing);
+  if (e != cudaSuccess || missing != 0) {
+    if (e != cudaSuccess) cudaGetLastError();
+    if (slot) d->release(slot);
+    return nullptr;
+  }
+  return slot;
+}
+
 // The closure-node list of an IWB domain on the TMA path (one field per
 // node, FP32/FP16/BF16 storage): classes whose geometry code is >= 2.
 int build_iwb_closure(pfdtd_domain* d, const std::vector<uint16_t>& keys) {
@@ -496,32 +529,24 @@ int build_iwb_closure(pfdtd_domain* d, const std::vector<uint16_t>& keys) {
   if (int rc = build_flagged_list(d, flag, &list, &n)) return rc;
   if (n > 0) {
     cudaStream_t s = d->stream;
-    PFDTD_CK(d->alloc(&d->d_iwb_closure, sizeof(ClosureRec) * (size_t)n));
+    cudaError_t e = d->alloc(&d->d_iwb_closure, sizeof(ClosureRec) * (size_t)n);
+    if (e != cudaSuccess) {
+      d->release(list);
+      d->d_iwb_closure = nullptr;
+      return cuda_fail(e, "IWB closure records", __FILE__, __LINE__);
+    }
     k_closure_records<<<grid_for(n), 256, 0, s>>>(list, n, d->d_cls, d->cls_bytes, d->d_iwb_mask,
                                                   (ClosureRec*)d->d_iwb_closure);
     count_launch();
-    PFDTD_CK(cudaGetLastError());
+    e = cudaGetLastError();
     d->release(list);
-    if (d->n_dif > 0 && d->n_dif < ((int64_t)1 << 31) && d->d_dif_list) {
-      // the DIF slot of every record, so that the closure pass applies the
-      // DIF update itself; kept only if every DIF node has a record
-      int32_t* slot = nullptr;
-      unsigned* d_missing = nullptr;
-      PFDTD_CK(d->alloc((void**)&slot, sizeof(int32_t) * (size_t)n));
-      PFDTD_CK(d->alloc((void**)&d_missing, sizeof(unsigned)));
-      PFDTD_CK(cudaMemsetAsync(slot, 0xFF, sizeof(int32_t) * (size_t)n, s));
-      PFDTD_CK(cudaMemsetAsync(d_missing, 0, sizeof(unsigned), s));
-      k_closure_dif_slots<<<grid_for(d->n_dif), 256, 0, s>>>(
-          d->d_dif_list, d->n_dif, (const ClosureRec*)d->d_iwb_closure, n, slot, d_missing);
-      count_launch();
-      PFDTD_CK(cudaGetLastError());
-      unsigned missing = 1;
-      PFDTD_CK(cudaMemcpyAsync(&missing, d_missing, sizeof(unsigned), cudaMemcpyDeviceToHost, s));
-      PFDTD_CK(cudaStreamSynchronize(s));
-      d->release(d_missing);
-      if (missing == 0) d->d_iwb_closure_dif = slot;
-      else d->release(slot);
-    }
+    if (e != cudaSuccess) return cuda_fail(e, "k_closure_records", __FILE__, __LINE__);
+    // PFDTD_IWB_DIF_UNFUSED=1 keeps the DIF update in its own pass (a test
+    // hook: both paths give the same result bit for bit).
+    const char* unfused = std::getenv("PFDTD_IWB_DIF_UNFUSED");
+    if (d->n_dif > 0 && d->n_dif < ((int64_t)1 << 31) && d->d_dif_list &&
+        !(unfused && unfused[0] == '1'))
+      d->d_iwb_closure_dif = closure_dif_slots(d, n);
   }
   d->n_iwb_closure = n;
   d->iwb_closure_ready = true;

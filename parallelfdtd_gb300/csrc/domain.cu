@@ -350,6 +350,9 @@ int pfdtd_create_batched(int64_t dim_x, int64_t dim_y, int64_t dim_z, int fields
   }
   if (device < 0 || device >= ndev) return fail(PFDTD_ERR_ARG, "device index out of range");
   DeviceGuard g(device);
+  // The no-allocation slice capture's fixed scratch is placed on the device
+  // now, before this domain's buffers take the memory it could need.
+  noalloc_prepare(device);
   pfdtd_domain* d = new pfdtd_domain();
   d->device = device;
   d->serial = ++g_serial;
@@ -471,6 +474,23 @@ int pfdtd_set_quirks(pfdtd_domain* d, int quirks) {
     }
   }
   d->quirks = quirks;
+  return PFDTD_OK;
+}
+
+int pfdtd_set_update_form(pfdtd_domain* d, int form) {
+  if (int rc = check_domain(d)) return rc;
+  if (form != PFDTD_FORM_REFERENCE && form != PFDTD_FORM_DIFFERENCE)
+    return fail(PFDTD_ERR_ARG, "unknown update form");
+  if (form != PFDTD_FORM_REFERENCE && d->precision == PFDTD_F64)
+    return fail(PFDTD_ERR_UNSUPPORTED, "the difference form is built for float arithmetic");
+  if (form != d->update_form) {
+    d->update_form = form;
+    d->classes_dirty = true;
+    if (d->graph.exec) {
+      cudaGraphExecDestroy(d->graph.exec);
+      d->graph.exec = nullptr;
+    }
+  }
   return PFDTD_OK;
 }
 
@@ -1131,20 +1151,34 @@ int pfdtd_autotune(pfdtd_domain* d, int max_depth, int iters, int* best_depth, i
       return fail(PFDTD_ERR_NOMEM, "autotune field snapshot allocation failed");
     }
   }
-  PFDTD_CK(cudaMemcpyAsync(keep[0], d->field_base[d->cur], fbytes, cudaMemcpyDeviceToDevice, s));
-  PFDTD_CK(cudaMemcpyAsync(keep[1], d->field_base[d->prev], fbytes, cudaMemcpyDeviceToDevice, s));
   // the IWB closure pass also advances the DIF filter states: keep them too
   void* keep_dif = nullptr;
   const size_t dbytes = d->n_dif > 0 ? (size_t)d->n_dif * d->K * 4 * d->arith_size() : 0;
-  if (dbytes) {
-    if (cudaMallocAsync(&keep_dif, dbytes, s) != cudaSuccess) {
+  {
+    cudaError_t e = cudaMemcpyAsync(keep[0], d->field_base[d->cur], fbytes,
+                                    cudaMemcpyDeviceToDevice, s);
+    if (e == cudaSuccess)
+      e = cudaMemcpyAsync(keep[1], d->field_base[d->prev], fbytes, cudaMemcpyDeviceToDevice, s);
+    int code = PFDTD_ERR_CUDA;
+    if (e == cudaSuccess && dbytes) {
+      e = cudaMallocAsync(&keep_dif, dbytes, s);
+      if (e != cudaSuccess) {
+        keep_dif = nullptr;
+        code = PFDTD_ERR_NOMEM;
+      } else {
+        e = cudaMemcpyAsync(keep_dif, d->d_dif_state, dbytes, cudaMemcpyDeviceToDevice, s);
+      }
+    }
+    if (e != cudaSuccess) {
       cudaGetLastError();
       cudaFreeAsync(keep[0], s);
       cudaFreeAsync(keep[1], s);
+      if (keep_dif) cudaFreeAsync(keep_dif, s);
       d->tb_depth = depth0;
-      return fail(PFDTD_ERR_NOMEM, "autotune filter-state snapshot allocation failed");
+      return code == PFDTD_ERR_NOMEM
+                 ? fail(code, "autotune filter-state snapshot allocation failed")
+                 : cuda_fail(e, "autotune snapshot", __FILE__, __LINE__);
     }
-    PFDTD_CK(cudaMemcpyAsync(keep_dif, d->d_dif_state, dbytes, cudaMemcpyDeviceToDevice, s));
   }
   double best = 1e300;
   int bd = 0, bs = -1;

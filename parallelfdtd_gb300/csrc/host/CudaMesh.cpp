@@ -168,6 +168,9 @@ void CudaMesh::makePartition(unsigned int number_of_partitions,
     for (unsigned i = 0; i < number_of_partitions; ++i) device_list.push_back(i);
   device_list_ = device_list;
   partition_indexing_ = getPartitionIndexing((int)number_of_partitions, (int)dim_z_);
+  memory_splits_.clear();
+  for (const std::vector<unsigned int>& part : partition_indexing_)
+    memory_splits_.push_back(part.empty() ? 0u : part.front());
   number_of_partitions_ = number_of_partitions;
   partition_size_ = (unsigned)partition_indexing_.at(0).size();
   if (domain_) {
@@ -266,6 +269,7 @@ void CudaMesh::destroyPartitions() {
   for (unsigned char* p : position_idx_ptr_) (void)p;
   position_idx_ptr_.clear();
   material_idx_ptr_.clear();
+  memory_splits_.clear();
   pressures_.clear();
   pressures_past_.clear();
   pressures_double_.clear();

@@ -40,7 +40,8 @@ struct pfdtd_request {
   int n_mat = 0, n_coef = 20;
   std::vector<int32_t> dif_flags;
   std::vector<double> dif_coefs;
-  double params[4] = {0.57735026918962576, 1.0 / 3.0, 1.0 / 3.0, 0.0};
+  // lambda = sqrt(1/3), as SimulationParameters::setUpdateType sets it
+  double params[4] = {std::sqrt(1.0 / 3.0), 1.0 / 3.0, 1.0 / 3.0, 0.0};
   int n_src = 0;
   int64_t n_samples = 0;
   std::vector<int64_t> src_xyz;
@@ -60,6 +61,21 @@ size_t storage_size(int precision) {
   return precision == PFDTD_F64 ? 8 : (precision == PFDTD_F32 ? 4 : 2);
 }
 size_t arith_size(int precision) { return precision == PFDTD_F64 ? 8 : 4; }
+
+// Fields that carry a source: the work a request asks for.  A batched request
+// rounds its field count up to a power of two; the padding fields are
+// computed but are not counted as node-updates.
+int source_fields(const pfdtd_request* r) {
+  if (r->n_src <= 0) return r->fields;
+  std::vector<bool> seen((size_t)r->fields, false);
+  int n = 0;
+  for (int32_t f : r->src_field)
+    if (f >= 0 && f < r->fields && !seen[(size_t)f]) {
+      seen[(size_t)f] = true;
+      ++n;
+    }
+  return n > 0 ? n : r->fields;
+}
 
 struct Job {
   pfdtd_request* req = nullptr;
@@ -192,7 +208,7 @@ void scheduler(pfdtd_server* s) {
         s->st.completed++;
         const pfdtd_request* r = j.req;
         s->st.node_updates += (double)r->X * (double)r->Y * (double)(r->Z - 2) *
-                              (double)r->steps * (double)r->fields;
+                              (double)r->steps * (double)source_fields(r);
       } else {
         s->st.failed++;
       }

@@ -18,8 +18,11 @@ namespace {
 
 // Largest slice (nodes) the scratch holds: 1,048,576 nodes, e.g. 1024 x 1024.
 constexpr int64_t kNoAllocMaxSliceNodes = (int64_t)1 << 20;
-// 4 bytes of pressure (float) plus 1 node byte per slice node: 5 MiB.  Every
-// GPU the library is loaded on holds this array until the process exits.
+// 4 bytes of pressure (float) plus 1 node byte per slice node: 5 MiB.  CUDA
+// loads a module's __device__ arrays onto a GPU lazily, the first time the
+// module is used there; domain creation resolves the scratch's address
+// (noalloc_prepare), so every GPU that has had a domain holds these 5 MiB,
+// taken before the domain's own buffers, until the process exits.
 constexpr size_t kNoAllocScratchBytes = (size_t)kNoAllocMaxSliceNodes * 5;
 
 static __device__ __align__(256) unsigned char g_slice_scratch[kNoAllocScratchBytes];
@@ -68,6 +71,18 @@ __global__ void k_slice_into(const S* __restrict__ P, const uint8_t* __restrict_
 }
 
 }  // namespace
+
+// Places the scratch on `device` (the current device) and caches its address.
+// Called at domain creation so that the 5 MiB are taken before the caller
+// commits the device's memory; a failure here is cleared and the first
+// no-allocation capture on the device tries again.
+int noalloc_prepare(int device) {
+  void* p = nullptr;
+  int rc = scratch_address(device, &p);
+  if (rc != PFDTD_OK) cudaGetLastError();
+  return rc;
+}
+
 }  // namespace pfdtd
 
 using namespace pfdtd;

@@ -29,7 +29,7 @@ template <typename S, typename C, int SCHEME>
 __global__ void __launch_bounds__(kBX * kBY)
 k_update_zmarch(const C* __restrict__ cls, const S* __restrict__ P, S* __restrict__ Pp,
                 ClassTab<typename Store<S>::A> tab, int X, int Y, int64_t XY, int z_last,
-                int zc, typename Store<S>::A l2, int ks, int kshift) {
+                int zc, typename Store<S>::A l2, int ks, int kshift, int form) {
   using A = typename Store<S>::A;
   using R = Rn<A>;
   using St = Store<S>;
@@ -75,8 +75,16 @@ k_update_zmarch(const C* __restrict__ cls, const S* __restrict__ P, S* __restric
     if (SCHEME == 0) {
       // S = P[z+1] + P[z-1] + P[y+1] + P[y-1] + P[x+1] + P[x-1]  (kernels3d.cu:525)
       const A s6 = R::add(R::add(R::add(R::add(R::add(pn, pm), yp), ym), xp), xm);
-      // sw/(1+beta) * ((2 - K l2) p + l2 S - (1 - beta) pp)     (kernels3d.cu:526)
-      out = R::mul(ca, R::sub(R::add(R::mul(cb, pc), R::mul(l2, s6)), R::mul(cc, pp)));
+      if (sizeof(A) == 4 && form) {
+        // difference form: a (((1+beta) p + (1-beta)(p - pp)) + l2 (S - K p)),
+        // cb = K and the pos word holds the float 1 + beta
+        const A e = (A)__uint_as_float(cp);
+        out = R::mul(ca, R::add(R::add(R::mul(e, pc), R::mul(cc, R::sub(pc, pp))),
+                                R::mul(l2, R::sub(s6, R::mul(cb, pc)))));
+      } else {
+        // sw/(1+beta) * ((2 - K l2) p + l2 S - (1 - beta) pp)   (kernels3d.cu:526)
+        out = R::mul(ca, R::sub(R::add(R::mul(cb, pc), R::mul(l2, s6)), R::mul(cc, pp)));
+      }
     } else {
       // Mirrored boundary neighbour per axis (kernels3d.cu:642-659).
       const A dx = (A)(cp & 1u), dy = (A)((cp >> 1) & 1u), dz = (A)((cp >> 2) & 1u);
@@ -280,7 +288,7 @@ int launch_update_t(pfdtd_domain* d, const void* cur, void* past, cudaStream_t s
                   (const uint32_t*)(tb + 3 * as * d->n_classes), d->n_classes};
   k_update_zmarch<S, C, SCHEME><<<dim3(gx, gy, gz), dim3(kBX, kBY), 0, s>>>(
       (const C*)d->d_cls, (const S*)cur, (S*)past, tab, (int)XE, (int)d->Y, d->XY * d->K,
-      (int)(d->Z - 1), (int)zc, (A)d->params[1], d->K, d->kshift);
+      (int)(d->Z - 1), (int)zc, (A)d->params[1], d->K, d->kshift, d->class_form);
   count_launch();
   PFDTD_CK(cudaGetLastError());
   return PFDTD_OK;
@@ -341,7 +349,7 @@ int launch_io_t(pfdtd_domain* d, void* cur, void* rec_out, int64_t rec_ld, int64
 }  // namespace
 
 // Host-side class coefficient evaluation (classes_host.cpp).
-int eval_class_coefs(int precision, int scheme, int quirks, const double* params,
+int eval_class_coefs(int precision, int scheme, int form, int quirks, const double* params,
                      const std::vector<double>& materials, int n_mat, int n_coef,
                      const std::vector<uint16_t>& keys, std::vector<uint8_t>& out_tab);
 
@@ -375,9 +383,18 @@ int launch_io(pfdtd_domain* d, void* cur, void* rec_out, int64_t rec_ld, int64_t
 int build_classes(pfdtd_domain* d) {
   const int scheme = (d->scheme == PFDTD_SRL || d->scheme == PFDTD_IWB) ? d->scheme
                                                                        : PFDTD_SRL_FORWARD;
-  if (!d->classes_dirty && d->class_scheme == scheme) return PFDTD_OK;
+  const int form = scheme == PFDTD_SRL_FORWARD ? d->update_form : PFDTD_FORM_REFERENCE;
+  if (!d->classes_dirty && d->class_scheme == scheme && d->class_form == form) return PFDTD_OK;
   if (!d->nodes_set) return fail(PFDTD_ERR_STATE, "node bytes not set");
   if (d->n_mat <= 0) return fail(PFDTD_ERR_STATE, "material table not set");
+  if (form != PFDTD_FORM_REFERENCE) {
+    for (int32_t f : d->dif_flags)
+      if (f)
+        return fail(PFDTD_ERR_UNSUPPORTED,
+                    "the difference form is not built for frequency-dependent boundaries");
+    if (d->precision == PFDTD_F64)
+      return fail(PFDTD_ERR_UNSUPPORTED, "the difference form is built for float arithmetic");
+  }
   cudaStream_t s = d->stream;
   uint8_t* d_present = nullptr;
   PFDTD_CK(cudaMallocAsync((void**)&d_present, 65536, s));
@@ -417,8 +434,8 @@ int build_classes(pfdtd_domain* d) {
     }
   if (keys.empty()) keys.push_back(0);  // grid without updated planes
   std::vector<uint8_t> tab;
-  int rc = eval_class_coefs(d->precision, scheme, d->quirks, d->params, d->materials, d->n_mat,
-                            d->n_coef, keys, tab);
+  int rc = eval_class_coefs(d->precision, scheme, form, d->quirks, d->params, d->materials,
+                            d->n_mat, d->n_coef, keys, tab);
   if (rc != PFDTD_OK) return rc;
   const int n_classes = (int)keys.size();
   const int cls_bytes = n_classes <= 256 ? 1 : 2;
@@ -449,6 +466,7 @@ int build_classes(pfdtd_domain* d) {
   PFDTD_CK(cudaStreamSynchronize(s));
   d->n_classes = n_classes;
   d->class_scheme = scheme;
+  d->class_form = form;
   rc = build_dif(d, keys, tab);
   if (rc != PFDTD_OK) return rc;
   rc = build_iwb_closure(d, keys);

@@ -70,6 +70,7 @@ int tb_usable(const pfdtd_domain* d, std::string* why) {
   if (d->class_scheme != PFDTD_SRL_FORWARD && d->class_scheme != PFDTD_SRL)
     return no("only the SRL forward and centred schemes are blocked");
   if (d->n_dif > 0) return no("frequency-dependent boundaries need the per-step update");
+  if (d->class_form != PFDTD_FORM_REFERENCE) return no("the difference form runs the per-step update");
   if (d->cls_bytes != 1) return no("more than 256 node classes");
   if (d->X % 4 != 0) return no("X must be a multiple of 4");
   if (d->K != 1 && d->K % 4 != 0) return no("batched fields must be a multiple of 4");

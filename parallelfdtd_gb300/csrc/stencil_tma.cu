@@ -319,7 +319,7 @@ k_update_tma(const __grid_constant__ CUtensorMap map_cur, const __grid_constant_
              const __grid_constant__ CUtensorMap map_mask, const S* __restrict__ P,
              S* __restrict__ Pp, ClassTab<typename Store<S>::A> tab, int X, int Y, int64_t XY,
              int z_last, int zc, typename Store<S>::A l2, int* __restrict__ err, int kshift = 0,
-             float* __restrict__ iwb_sw = nullptr, float nzf = -0.0f) {
+             float* __restrict__ iwb_sw = nullptr, float nzf = -0.0f, int form = 0) {
   using A = typename Store<S>::A;
   using R = Rn<A>;
   using St = Store<S>;
@@ -543,12 +543,13 @@ k_update_tma(const __grid_constant__ CUtensorMap map_cur, const __grid_constant_
         auto pr = [](const V4<S>& v, int h) -> f2 {
           return pk2(St::load(v.v[2 * h]), St::load(v.v[2 * h + 1]));
         };
-        f2 aa[2], bb[2], cc[2], xm2[2], xp2[2];
+        f2 aa[2], bb[2], cc[2], ee[2], xm2[2], xp2[2];
         if constexpr (BATCHED) {
           const PackedCoef<A> k = coef(0);
           aa[0] = aa[1] = pk2(k.a, k.a);
           bb[0] = bb[1] = pk2(k.b, k.b);
           cc[0] = cc[1] = pk2(k.c, k.c);
+          ee[0] = ee[1] = pk2(__uint_as_float(k.pos), __uint_as_float(k.pos));
           xm2[0] = pr(vxm, 0); xm2[1] = pr(vxm, 1);
           xp2[0] = pr(vxp, 0); xp2[1] = pr(vxp, 1);
         } else {
@@ -558,6 +559,7 @@ k_update_tma(const __grid_constant__ CUtensorMap map_cur, const __grid_constant_
             aa[h] = pk2(k0.a, k1.a);
             bb[h] = pk2(k0.b, k1.b);
             cc[h] = pk2(k0.c, k1.c);
+            ee[h] = pk2(__uint_as_float(k0.pos), __uint_as_float(k1.pos));
           }
           const A c0 = St::load(vc.v[0]), c1 = St::load(vc.v[1]), c2 = St::load(vc.v[2]),
                   c3 = St::load(vc.v[3]);
@@ -569,8 +571,16 @@ k_update_tma(const __grid_constant__ CUtensorMap map_cur, const __grid_constant_
         for (int h = 0; h < 2; ++h) {
           const f2 s6 = add2(add2(add2(add2(add2(pr(vzp, h), pr(vzm, h)), pr(vyp, h)),
                                       pr(vym, h)), xp2[h]), xm2[h]);
-          const f2 o = mul2(aa[h], sub2(add2(fma2(bb[h], pr(vc, h), nz), fma2(l22, s6, nz)),
-                                        fma2(cc[h], pr(vpp, h), nz)));
+          f2 o;
+          if (form) {
+            // difference form: a (((1+beta) p + (1-beta)(p - pp)) + l2 (S - K p))
+            const f2 pc2 = pr(vc, h);
+            o = mul2(aa[h], add2(add2(fma2(ee[h], pc2, nz), fma2(cc[h], sub2(pc2, pr(vpp, h)), nz)),
+                                 fma2(l22, sub2(s6, fma2(bb[h], pc2, nz)), nz)));
+          } else {
+            o = mul2(aa[h], sub2(add2(fma2(bb[h], pr(vc, h), nz), fma2(l22, s6, nz)),
+                                 fma2(cc[h], pr(vpp, h), nz)));
+          }
           float lo, hi;
           up2(o, lo, hi);
           if constexpr (sizeof(S) == 4) {
@@ -613,7 +623,13 @@ k_update_tma(const __grid_constant__ CUtensorMap map_cur, const __grid_constant_
         A out;
         if (SCHEME == 0) {
           const A s6 = R::add(R::add(R::add(R::add(R::add(pn, pm), yp), ym), xp), xm);
-          out = R::mul(k.a, R::sub(R::add(R::mul(k.b, pc), R::mul(l2, s6)), R::mul(k.c, pp)));
+          if (sizeof(A) == 4 && form) {
+            const A e = (A)__uint_as_float(k.pos);
+            out = R::mul(k.a, R::add(R::add(R::mul(e, pc), R::mul(k.c, R::sub(pc, pp))),
+                                     R::mul(l2, R::sub(s6, R::mul(k.b, pc)))));
+          } else {
+            out = R::mul(k.a, R::sub(R::add(R::mul(k.b, pc), R::mul(l2, s6)), R::mul(k.c, pp)));
+          }
         } else {
           const uint32_t cp = k.pos;
           const A dx = (A)(cp & 1u), dy = (A)((cp >> 1) & 1u), dz = (A)((cp >> 2) & 1u);
@@ -763,7 +779,8 @@ int launch_tma_t(pfdtd_domain* d, const void* cur, void* past, cudaStream_t s) {
   k_update_tma<S, C, SCHEME, Lay, BATCHED><<<dim3(gx, gy, gz), Lay::THREADS, Lay::SMEM, s>>>(
       ts.halo[cur_i], ts.tile[past_i], ts.cls, Lay::MASK ? ts.mask : ts.cls, (const S*)cur,
       (S*)past, tab, (int)XE, (int)d->Y, d->XY * d->K, (int)(d->Z - 1), (int)zc,
-      (A)d->params[1], d->d_err, d->kshift, SCHEME == 3 ? d->d_iwb_sw : nullptr, -0.0f);
+      (A)d->params[1], d->d_err, d->kshift, SCHEME == 3 ? d->d_iwb_sw : nullptr, -0.0f,
+      d->class_form);
   count_launch();
   PFDTD_CK(cudaGetLastError());
   return PFDTD_OK;

@@ -33,11 +33,14 @@ def arith_dtype(precision: int):
 
 
 def default_params(octave: int = 0, scheme="forward", lam: Optional[float] = None) -> np.ndarray:
-    """[lambda, lambda^2, 1/3, octave] at lambda = 1/sqrt(3), as the reference's
-    SimulationParameters::getParameterPtrDouble (SimulationParameters.cpp:389-396);
-    lambda = 1 (its stability limit) for the IWB scheme unless `lam` is given."""
+    """[lambda, lambda^2, 1/3, octave] as the reference's
+    SimulationParameters::getParameterPtrDouble (SimulationParameters.cpp:389-396)
+    after setUpdateType, which every reference entry point calls and which sets
+    lambda = sqrt(1/3) (SimulationParameters.cpp:123-137; one ulp below the
+    constructor's 1/sqrt(3) in double); lambda = 1 (its stability limit) for
+    the IWB scheme unless `lam` is given."""
     if lam is None:
-        lam = 1.0 if scheme_code(scheme) == L.IWB else 1.0 / math.sqrt(3.0)
+        lam = 1.0 if scheme_code(scheme) == L.IWB else math.sqrt(1.0 / 3.0)
     return np.array([lam, lam * lam, 1.0 / 3.0, float(octave)], dtype=np.float64)
 
 
@@ -104,6 +107,12 @@ class Domain:
 
     def set_scheme(self, scheme) -> None:
         L.call("pfdtd_set_scheme", self.handle, scheme_code(scheme))
+
+    def set_update_form(self, form) -> None:
+        """"reference" (the reference's expression, bit for bit) or
+        "difference" (the same forward update with less float roundoff)."""
+        code = {"reference": 0, "difference": 1}[form] if isinstance(form, str) else int(form)
+        L.call("pfdtd_set_update_form", self.handle, code)
 
     def set_nodes(self, pos: np.ndarray, mat: np.ndarray) -> None:
         pos = np.ascontiguousarray(pos, dtype=np.uint8).reshape(-1)

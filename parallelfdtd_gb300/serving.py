@@ -48,6 +48,7 @@ class Request:
         self.precision = precision_code(precision)
         self.scheme = scheme_code(scheme)
         self.n_rec = 0
+        self.source_fields = self.fields
         h = C.c_void_p()
         L.call("pfdtd_request_create", *self.dims, self.fields, self.precision, self.scheme,
                self.steps, C.byref(h))
@@ -92,6 +93,9 @@ class Request:
         s = np.ascontiguousarray(samples, dtype=np.float64).reshape(n, -1)
         L.call("pfdtd_request_set_sources", self.handle, n, _p(x, C.c_int64), _p(f, C.c_int32),
                _p(ty, C.c_int32), _p(s, C.c_double), s.shape[1])
+        if n > 0:
+            used = {0} if f is None else {int(v) for v in f if 0 <= int(v) < self.fields}
+            self.source_fields = len(used) or self.fields
         return self
 
     def set_receivers(self, xyz, fields=None) -> "Request":
@@ -112,6 +116,14 @@ class Request:
         return int(b.value)
 
     def node_updates(self) -> float:
+        """Updates of the fields that carry a source: a request whose source
+        count was rounded up to a power of two is not credited for the
+        padding fields it also computes."""
+        X, Y, Z = self.dims
+        return float(X) * Y * (Z - 2) * self.steps * self.source_fields
+
+    def computed_updates(self) -> float:
+        """Every field the request computes, padding included."""
         X, Y, Z = self.dims
         return float(X) * Y * (Z - 2) * self.steps * self.fields
 
@@ -268,6 +280,7 @@ def run_trace(server: Server, requests: Sequence[Request], arrivals: Sequence[fl
     """Submit each request at its arrival time (seconds after the start),
     wait for all; returns per-request times and the aggregate figures."""
     updates = [r.node_updates() for r in requests]
+    computed = [r.computed_updates() for r in requests]
     t0 = time.perf_counter()
     tickets = []
     for req, at in zip(requests, arrivals):
@@ -289,6 +302,7 @@ def run_trace(server: Server, requests: Sequence[Request], arrivals: Sequence[fl
     tot = np.array([t[2] for t in times])
     pct = lambda a, p: float(np.percentile(a, p))
     return {"wall_s": wall, "node_updates": float(sum(updates)),
+            "computed_updates": float(sum(computed)), "requests": len(requests),
             "throughput": float(sum(updates)) / wall,
             "latency_p50_s": pct(tot, 50), "latency_p99_s": pct(tot, 99),
             "queue_p50_s": pct(q, 50), "queue_p99_s": pct(q, 99),

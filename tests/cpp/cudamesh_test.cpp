@@ -7,6 +7,7 @@
 #include <cuda_runtime.h>
 
 #include <cstring>
+#include <stdexcept>
 #include <vector>
 
 #include "App.h"
@@ -136,6 +137,11 @@ static void get_set_multi() {  // CudaMeshTest.cpp:260-303
   std::vector<unsigned int> devices(5, 0);
   mesh.makePartition(5, devices);
   CHECK_EQUAL(mesh.pressures_.size(), (size_t)5);
+  // each partition's first global slice (partitions overlap by one slice)
+  for (unsigned i = 0; i < 5; ++i)
+    CHECK_EQUAL(mesh.getMemorySplitAt(i), mesh.getFirstSliceIdx((int)i));
+  CHECK_EQUAL(mesh.getMemorySplitAt(1), 9u);
+  CHECK_THROW(mesh.getMemorySplitAt(5), std::out_of_range);
   int dev = 0, elem = 0;
   mesh.getElementIdxAndDevice(10, 10, 11, &dev, &elem);
   CHECK_EQUAL(dev, 1);

@@ -178,6 +178,20 @@ static void partition_indexing() {  // CudaMeshTest.cpp:182-218
   for (size_t j = 0; j < one[0].size(); ++j) CHECK_EQUAL(one[0][j], (unsigned)j);
 }
 
+static void split_partitions() {  // cudaMesh.h:309-318
+  CudaMesh mesh;
+  std::vector<std::vector<unsigned> > parts = mesh.getPartitionIndexing(4, 30);
+  std::vector<double*> bufs = mesh.splitPartitions<double>(parts, 12);
+  CHECK_EQUAL(bufs.size(), parts.size());
+  for (size_t i = 0; i < bufs.size(); ++i) {
+    bool zero = bufs[i] != NULL;
+    for (size_t k = 0; zero && k < 12 * parts[i].size(); ++k) zero = bufs[i][k] == 0.0;
+    CHECK_EQUAL(zero, true);
+    free(bufs[i]);
+  }
+  CHECK_THROW(mesh.getMemorySplitAt(0), std::out_of_range);  // no partitions made yet
+}
+
 int main(int argc, char** argv) {
   parameter_vector();
   sources_receivers();
@@ -190,5 +204,6 @@ int main(int argc, char** argv) {
   materials_index();
   reflectances();
   partition_indexing();
+  split_partitions();
   TEST_MAIN_END();
 }

@@ -4,8 +4,10 @@ stand-in MEX API of this folder, and link it with libpfdtd.so.
 
     python tests/mex_stub/build_gateway.py <out_dir> [reference_dir]
 
-reference_dir defaults to $PFDTD_REFERENCE_DIR, else /root/reference.  Prints
-the path of the linked host program.  Nothing is copied out of the reference.
+reference_dir defaults to where the oracle's reference build recipe finds the
+reference (oracle/build_ref.py: $PFDTD_REFERENCE_DIR, else its mount point);
+None when it is absent.  Prints the path of the linked host program.  Nothing
+is copied out of the reference.
 """
 from __future__ import annotations
 
@@ -17,8 +19,11 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 REPO = os.path.dirname(os.path.dirname(HERE))
 
 
-def reference_dir(arg: str | None = None) -> str:
-    return arg or os.environ.get("PFDTD_REFERENCE_DIR", "/root/reference")
+def reference_dir(arg: str | None = None) -> str | None:
+    if REPO not in sys.path:
+        sys.path.insert(0, REPO)
+    from oracle import build_ref
+    return build_ref.reference_dir(arg)
 
 
 def gateway_source(ref: str) -> str:
@@ -26,7 +31,10 @@ def gateway_source(ref: str) -> str:
 
 
 def build(out_dir: str, ref: str | None = None) -> str:
-    src = gateway_source(reference_dir(ref))
+    where = reference_dir(ref)
+    if where is None:
+        raise FileNotFoundError("reference sources not found (set PFDTD_REFERENCE_DIR)")
+    src = gateway_source(where)
     lib_dir = os.path.join(REPO, "parallelfdtd_gb300")
     cuda_inc = os.path.join(os.environ.get("CUDA_HOME", "/usr/local/cuda"), "include")
     inc = ["-I" + HERE, "-I" + os.path.join(REPO, "include"),

@@ -17,8 +17,12 @@ def _lib_built():
     return os.path.exists(os.path.join(os.path.dirname(B.__file__), "libpfdtd.so"))
 
 
-@pytest.mark.skipif(not os.path.exists(build_gateway.gateway_source(build_gateway.reference_dir())),
-                    reason="reference tree not present")
+def _gateway_present():
+    ref = build_gateway.reference_dir()
+    return ref is not None and os.path.exists(build_gateway.gateway_source(ref))
+
+
+@pytest.mark.skipif(not _gateway_present(), reason="reference tree not present")
 def test_reference_mex_gateway_compiles_links_and_runs(tmp_path):
     if not _lib_built():
         pytest.skip("libpfdtd.so not built")

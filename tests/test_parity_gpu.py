@@ -164,8 +164,8 @@ def test_odd_sizes_and_edges(gpu, O):
 
 def test_full_size_grid_short_run(gpu, O):
     """The 512 x 384 x 256 room with 40 boxes, 20 materials: bit-identical
-    receivers and fields after a short run (the full 2000-step run is the
-    benchmark; its size-independent checks are in test_properties_gpu)."""
+    receivers and fields after a short run (the full 2000-step run is in
+    tests/test_full_size_gpu.py and tests/test_ref_parity_gpu.py)."""
     room = rooms.boxes_room((512, 384, 256), n_boxes=40, edge=(8, 64), n_materials=20, seed=2)
     steps = 12
     rec = room.random_air_nodes(8, seed=9)
@@ -500,9 +500,9 @@ def test_iwb_open_x_faces(gpu, O, prec, variant):
 def test_iwb_tile_shapes(gpu, O, prec, shape):
     """Every IWB tile shape on the TMA path equals the oracle, with DIF walls:
     shapes 0..5 run the closure inside the streaming kernel, 6..8 leave the
-    nodes with a closed neighbour to the closure pass (which hands the DIF
-    nodes' neighbour sums to the DIF pass).  The room is not a multiple of
-    the 64- or 128-node tiles in x or of the tile rows in y."""
+    nodes with a closed neighbour to the closure pass, which also applies the
+    DIF update of those nodes.  The room is not a multiple of the 64- or
+    128-node tiles in x or of the tile rows in y."""
     from parallelfdtd_gb300 import materials
     room = rooms.boxes_room((208, 44, 36), n_boxes=6, edge=(5, 12), n_materials=6, seed=16)
     steps = 90
@@ -785,3 +785,87 @@ def test_render_pipeline(gpu):
                                                   axis=0), axis=0)
     ref = resample_poly(f, 48000, fs, axis=0, window=pf.resample_taps(48000, fs))
     assert y.shape == ref.shape and np.max(np.abs(y - ref)) <= 1e-12 * np.max(np.abs(ref))
+
+
+def _iwb_dif_room():
+    from parallelfdtd_gb300 import materials
+    room = rooms.boxes_room((208, 44, 36), n_boxes=6, edge=(5, 12), n_materials=6, seed=16)
+    flags = np.array([m % 2 for m in range(6)], np.int32)
+    table = materials.dif_table(materials.positive_real_filters(6, 3, seed=2), 3)
+    return room, flags, table
+
+
+@pytest.mark.parametrize("shape", [6, 7, 8])
+def test_iwb_closure_pass_unfused_dif(gpu, O, monkeypatch, shape):
+    """The closure pass with the DIF update left to its own pass
+    (PFDTD_IWB_DIF_UNFUSED=1, the path a DIF node without a closure record
+    takes) equals the fused closure pass and the oracle bit for bit."""
+    room, flags, table = _iwb_dif_room()
+    steps = 90
+    srcs = room.random_air_nodes(2, seed=1)
+    rec = room.random_air_nodes(4, seed=2)
+    pulse = rooms.gaussian_pulse(steps, 3.0)
+    params = default_params(scheme="iwb")
+    out = {}
+    for unfused in (False, True):
+        if unfused:
+            monkeypatch.setenv("PFDTD_IWB_DIF_UNFUSED", "1")
+        else:
+            monkeypatch.delenv("PFDTD_IWB_DIF_UNFUSED", raising=False)
+        with Domain(room.dims, "f32") as d:
+            d.set_voxels(room.bid, room.mat, centred=True)
+            d.set_materials(room.admittance)
+            d.set_params(params)
+            d.set_scheme("iwb")
+            d.set_dif_filters(flags, table)
+            d.set_kernel("tma")
+            L.call("pfdtd_set_tile", d.handle, shape)
+            d.set_sources(srcs, [1, 1], np.stack([pulse, -0.5 * pulse]))
+            d.set_receivers(rec)
+            g, _, st = d.run(steps)
+            assert st == 0
+            out[unfused] = (g, d.download_field(L.FIELD_CURRENT))
+    monkeypatch.delenv("PFDTD_IWB_DIF_UNFUSED", raising=False)
+    assert np.array_equal(out[False][0], out[True][0])
+    assert np.array_equal(out[False][1], out[True][1])
+    pos, mat = O.encode_nodes(room.bid, room.mat, True)
+    r, rP, _ = O.run(pos, mat, room.dims, room.admittance, params, [room.flat(*s) for s in srcs],
+                     [1, 1], np.stack([pulse, -0.5 * pulse]), [room.flat(*x) for x in rec], steps,
+                     scheme=3, dif=(flags, table))
+    assert np.abs(r).max() > 1e-4
+    assert np.array_equal(out[True][0], r) and np.array_equal(out[True][1], rP)
+
+
+def test_autotune_mid_run_keeps_dif_state(gpu):
+    """An IWB room with frequency-dependent walls: 40 steps, then the
+    autotuner (whose timing launches advance the fields and the DIF filter
+    states), then 50 more steps without a reset.  Receivers and fields equal
+    a run that was never autotuned, bit for bit."""
+    room, flags, table = _iwb_dif_room()
+    steps, cut = 90, 40
+    srcs = room.random_air_nodes(2, seed=1)
+    rec = room.random_air_nodes(4, seed=2)
+    pulse = rooms.gaussian_pulse(steps, 3.0)
+    params = default_params(scheme="iwb")
+    res = []
+    for tune in (False, True):
+        with Domain(room.dims, "f32") as d:
+            d.set_voxels(room.bid, room.mat, centred=True)
+            d.set_materials(room.admittance)
+            d.set_params(params)
+            d.set_scheme("iwb")
+            d.set_dif_filters(flags, table)
+            d.set_sources(srcs, [1, 1], np.stack([pulse, -0.5 * pulse]))
+            d.set_receivers(rec)
+            assert d.dif_count() > 0
+            out = np.zeros((len(rec), steps), np.float32)
+            for s in range(cut):
+                d.step(s, 1, out, steps)
+            if tune:
+                d.autotune(max_depth=0, iters=3)
+            for s in range(cut, steps):
+                d.step(s, 1, out, steps)
+            res.append((out, d.download_field(L.FIELD_CURRENT), d.download_field(L.FIELD_PAST)))
+    assert np.abs(res[0][0]).max() > 1e-4
+    for a, b in zip(res[0], res[1]):
+        assert np.array_equal(a, b)
