@@ -74,6 +74,9 @@ def parse():
     p.add_argument("--vs-f64", action="store_true",
                    help="also run the same workload with FP64 fields and report each "
                         "receiver's relative L2 error against it")
+    p.add_argument("--form", choices=["reference", "difference"], default="reference",
+                   help="arithmetic form of the forward update (difference: the same update "
+                        "with less float roundoff; see pfdtd_set_update_form)")
     p.add_argument("--tb", type=int, default=0,
                    help="temporal block depth (0 = one update kernel per step; 2, 3, 4)")
     p.add_argument("--fields", type=int, default=1,
@@ -238,11 +241,24 @@ def cpu_baseline(room, src, rec, budget_s: float, fields=1):
     t0 = time.perf_counter()
     O.run(*args, rooms.impulse(n1)[None], rec_idx, n1, threads=1)
     dt1 = time.perf_counter() - t0
+    # the 64^3 shoebox of the contract (6 wall materials, soft Gaussian at the
+    # centre, receiver (16, 40, 24)), all 500 steps
+    box = rooms.shoebox((64, 64, 64), n_materials=6, seed=1)
+    bpos, bmat = O.encode_nodes(box.bid, box.mat, centred=False)
+    c1_steps = 500
+    t0 = time.perf_counter()
+    O.run(bpos, bmat, box.dims, box.admittance, default_params(), [box.flat(32, 32, 32)], [1],
+          rooms.gaussian_pulse(c1_steps, 5.0)[None], [box.flat(16, 40, 24)], c1_steps,
+          threads=threads)
+    dtc1 = time.perf_counter() - t0
     return {"value": X * Y * (Z - 2) * n / dt, "unit": METRIC, "cores": threads,
             "kind": "port",
             "sample": f"{X}x{Y}x{Z} room, {n} leapfrog steps of one field, FP32 "
                       f"SRL forward, {threads} OpenMP threads",
             "one_thread": {"value": X * Y * (Z - 2) * n1 / dt1, "sample": f"{n1} steps"},
+            "c1_shoebox": {"value": 64 * 64 * 62 * c1_steps / dtc1,
+                           "sample": "64^3 shoebox, all 500 steps, FP32 SRL forward, "
+                                     f"{threads} OpenMP threads"},
             "cpu_model": cpu_model()}
 
 
@@ -402,6 +418,8 @@ def main():
         dom.set_params(default_params(scheme=a.scheme,
                                       lam=a.iwb_lambda if a.scheme == "iwb" else None))
         dom.set_scheme(a.scheme)
+        if a.form != "reference" and dom.precision != 1:  # the FP64 comparison run keeps
+            dom.set_update_form(a.form)                    # the reference form
 
     d = Domain(dims, prec, device=local, fields=K)
     setup(d)
@@ -530,7 +548,7 @@ def main():
                        "courant": float(default_params(scheme=a.scheme, lam=a.iwb_lambda
                                                        if a.scheme == "iwb" else None)[0]),
                        "fdtd_steps_per_step": S, "nodes": X * Y * Z, "fields": K,
-                       "temporal_block": a.tb,
+                       "temporal_block": a.tb, "update_form": a.form,
                        "bytes_per_update": bpu,
                        "parallelism": f"replicas x{world}",
                        "l2": f"inputs larger than L2 (fields 2 x {X * Y * Z * K * esize / 1e6:.0f} MB "

@@ -190,6 +190,15 @@ int pfdtd_set_scheme(pfdtd_domain* d, int scheme);
  *   orders of magnitude at the same memory traffic.  Float arithmetic only
  *   (FP32, FP16, BF16 storage); no frequency-dependent boundaries and no
  *   temporal blocking (PFDTD_ERR_UNSUPPORTED at the next run).  */
+/* Bound, in nanoseconds, of each pipeline wait inside the TMA update kernels
+ * (no counterpart in the reference; default 2 s, 0 restores it).  A wait that
+ * runs out raises the domain's error flag; the kernel stops issuing loads,
+ * waits for the loads already in flight (always with the 2 s bound) and
+ * returns, later launches of the run do nothing, and the run returns
+ * PFDTD_ERR_CUDA with the flag cleared, the context still usable.  A watchdog
+ * for stalled pipelines; tests set it very low to exercise that path. */
+int pfdtd_set_wait_limit(pfdtd_domain* d, uint64_t ns);
+
 #define PFDTD_FORM_REFERENCE 0
 #define PFDTD_FORM_DIFFERENCE 1
 int pfdtd_set_update_form(pfdtd_domain* d, int form);

@@ -6,12 +6,16 @@
 // against it.  Only the tests, the smoke check and the CPU-baseline leg of
 // the benchmark load it; nothing in the product links or calls it.
 //
-// Parity pin: the reference cannot be built here (Boost, GL and the external
-// voxelizer are missing, its gencodes predate nvcc 13), so this restatement is
-// pinned against the known-answer values the reference's own unit tests hold
-// (tests/SimulationParametersTest.cpp, tests/MaterialHandlerTest.cpp,
-// tests/CudaMeshTest.cpp) and against its partition-invariance property.
-// Field values themselves have no golden vectors in the reference.
+// Parity pin: the reference's own update, padding and node-translation
+// kernels and its host classes, compiled unchanged (oracle/build_ref.py),
+// produced the golden vectors in tests/golden/ref_fields.npz and
+// ref_host_golden.txt (tests/golden/make_ref_golden.py); this restatement
+// reproduces every one of them bit for bit (tests/test_ref_golden_cpu.py).
+// It is also pinned against the known-answer values the reference's unit
+// tests hold (tests/SimulationParametersTest.cpp, MaterialHandlerTest.cpp,
+// CudaMeshTest.cpp) and its partition-invariance property.  The IWB scheme,
+// the DIF walls, 16-bit storage and the difference form have no counterpart
+// in the reference and follow this library's written specification.
 //
 // Every function cites the reference file:line it follows.  Build with
 // -ffp-contract=off so that every product is rounded before it is summed,

@@ -69,6 +69,7 @@ _SIGNATURES = {
     "pfdtd_set_receivers": (_i32, [_vp, _i32, C.POINTER(_i64)]),
     "pfdtd_set_scheme": (_i32, [_vp, _i32]),
     "pfdtd_set_update_form": (_i32, [_vp, _i32]),
+    "pfdtd_set_wait_limit": (_i32, [_vp, C.c_uint64]),
     "pfdtd_run": (_i32, [_vp, _i64, _vp, INTERRUPT_FN, PROGRESS_FN, C.POINTER(C.c_double)]),
     "pfdtd_run_device": (_i32, [_vp, _i64, _vp]),
     "pfdtd_profile_update": (_i32, [_vp, _i32]),

@@ -278,6 +278,9 @@ struct pfdtd_domain {
   int kernel_variant = PFDTD_KERNEL_AUTO;
   int tma_tile = -1;         // tile shape of the TMA kernel, -1 automatic (stencil_tma.cu)
   int* d_err = nullptr;
+  // bound of each pipeline wait of the TMA update kernels (ns); the drain of
+  // loads in flight always keeps its own 2 s bound
+  uint64_t wait_ns = 2000000000ull;
   pfdtd::TmaState tma;
 
   // temporal blocking (stencil_tb.cu): requested depth (0 off) and the

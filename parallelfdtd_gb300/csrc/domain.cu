@@ -477,6 +477,16 @@ int pfdtd_set_quirks(pfdtd_domain* d, int quirks) {
   return PFDTD_OK;
 }
 
+int pfdtd_set_wait_limit(pfdtd_domain* d, uint64_t ns) {
+  if (int rc = check_domain(d)) return rc;
+  d->wait_ns = ns == 0 ? 2000000000ull : ns;
+  if (d->graph.exec) {  // the limit is a kernel argument baked into the graph
+    cudaGraphExecDestroy(d->graph.exec);
+    d->graph.exec = nullptr;
+  }
+  return PFDTD_OK;
+}
+
 int pfdtd_set_update_form(pfdtd_domain* d, int form) {
   if (int rc = check_domain(d)) return rc;
   if (form != PFDTD_FORM_REFERENCE && form != PFDTD_FORM_DIFFERENCE)

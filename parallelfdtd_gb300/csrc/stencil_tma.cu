@@ -102,9 +102,10 @@ __device__ __forceinline__ uint64_t global_ns() {
   return t;
 }
 
-// Wait for the phase with the given parity, for at most kWaitLimitNs; false
-// on expiry.
-__device__ __forceinline__ bool mbar_wait(uint32_t bar, uint32_t parity) {
+// Wait for the phase with the given parity, for at most limit_ns; false on
+// expiry.
+__device__ __forceinline__ bool mbar_wait(uint32_t bar, uint32_t parity,
+                                          uint64_t limit_ns = kWaitLimitNs) {
   uint64_t start = 0;
   for (uint32_t i = 0;; ++i) {
     uint32_t done;
@@ -119,7 +120,7 @@ __device__ __forceinline__ bool mbar_wait(uint32_t bar, uint32_t parity) {
     if ((i & 255) == 0) {
       const uint64_t now = global_ns();
       if (i == 0) start = now;
-      else if (now - start > kWaitLimitNs) return false;
+      else if (now - start > limit_ns) return false;
     }
   }
 }
@@ -264,9 +265,10 @@ __device__ __forceinline__ void iwb_plane_sums(const S* pl, int si, const S* __r
 
 // Producer of the stage ring (one thread): stage k receives the P^n plane
 // z0-1+k of the tile with its halo and, from k = 2 on, the P^{n-1} plane and
-// the class ids of plane z0+k-2.  Every wait is bounded; on expiry it raises
-// the error flag and the abort flag, then waits (bounded) for the loads it
-// already issued before returning.
+// the class ids of plane z0+k-2.  Every wait is bounded (wait_ns for a free
+// stage); on expiry it raises the error flag and the abort flag, then waits
+// for the loads it already issued, with the full kWaitLimitNs whatever
+// wait_ns is, so that no bulk copy is in flight when the CTA exits.
 template <typename Lay>
 __device__ __forceinline__ void tma_producer(const CUtensorMap* map_cur,
                                              const CUtensorMap* map_past,
@@ -274,13 +276,14 @@ __device__ __forceinline__ void tma_producer(const CUtensorMap* map_cur,
                                              const CUtensorMap* map_mask, unsigned char* smem,
                                              uint32_t bar_full, uint32_t bar_empty,
                                              volatile int* abort_flag, int x0, int y0, int z0,
-                                             int Y, int K, int kshift, int* err) {
+                                             int Y, int K, int kshift, int* err,
+                                             uint64_t wait_ns) {
   constexpr int NS = Lay::NS, H = Lay::H;
   int issued = 0;
   for (int k = 0; k < K; ++k) {
     const int slot = k % NS;
     if (k >= NS) {
-      if (!mbar_wait(bar_empty + 8 * slot, (uint32_t)((k / NS - 1) & 1))) {
+      if (!mbar_wait(bar_empty + 8 * slot, (uint32_t)((k / NS - 1) & 1), wait_ns)) {
         atomicExch(err, 1);
         *abort_flag = 1;
         break;
@@ -319,7 +322,8 @@ k_update_tma(const __grid_constant__ CUtensorMap map_cur, const __grid_constant_
              const __grid_constant__ CUtensorMap map_mask, const S* __restrict__ P,
              S* __restrict__ Pp, ClassTab<typename Store<S>::A> tab, int X, int Y, int64_t XY,
              int z_last, int zc, typename Store<S>::A l2, int* __restrict__ err, int kshift = 0,
-             float* __restrict__ iwb_sw = nullptr, float nzf = -0.0f, int form = 0) {
+             float* __restrict__ iwb_sw = nullptr, float nzf = -0.0f, int form = 0,
+             uint64_t wait_ns = kWaitLimitNs) {
   using A = typename Store<S>::A;
   using R = Rn<A>;
   using St = Store<S>;
@@ -366,7 +370,7 @@ k_update_tma(const __grid_constant__ CUtensorMap map_cur, const __grid_constant_
   if (warp == kConsumerWarps) {
     if (lane == 0)
       tma_producer<Lay>(&map_cur, &map_past, &map_cls, &map_mask, smem, bar_full, bar_empty,
-                        abort_flag, x0, y0, z0, Y, K, kshift, err);
+                        abort_flag, x0, y0, z0, Y, K, kshift, err, wait_ns);
     return;
   }
 
@@ -380,7 +384,7 @@ k_update_tma(const __grid_constant__ CUtensorMap map_cur, const __grid_constant_
   const int y = y0 + ly;
   const bool active = (x < X) && (y < Y);  // X is a multiple of 4: all 4 or none
   const int si = (ly + 1) * PW + lx + H;   // centre of the thread's first node
-  bool ok = mbar_wait(bar_full, 0) && mbar_wait(bar_full + 8, 0);
+  bool ok = mbar_wait(bar_full, 0, wait_ns) && mbar_wait(bar_full + 8, 0, wait_ns);
   // IWB: raw in-plane sums of planes z-1 (m) and z (c) carried along the
   // z-march; each plane's sums are computed once and used for three planes.
   float cm0[kVec], cm1[kVec], cm2[kVec], cc0[kVec], cc1[kVec], cc2[kVec];
@@ -396,7 +400,7 @@ k_update_tma(const __grid_constant__ CUtensorMap map_cur, const __grid_constant_
   }
   for (int j = 0; j < nplanes && ok; ++j) {
     const int sm = j % NS, sc_ = (j + 1) % NS, sp_ = (j + 2) % NS;
-    if (!mbar_wait(bar_full + 8 * sp_, (uint32_t)(((j + 2) / NS) & 1))) {
+    if (!mbar_wait(bar_full + 8 * sp_, (uint32_t)(((j + 2) / NS) & 1), wait_ns)) {
       ok = false;
       break;
     }
@@ -540,8 +544,19 @@ k_update_tma(const __grid_constant__ CUtensorMap map_cur, const __grid_constant_
                                __ldg(tab.c + cid[e]), __ldg(tab.pos + cid[e])};
         };
         const f2 l22 = pk2(l2, l2), nz = pk2(nzf, nzf);
+        // elements 2h, 2h+1 as a float pair; a 16-bit pair is converted as
+        // one 32-bit word (both conversions are exact)
         auto pr = [](const V4<S>& v, int h) -> f2 {
-          return pk2(St::load(v.v[2 * h]), St::load(v.v[2 * h + 1]));
+          if constexpr (std::is_same<S, __half>::value) {
+            const float2 f = __half22float2(__halves2half2(v.v[2 * h], v.v[2 * h + 1]));
+            return pk2(f.x, f.y);
+          } else if constexpr (std::is_same<S, __nv_bfloat16>::value) {
+            const uint32_t w = (uint32_t)__bfloat16_as_ushort(v.v[2 * h]) |
+                               ((uint32_t)__bfloat16_as_ushort(v.v[2 * h + 1]) << 16);
+            return pk2(__uint_as_float(w << 16), __uint_as_float(w & 0xFFFF0000u));
+          } else {
+            return pk2(St::load(v.v[2 * h]), St::load(v.v[2 * h + 1]));
+          }
         };
         f2 aa[2], bb[2], cc[2], ee[2], xm2[2], xp2[2];
         if constexpr (BATCHED) {
@@ -780,7 +795,7 @@ int launch_tma_t(pfdtd_domain* d, const void* cur, void* past, cudaStream_t s) {
       ts.halo[cur_i], ts.tile[past_i], ts.cls, Lay::MASK ? ts.mask : ts.cls, (const S*)cur,
       (S*)past, tab, (int)XE, (int)d->Y, d->XY * d->K, (int)(d->Z - 1), (int)zc,
       (A)d->params[1], d->d_err, d->kshift, SCHEME == 3 ? d->d_iwb_sw : nullptr, -0.0f,
-      d->class_form);
+      d->class_form, d->wait_ns);
   count_launch();
   PFDTD_CK(cudaGetLastError());
   return PFDTD_OK;

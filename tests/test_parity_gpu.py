@@ -869,3 +869,36 @@ def test_autotune_mid_run_keeps_dif_state(gpu):
     assert np.abs(res[0][0]).max() > 1e-4
     for a, b in zip(res[0], res[1]):
         assert np.array_equal(a, b)
+
+
+def test_pipeline_wait_timeout_reports_and_recovers(gpu, O):
+    """The bounded waits of the TMA update kernel: with every pipeline wait
+    limited to 1 ns, waits run out, the kernel raises the domain's error flag
+    (after waiting, with its full bound, for the loads it already issued),
+    later launches do nothing, and the run reports PFDTD_ERR_CUDA.  The same
+    domain, back at the default bound, then runs and equals the oracle."""
+    room = rooms.boxes_room((256, 96, 64), n_boxes=5, edge=(6, 16), n_materials=6, seed=43)
+    steps = 60
+    src = room.random_air_nodes(1, seed=1)
+    rec = room.random_air_nodes(3, seed=2)
+    pulse = rooms.gaussian_pulse(steps, 3.0)
+    with Domain(room.dims, "f32") as d:
+        d.set_voxels(room.bid, room.mat, centred=False)
+        d.set_materials(room.admittance)
+        d.set_params()
+        d.set_kernel("tma")
+        d.set_sources(src, [1], pulse[None])
+        d.set_receivers(rec)
+        L.call("pfdtd_set_wait_limit", d.handle, 1)
+        with pytest.raises(L.PfdtdError) as ex:
+            d.run(steps)
+        assert ex.value.status == L.ERR_CUDA and "timed out" in str(ex.value)
+        L.call("pfdtd_set_wait_limit", d.handle, 0)
+        d.reset_fields()
+        g, _, st = d.run(steps)
+        assert st == 0 and d.kernel() == "tma"
+    pos, mat = O.encode_nodes(room.bid, room.mat, False)
+    r, _, _ = O.run(pos, mat, room.dims, room.admittance, default_params(),
+                    [room.flat(*src[0])], [1], pulse[None], [room.flat(*x) for x in rec], steps)
+    assert np.abs(r).max() > 1e-4
+    assert np.array_equal(g, r)

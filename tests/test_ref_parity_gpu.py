@@ -155,3 +155,53 @@ def test_full_room_full_length_vs_reference_gpu(gpu, R, scheme, double):
                                fields=False)
     err = rel_l2(out, rf)
     assert err <= TOL[double], f"vs contracted reference: relative L2 {err:.3e}"
+
+
+def test_reference_kernel_speed(gpu, R):
+    """Times the reference's own forward kernel (as nvcc compiles it by
+    default for sm_103a) with launchFDTD3d's host sequence against this
+    library's run on the benchmark room, 200 steps, FP32.  Both give the same
+    receivers within the contract tolerance; this library must be faster.
+    The figures are printed (and written to $PFDTD_REPORT_DIR when set)."""
+    import time
+    room = c2_room()
+    steps = 200
+    recs = room.random_air_nodes(8, seed=9)
+    src = room.random_air_nodes(1, seed=8)[0]
+    X, Y, _ = room.dims
+    flat = lambda c: c[2] * X * Y + c[1] * X + c[0]  # noqa: E731
+    params = default_params(octave=1).astype(np.float32)
+    table = room.admittance.astype(np.float32).reshape(-1)
+    samples = rooms.impulse(steps)[None].astype(np.float32)
+    t0 = time.perf_counter()
+    rf, _, _, _, kms = R.run_gpu(room.bid, room.mat, room.dims, "forward", table, params,
+                                 [flat(src)], samples, [flat(r) for r in recs], steps,
+                                 fields=False)
+    ref_wall = time.perf_counter() - t0
+    with Domain(room.dims, "f32") as d:
+        d.set_voxels(room.bid, room.mat, centred=False)
+        d.set_materials(room.admittance)
+        d.set_params(params.astype(np.float64))
+        d.set_quirks(L.QUIRK_SOFTSRC)
+        d.set_sources([src], [1], samples)
+        d.set_receivers(recs)
+        d.run(steps)  # warm-up: class build, graph capture
+        t0 = time.perf_counter()
+        out, sec_per_step, st = d.run(steps)
+        ours_wall = time.perf_counter() - t0
+    assert st == 0
+    assert rel_l2(out, rf) <= TOL[False]
+    updates = float(X) * Y * (room.dims[2] - 2) * steps
+    rep = {"room": "512x384x256 boxes room", "steps": steps,
+           "reference_kernel_node_updates_per_s": updates / (kms * 1e-3),
+           "reference_host_loop_node_updates_per_s": updates / ref_wall,
+           "this_library_node_updates_per_s": updates / ours_wall,
+           "reference_kernel_ms_per_step": kms / steps,
+           "this_library_ms_per_step": ours_wall * 1e3 / steps}
+    print(json.dumps(rep))
+    out_dir = os.environ.get("PFDTD_REPORT_DIR")
+    if out_dir:
+        os.makedirs(out_dir, exist_ok=True)
+        with open(os.path.join(out_dir, "reference_kernel_speed.json"), "w") as f:
+            json.dump(rep, f, indent=1)
+    assert rep["this_library_node_updates_per_s"] > rep["reference_kernel_node_updates_per_s"]
