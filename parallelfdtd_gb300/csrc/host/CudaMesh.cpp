@@ -84,7 +84,7 @@ void CudaMesh::setupCommon(unsigned char* d_position_ptr, unsigned char* d_mater
         "CudaMesh::setupMesh - boundary count");
   num_air_elements_total_ = air;
   num_boundary_elements_total_ = boundary;
-  c_log_msg(LOG_INFO, "CudaMesh::setupMesh - dim x: %u y: %u z: %u, air %u, boundary %u", dim_x_,
+  c_log_msg(LOG_INFO, "mesh %u x %u x %u: %u air nodes, %u boundary nodes", dim_x_,
             dim_y_, dim_z_, air, boundary);
 }
 
@@ -321,7 +321,7 @@ double CudaMesh::getSampleValue(unsigned int x, unsigned int y, unsigned int z) 
 
 double CudaMesh::getSampleAtValue(unsigned int x, unsigned int y, unsigned int z, unsigned int p) {
   if (z > partition_indexing_.at(p).size()) {
-    c_log_msg(LOG_WARNING, "CudaMesh::getSampleAt - z %u out of range %u", z,
+    c_log_msg(LOG_WARNING, "slice %u is outside the partition (%u slices); sample read as 0", z,
               (unsigned)partition_indexing_.at(p).size());
     return 0.0;
   }

@@ -20,7 +20,7 @@ void MaterialHandler::addMaterials(float* material_ptr, unsigned int number_of_s
 // material or appends a new one (MaterialHandler.cpp:47-65, :186-204).
 unsigned int MaterialHandler::addSurfaceMaterial(std::vector<float> coefs) {
   if (number_of_coefficients_ != coefs.size())
-    c_log_msg(LOG_ERROR, "MaterialHandler::addSurfaceMaterial - invalid number of coefficients %u, should be %u",
+    c_log_msg(LOG_ERROR, "material rows carry %u coefficients; this handler expects %u",
               (unsigned)coefs.size(), (unsigned)MATERIAL_COEF_NUM);
   while (coefs.size() <= MATERIAL_COEF_NUM) coefs.push_back(0.f);
   const unsigned int idx = checkIfUnique(coefs);
@@ -31,7 +31,7 @@ unsigned int MaterialHandler::addSurfaceMaterial(std::vector<float> coefs) {
 
 float MaterialHandler::getUniqueCoefAt(unsigned int material, unsigned int coef_idx) {
   if (coef_idx >= (unsigned)MATERIAL_COEF_NUM) {
-    c_log_msg(LOG_ERROR, "MaterialHandler::getUniqueCoefAt - invalid index %u", coef_idx);
+    c_log_msg(LOG_ERROR, "coefficient index %u is past the 20 per material", coef_idx);
     throw std::out_of_range("Coef idx out of range");
   }
   return unique_coefficients_.at(material).coefs[coef_idx];
@@ -39,7 +39,7 @@ float MaterialHandler::getUniqueCoefAt(unsigned int material, unsigned int coef_
 
 float MaterialHandler::getSurfaceCoefAt(unsigned int surface, unsigned int coef_idx) {
   if (coef_idx >= (unsigned)MATERIAL_COEF_NUM) {
-    c_log_msg(LOG_ERROR, "MaterialHandler::getSurfaceCoefAt - invalid index %u", coef_idx);
+    c_log_msg(LOG_ERROR, "coefficient index %u is past the 20 per surface", coef_idx);
     throw std::out_of_range("Coef idx out of range");
   }
   return getUniqueCoefAt(material_indices_.at(surface), coef_idx);
@@ -113,7 +113,7 @@ void MaterialHandler::setGlobalMaterial(unsigned int number_of_surfaces, float c
 
 void MaterialHandler::setMaterialIndexAt(unsigned int surface_idx, unsigned char material_idx) {
   if (surface_idx >= number_of_surfaces_) {
-    c_log_msg(LOG_INFO, "MaterialHandler::setMaterialIndexAt - surface index %u out of bounds %u, returning",
+    c_log_msg(LOG_INFO, "no surface %u (there are %u); material index left unchanged",
               surface_idx, number_of_surfaces_);
     return;
   }

@@ -25,7 +25,7 @@ void SimulationParameters::readGridIr(std::string ir_fp) {
   grid_ir_.clear();
   std::ifstream in(ir_fp.c_str());
   if (!in.good()) {
-    c_log_msg(LOG_DEBUG, "SimulationParameters::readGridIr - invalid file %s", ir_fp.c_str());
+    c_log_msg(LOG_DEBUG, "grid impulse response file %s could not be read", ir_fp.c_str());
     version_ = nextVersion();
     return;
   }
@@ -50,7 +50,7 @@ void SimulationParameters::addSource(Source src) {
 
 void SimulationParameters::updateSourceAt(unsigned int i, Source src) {
   if (i >= sources_.size())
-    c_log_msg(LOG_ERROR, "SimulationParameters::updateSourceAt : index %u out of range", i);
+    c_log_msg(LOG_ERROR, "no source %u to update", i);
   sources_.at(i) = src;
   version_ = nextVersion();
 }
@@ -59,14 +59,14 @@ void SimulationParameters::updateSourceAt(unsigned int i, Source src) {
 // (SimulationParameters.cpp:63) but stores into the receiver list.
 void SimulationParameters::updateReceiverAt(unsigned int i, Receiver rec) {
   if (i >= sources_.size())
-    c_log_msg(LOG_ERROR, "SimulationParameters::updateReceiverAt : index %u out of range", i);
+    c_log_msg(LOG_ERROR, "no receiver %u to update", i);
   receivers_.at(i) = rec;
   version_ = nextVersion();
 }
 
 void SimulationParameters::removeSource(unsigned int i) {
   if (i >= sources_.size()) {
-    c_log_msg(LOG_ERROR, "SimulationParameters::removeSource : index %u out of range", i);
+    c_log_msg(LOG_ERROR, "no source %u to remove", i);
     throw std::out_of_range("SimulationParameters::removeSource: idx out of range");
   }
   sources_.erase(sources_.begin() + i);
@@ -75,7 +75,7 @@ void SimulationParameters::removeSource(unsigned int i) {
 
 void SimulationParameters::removeReceiver(unsigned int i) {
   if (i >= receivers_.size()) {
-    c_log_msg(LOG_ERROR, "SimulationParameters::removeReceiver : index %u out of range", i);
+    c_log_msg(LOG_ERROR, "no receiver %u to remove", i);
     throw std::out_of_range("SimulationParameters::removeReceiver: idx out of range");
   }
   receivers_.erase(receivers_.begin() + i);
@@ -89,7 +89,7 @@ void SimulationParameters::resetSourcesAndReceivers() {
 }
 
 void SimulationParameters::addInputData(float* data, unsigned int number_of_samples) {
-  if (!data) c_log_msg(LOG_WARNING, "SimulationParameters::addInputData : invalid input data (NULL)");
+  if (!data) c_log_msg(LOG_WARNING, "input data pointer is null; nothing added");
   std::vector<float> v(number_of_samples, 0.f);
   if (data)
     for (unsigned int i = 0; i < number_of_samples; ++i) v[i] = data[i];
@@ -132,7 +132,7 @@ double SimulationParameters::getSourceSampleDouble(unsigned int source_idx, unsi
 // vector::at, SimulationParameters.cpp:161-174); past the end gives 0.
 float SimulationParameters::getInputDataSample(unsigned int idx, unsigned int sample) {
   if (idx >= source_input_data_.size())
-    c_log_msg(LOG_ERROR, "SimulationParameters::getInputDataSample : invalid data index: %u", idx);
+    c_log_msg(LOG_ERROR, "no input data vector %u", idx);
   const std::vector<float>& v = source_input_data_.at(idx);
   if (sample >= v.size()) return 0.f;
   return v.at(sample);
@@ -140,7 +140,7 @@ float SimulationParameters::getInputDataSample(unsigned int idx, unsigned int sa
 
 double SimulationParameters::getInputDataSampleDouble(unsigned int idx, unsigned int sample) {
   if (idx >= source_input_data_double_.size())
-    c_log_msg(LOG_ERROR, "SimulationParameters::getInputDataSampleDouble : invalid data index: %u", idx);
+    c_log_msg(LOG_ERROR, "no input data vector %u (double)", idx);
   const std::vector<double>& v = source_input_data_double_.at(idx);
   if (sample >= v.size()) return 0.0;
   return v.at(sample);
@@ -268,7 +268,7 @@ float* SimulationParameters::getSourceVectorAt(unsigned int source_idx) {
     if (pfdtd_transparent_source(regular.data(), (int64_t)regular.size(),
                                  grid_ir_.empty() ? nullptr : grid_ir_.data(),
                                  (int64_t)grid_ir_.size(), v.data(), dev) != PFDTD_OK) {
-      c_log_msg(LOG_ERROR, "SimulationParameters::getSourceVectorAt - %s", pfdtd_last_error());
+      c_log_msg(LOG_ERROR, "transparent source vector: %s", pfdtd_last_error());
       throw(-1);
     }
     source_output_data_.at(source_idx) = v;

@@ -102,10 +102,31 @@ __device__ __forceinline__ uint64_t global_ns() {
   return t;
 }
 
+// Non-blocking test of the phase with the given parity.
+__device__ __forceinline__ bool mbar_test(uint32_t bar, uint32_t parity) {
+  uint32_t done;
+  asm volatile(
+      "{\n\t.reg .pred p;\n\t"
+      "mbarrier.test_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+      "selp.u32 %0, 1, 0, p;\n\t}"
+      : "=r"(done)
+      : "r"(bar), "r"(parity)
+      : "memory");
+  return done != 0;
+}
+
 // Wait for the phase with the given parity, for at most limit_ns; false on
-// expiry.
+// expiry.  A bound under 1 ms (a watchdog set short) polls without blocking
+// and reads the clock at every poll, since a blocking try_wait may itself
+// sleep longer than such a bound.
 __device__ __forceinline__ bool mbar_wait(uint32_t bar, uint32_t parity,
                                           uint64_t limit_ns = kWaitLimitNs) {
+  if (limit_ns < 1000000ull) {
+    const uint64_t t0 = global_ns();
+    while (!mbar_test(bar, parity))
+      if (global_ns() - t0 > limit_ns) return false;
+    return true;
+  }
   uint64_t start = 0;
   for (uint32_t i = 0;; ++i) {
     uint32_t done;
@@ -398,6 +419,9 @@ k_update_tma(const __grid_constant__ CUtensorMap map_cur, const __grid_constant_
                                        g0 + XY, x, X, no_mask, cc0, cc0, cc1, cc2);
     }
   }
+  // IWB: unrolled by three, the period of the plane-sum registers' rotation,
+  // so the rotation is a renaming rather than register moves
+#pragma unroll(SCHEME == 3 ? 3 : 1)
   for (int j = 0; j < nplanes && ok; ++j) {
     const int sm = j % NS, sc_ = (j + 1) % NS, sp_ = (j + 2) % NS;
     if (!mbar_wait(bar_full + 8 * sp_, (uint32_t)(((j + 2) / NS) & 1), wait_ns)) {
@@ -846,7 +870,9 @@ int launch_tma_s<float>(pfdtd_domain* d, const void* cur, void* past, cudaStream
   if (d->K > 1)  // 256 elements (256/K nodes) x 4 rows
     return launch_tma_batched<float, Layout<float, uint8_t, 256, 4, 8, false>,
                               Layout<float, uint16_t, 256, 4, 8, false>>(d, cur, past, s);
-  switch (d->tma_tile < 0 ? auto_tile(d) : d->tma_tile) {
+  // ids 9 and 10 name IWB-only shapes: the 7-point update takes its
+  // automatic tile for them
+  switch (d->tma_tile < 0 || d->tma_tile > 8 ? auto_tile(d) : d->tma_tile) {
 #define PFDTD_CASE(id, tx, ty, ns, xh)                                                    \
   case id:                                                                                \
     return launch_tma_l<float, Layout<float, uint8_t, tx, ty, ns, xh>,                     \
@@ -875,7 +901,7 @@ int launch_tma_16(pfdtd_domain* d, const void* cur, void* past, cudaStream_t s) 
   if (d->K > 1)
     return launch_tma_batched<S, Layout<S, uint8_t, 256, 8, 8, false, false, 2>,
                               Layout<S, uint16_t, 256, 8, 8, false, false, 2>>(d, cur, past, s);
-  switch (d->tma_tile < 0 ? auto_tile16(d) : d->tma_tile) {
+  switch (d->tma_tile < 0 || d->tma_tile > 3 ? auto_tile16(d) : d->tma_tile) {
 #define PFDTD_CASE16(id, tx, ty, ns, xh)                                                  \
   case id:                                                                                \
     return launch_tma_l<S, Layout<S, uint8_t, tx, ty, ns, xh, false, 2>,                   \
@@ -914,7 +940,8 @@ int launch_tma_s<double>(pfdtd_domain* d, const void* cur, void* past, cudaStrea
 // fit).  Without masks, every node takes the open sums in the kernel and the
 // closure nodes are updated by the sparse closure pass after it: 6 = 128 x 8
 // (288 threads), 6 stages, three CTAs per SM (the default), 7 = 128 x 4 (160
-// threads), 8 stages, four CTAs, 8 = 128 x 8, 8 stages, two CTAs.  With masks a warp that holds one closure
+// threads), 8 stages, four CTAs, 8 = 128 x 8, 8 stages, two CTAs, 9 = 128 x 8,
+// 5 stages, four CTAs, 10 = 128 x 4, 6 stages, six CTAs.  With masks a warp that holds one closure
 // node runs the substitution for all its lanes, and in the tiles along the x
 // walls that is every warp; the split keeps the streaming kernel on the open
 // path and leaves the ~2 % closure nodes to the gather pass.  Measured on the
@@ -936,8 +963,10 @@ int launch_iwb_l(pfdtd_domain* d, const void* cur, void* past, cudaStream_t s) {
 template <typename S, typename C>
 int launch_iwb_c(pfdtd_domain* d, const void* cur, void* past, cudaStream_t s) {
   int tile = d->tma_tile;
-  if (tile < 0 || tile > 8) tile = 6;
+  if (tile < 0 || tile > 10) tile = 6;
   switch (tile) {
+    case 9: return launch_iwb_l<S, C, 128, 8, 5, 4, false>(d, cur, past, s);
+    case 10: return launch_iwb_l<S, C, 128, 4, 6, 6, false>(d, cur, past, s);
     case 0: return launch_iwb_l<S, C, 64, 16, 8>(d, cur, past, s);
     case 1: return launch_iwb_l<S, C, 128, 8, 8>(d, cur, past, s);
     case 2: return launch_iwb_l<S, C, 128, 4, 5>(d, cur, past, s);
@@ -981,7 +1010,7 @@ bool uses_tma(const pfdtd_domain* d) {
 }
 
 // The TMA path needs 16-byte aligned rows for the fields and class ids.
-int tma_tile_count() { return 9; }
+int tma_tile_count() { return 11; }
 
 bool tma_supported(const pfdtd_domain* d) {
   // Batched fields: a thread's 4 elements must be 4 fields of one node, and

@@ -496,10 +496,10 @@ def test_iwb_open_x_faces(gpu, O, prec, variant):
 
 
 @pytest.mark.parametrize("prec", ["f32", "bf16"])
-@pytest.mark.parametrize("shape", list(range(9)))
+@pytest.mark.parametrize("shape", list(range(11)))
 def test_iwb_tile_shapes(gpu, O, prec, shape):
     """Every IWB tile shape on the TMA path equals the oracle, with DIF walls:
-    shapes 0..5 run the closure inside the streaming kernel, 6..8 leave the
+    shapes 0..5 run the closure inside the streaming kernel, 6..10 leave the
     nodes with a closed neighbour to the closure pass, which also applies the
     DIF update of those nodes.  The room is not a multiple of the 64- or
     128-node tiles in x or of the tile rows in y."""
@@ -795,7 +795,7 @@ def _iwb_dif_room():
     return room, flags, table
 
 
-@pytest.mark.parametrize("shape", [6, 7, 8])
+@pytest.mark.parametrize("shape", [6, 7, 8, 9, 10])
 def test_iwb_closure_pass_unfused_dif(gpu, O, monkeypatch, shape):
     """The closure pass with the DIF update left to its own pass
     (PFDTD_IWB_DIF_UNFUSED=1, the path a DIF node without a closure record
