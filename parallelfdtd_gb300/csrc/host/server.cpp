@@ -107,14 +107,35 @@ struct pfdtd_server {
 
 namespace {
 
+// x extent of the domain a request runs on.  The TMA update kernels need the
+// rows of node bytes 16-byte aligned (X a multiple of 16); other rooms run the
+// slower z-march kernel.  A request whose x = X-1 face holds no inside node,
+// and whose sources and receivers lie below X, runs on a domain padded with
+// outside nodes up to the next multiple of 16, as the reference pads its
+// meshes to the block size (cudaMesh.cu:253-304).  No inside node then reads
+// a different neighbour (the padding and the x = X-1 face are outside and
+// stay 0), so the receivers are those of the unpadded room.
+int64_t domain_x(const pfdtd_request* r) {
+  const int64_t X = r->X, Xp = (X + 15) / 16 * 16;
+  if (Xp == X || !r->nodes_set) return X;
+  for (int i = 0; i < r->n_src; ++i)
+    if (r->src_xyz[3 * (size_t)i] >= X) return X;
+  for (int i = 0; i < r->n_rec; ++i)
+    if (r->rec_xyz[3 * (size_t)i] >= X) return X;
+  for (int64_t row = 0; row < r->Y * r->Z; ++row)
+    if (r->pos[(size_t)(row * X + X - 1)] & 0x80u) return X;
+  return Xp;
+}
+
 uint64_t estimate_bytes(const pfdtd_request* r) {
   const uint64_t es = storage_size(r->precision), as = arith_size(r->precision);
-  const uint64_t N = (uint64_t)(r->X * r->Y * r->Z), K = (uint64_t)r->fields;
+  const uint64_t DX = (uint64_t)domain_x(r);
+  const uint64_t N = (uint64_t)(DX * r->Y * r->Z), K = (uint64_t)r->fields;
   const uint64_t align = 256 / es;
-  const uint64_t margin = (((uint64_t)r->X + 64) * K + align - 1) / align * align;
+  const uint64_t margin = ((DX + 64) * K + align - 1) / align * align;
   const uint64_t nfields = r->tb_depth >= 2 ? 4 : 2;
   uint64_t b = nfields * (N * K + 2 * margin) * es;
-  b += 2 * (N + 1 + (uint64_t)r->X) + N + 64;                  // node bytes, class ids
+  b += 2 * (N + 1 + DX) + N + 64;                              // node bytes, class ids
   b += (uint64_t)r->n_rec * (uint64_t)r->steps * as;         // receiver buffer
   b += (uint64_t)r->n_src * (uint64_t)r->n_samples * as + 4096;  // sources
   bool dif = false;
@@ -137,8 +158,18 @@ uint64_t estimate_bytes(const pfdtd_request* r) {
 int admit(pfdtd_server* s, Job& j) {
   pfdtd_request* r = j.req;
   pfdtd_domain* d = nullptr;
-  int rc = pfdtd_create_batched(r->X, r->Y, r->Z, r->fields, r->precision, s->device, &d);
+  const int64_t DX = domain_x(r);
+  int rc = pfdtd_create_batched(DX, r->Y, r->Z, r->fields, r->precision, s->device, &d);
   if (rc) return rc;
+  std::vector<uint8_t> ppos, pmat;  // node bytes re-laid on the padded rows
+  if (DX != r->X) {
+    ppos.assign((size_t)(DX * r->Y * r->Z), 0);
+    pmat.assign(ppos.size(), 0);
+    for (int64_t row = 0; row < r->Y * r->Z; ++row) {
+      std::memcpy(&ppos[(size_t)(row * DX)], &r->pos[(size_t)(row * r->X)], (size_t)r->X);
+      std::memcpy(&pmat[(size_t)(row * DX)], &r->mat[(size_t)(row * r->X)], (size_t)r->X);
+    }
+  }
   const size_t as = arith_size(r->precision);
   std::vector<uint8_t> samples(r->samples.size() * as);
   if (as == 8) {
@@ -149,7 +180,9 @@ int admit(pfdtd_server* s, Job& j) {
       std::memcpy(samples.data() + 4 * i, &v, 4);
     }
   }
-  if (!rc) rc = pfdtd_set_nodes(d, r->pos.data(), r->mat.data(), 0);
+  if (!rc)
+    rc = DX != r->X ? pfdtd_set_nodes(d, ppos.data(), pmat.data(), 0)
+                    : pfdtd_set_nodes(d, r->pos.data(), r->mat.data(), 0);
   if (!rc) rc = pfdtd_set_scheme(d, r->scheme);
   if (!rc) rc = pfdtd_set_materials(d, r->materials.data(), r->n_mat, r->n_coef);
   if (!rc && !r->dif_flags.empty())

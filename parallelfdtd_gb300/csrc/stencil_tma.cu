@@ -536,7 +536,9 @@ k_update_tma(const __grid_constant__ CUtensorMap map_cur, const __grid_constant_
       if (BATCHED) {
         const int kk = 1 << kshift;
         vxm = lx >= kk ? lds4(Pc + si - kk) : ldg4(P + idx - kk);
-        vxp = lx + kk < kTX ? lds4(Pc + si + kk) : ldg4(P + idx + kk);
+        // the last node of a row reads its flat-index neighbour (the next
+        // row's first node) from global memory, also in a partly filled tile
+        vxp = (lx + kk < kTX && x + kk < X) ? lds4(Pc + si + kk) : ldg4(P + idx + kk);
         const unsigned c = Cl[ly * (kTX >> kshift) + (lx >> kshift)];
 #pragma unroll
         for (int e = 0; e < kVec; ++e) cid[e] = c;
@@ -1015,10 +1017,12 @@ int tma_tile_count() { return 11; }
 bool tma_supported(const pfdtd_domain* d) {
   // Batched fields: a thread's 4 elements must be 4 fields of one node, and
   // the class box (tile elements / K, at least 16 bytes) must stay valid.
+  // A row that ends inside a tile is handled (TMA fills past the row end with
+  // zeros, stores stop at the row end, and the row's last node reads its
+  // flat-index neighbour from global memory).
   if (d->K > 1) {
     const int tile = d->precision == PFDTD_F64 ? 128 : 256;
     if (d->K % 4 != 0 || (tile / d->K) * d->cls_bytes < 16) return false;
-    if ((d->X * d->K) % tile != 0) return false;
   }
   if ((d->X * (int64_t)d->esize) % 16 != 0) return false;
   if ((d->X * (int64_t)d->cls_bytes) % 16 != 0) return false;

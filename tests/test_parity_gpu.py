@@ -902,3 +902,39 @@ def test_pipeline_wait_timeout_reports_and_recovers(gpu, O):
                     [room.flat(*src[0])], [1], pulse[None], [room.flat(*x) for x in rec], steps)
     assert np.abs(r).max() > 1e-4
     assert np.array_equal(g, r)
+
+
+@pytest.mark.parametrize("fields,prec", [(4, "f32"), (8, "f32"), (8, "f16"), (4, "f64")])
+def test_batched_partly_filled_tiles(gpu, O, fields, prec):
+    """Batched fields on the TMA path when a row of X*K elements ends inside
+    a 256-element tile (X = 80: 320 or 640 elements), with inside nodes on
+    both x faces so that the last node of a row reads the next row's first
+    node through the flat index: every field equals an oracle run of it
+    alone."""
+    room = rooms.boxes_room((80, 40, 32), n_boxes=4, edge=(4, 10), n_materials=5, seed=44)
+    X, Y, Z = room.dims
+    bid = room.bid.copy().reshape(Z, Y, X)
+    bid[4:24, 5:30, 0] = 26
+    bid[6:20, 3:28, -1] = 22
+    steps = 100
+    srcs = room.random_air_nodes(fields, seed=7)
+    srcs[0] = (X - 1, 10, 10)
+    recs = [(X - 1, 12, 12), (0, 12, 12)] + room.random_air_nodes(fields, seed=8)[2:]
+    pulse = rooms.gaussian_pulse(steps, 3.0)
+    samples = np.stack([pulse * (1.0 + 0.1 * f) for f in range(fields)])
+    with Domain(room.dims, prec, fields=fields) as d:
+        d.set_voxels(bid.reshape(-1), room.mat, centred=False)
+        d.set_materials(room.admittance)
+        d.set_params()
+        d.set_sources(srcs, [1] * fields, samples, fields=list(range(fields)))
+        d.set_receivers(recs, fields=list(range(fields)))
+        g, _, st = d.run(steps)
+        assert st == 0 and d.kernel() == "tma"
+    pos, mat = O.encode_nodes(bid.reshape(-1), room.mat, False)
+    for f in range(fields):
+        r, _, _ = O.run(pos, mat, room.dims, room.admittance, default_params(),
+                        [room.flat(*srcs[f])], [1], samples[f:f + 1], [room.flat(*recs[f])],
+                        steps, double=(prec == "f64"),
+                        storage=(prec if prec in ("f16", "bf16") else None))
+        assert np.abs(r).max() > 0 or f > 1
+        assert np.array_equal(g[f], r[0]), f"field {f}"
