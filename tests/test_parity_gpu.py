@@ -880,7 +880,7 @@ def test_pipeline_wait_timeout_reports_and_recovers(gpu, O):
     room = rooms.boxes_room((256, 96, 64), n_boxes=5, edge=(6, 16), n_materials=6, seed=43)
     steps = 60
     src = room.random_air_nodes(1, seed=1)
-    rec = room.random_air_nodes(3, seed=2)
+    rec = [src[0]] + room.random_air_nodes(2, seed=2)  # the source node sees the pulse
     pulse = rooms.gaussian_pulse(steps, 3.0)
     with Domain(room.dims, "f32") as d:
         d.set_voxels(room.bid, room.mat, centred=False)
