@@ -914,9 +914,12 @@ def test_batched_partly_filled_tiles(gpu, O, fields, prec):
     room = rooms.boxes_room((80, 40, 32), n_boxes=4, edge=(4, 10), n_materials=5, seed=44)
     X, Y, Z = room.dims
     bid = room.bid.copy().reshape(Z, Y, X)
-    bid[4:24, 5:30, 0] = 26
-    bid[6:20, 3:28, -1] = 22
-    steps = 100
+    # air nodes on both x faces; their neighbours' node codes still describe
+    # the closed room, so the field grows, and the run is kept short enough
+    # for 16-bit storage
+    bid[4:24, 5:30, 0] = 27
+    bid[6:20, 3:28, -1] = 27
+    steps = 40
     srcs = room.random_air_nodes(fields, seed=7)
     srcs[0] = (X - 1, 10, 10)
     recs = [(X - 1, 12, 12), (0, 12, 12)] + room.random_air_nodes(fields, seed=8)[2:]
@@ -936,5 +939,5 @@ def test_batched_partly_filled_tiles(gpu, O, fields, prec):
                         [room.flat(*srcs[f])], [1], samples[f:f + 1], [room.flat(*recs[f])],
                         steps, double=(prec == "f64"),
                         storage=(prec if prec in ("f16", "bf16") else None))
-        assert np.abs(r).max() > 0 or f > 1
+        assert np.isfinite(r).all() and (f > 1 or np.abs(r).max() > 1e-6)
         assert np.array_equal(g[f], r[0]), f"field {f}"
