@@ -922,6 +922,7 @@ def test_batched_partly_filled_tiles(gpu, O, fields, prec):
     steps = 40
     srcs = room.random_air_nodes(fields, seed=7)
     srcs[0] = (X - 1, 10, 10)
+    srcs[1] = (0, 11, 12)
     recs = [(X - 1, 12, 12), (0, 12, 12)] + room.random_air_nodes(fields, seed=8)[2:]
     pulse = rooms.gaussian_pulse(steps, 3.0)
     samples = np.stack([pulse * (1.0 + 0.1 * f) for f in range(fields)])
