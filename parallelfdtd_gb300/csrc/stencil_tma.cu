@@ -900,9 +900,18 @@ int launch_tma_16(pfdtd_domain* d, const void* cur, void* past, cudaStream_t s) 
   // Two CTAs per SM (registers capped to allow it): a 256 x 8 tile of 16-bit
   // fields holds half the bytes of the FP32 tile, and one CTA per SM leaves
   // too few loads in flight to stream at HBM speed.
-  if (d->K > 1)
+  if (d->K > 1) {
+    // batched tiles: default 256 x 8 elements, 8 stages, two CTAs per SM;
+    // 1 = 256 x 4, 8 stages, four CTAs; 2 = 256 x 8, 6 stages, two CTAs
+    if (d->tma_tile == 1)
+      return launch_tma_batched<S, Layout<S, uint8_t, 256, 4, 8, false, false, 4>,
+                                Layout<S, uint16_t, 256, 4, 8, false, false, 4>>(d, cur, past, s);
+    if (d->tma_tile == 2)
+      return launch_tma_batched<S, Layout<S, uint8_t, 256, 8, 6, false, false, 2>,
+                                Layout<S, uint16_t, 256, 8, 6, false, false, 2>>(d, cur, past, s);
     return launch_tma_batched<S, Layout<S, uint8_t, 256, 8, 8, false, false, 2>,
                               Layout<S, uint16_t, 256, 8, 8, false, false, 2>>(d, cur, past, s);
+  }
   switch (d->tma_tile < 0 || d->tma_tile > 3 ? auto_tile16(d) : d->tma_tile) {
 #define PFDTD_CASE16(id, tx, ty, ns, xh)                                                  \
   case id:                                                                                \

@@ -942,3 +942,32 @@ def test_batched_partly_filled_tiles(gpu, O, fields, prec):
                         storage=(prec if prec in ("f16", "bf16") else None))
         assert np.isfinite(r).all() and (f > 1 or np.abs(r).max() > 1e-6)
         assert np.array_equal(g[f], r[0]), f"field {f}"
+
+
+@pytest.mark.parametrize("tile", [1, 2])
+@pytest.mark.parametrize("fields,prec", [(16, "f16"), (8, "bf16")])
+def test_batched_16bit_tile_shapes(gpu, O, monkeypatch, tile, fields, prec):
+    """The batched 16-bit tile shapes (1: 256 x 4 elements, four CTAs per SM;
+    2: 256 x 8, six stages) equal an oracle run of each field alone."""
+    monkeypatch.setenv("PFDTD_TMA_TILE", str(tile))
+    room = rooms.boxes_room((64, 48, 40), n_boxes=5, edge=(5, 14), n_materials=6, seed=45)
+    steps = 90
+    pulse = rooms.gaussian_pulse(steps, 3.0)
+    srcs = room.random_air_nodes(fields, seed=5)
+    recs = room.random_air_nodes(fields, seed=6)
+    samples = np.stack([pulse * (1 + 0.1 * f) for f in range(fields)])
+    with Domain(room.dims, prec, fields=fields) as d:
+        d.set_voxels(room.bid, room.mat, centred=False)
+        d.set_materials(room.admittance)
+        d.set_params()
+        d.set_sources(srcs, [1] * fields, samples, fields=list(range(fields)))
+        d.set_receivers(recs, fields=list(range(fields)))
+        g, _, st = d.run(steps)
+        assert st == 0 and d.kernel() == "tma"
+    monkeypatch.delenv("PFDTD_TMA_TILE", raising=False)
+    pos, mat = O.encode_nodes(room.bid, room.mat, False)
+    for f in (0, fields - 1):
+        r, _, _ = O.run(pos, mat, room.dims, room.admittance, default_params(),
+                        [room.flat(*srcs[f])], [1], samples[f:f + 1], [room.flat(*recs[f])],
+                        steps, storage=prec)
+        assert np.array_equal(g[f], r[0]), f"field {f}"
