@@ -43,9 +43,10 @@ TOL = {False: 1e-5, True: 1e-12}
 # mode that every room here keeps (a constant field is a solution of the
 # boundary update too).  On the 64^3 shoebox after 500 steps the contracted
 # build differs from its own uncontracted arithmetic by 6.3e-4, about as much
-# as FP32 differs from FP64.  The bound below checks the same physics; the
-# bit-for-bit check is against the uncontracted build.
-TOL_CONTRACTED = {False: 2e-3, True: 1e-12}
+# as FP32 differs from FP64; in FP64 the same mechanism moves it by 1.2e-12.
+# The bounds below check the same physics; the bit-for-bit check is against
+# the uncontracted build.
+TOL_CONTRACTED = {False: 2e-3, True: 1e-11}
 
 
 @pytest.fixture(scope="module")
