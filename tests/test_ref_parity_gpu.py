@@ -175,13 +175,14 @@ def test_reference_kernel_speed(gpu, R):
     """Times the reference's own forward kernel (as nvcc compiles it by
     default for sm_103a) with launchFDTD3d's host sequence against this
     library's run on the benchmark room, 200 steps, FP32.  Both give the same
-    receivers within the contract tolerance; this library must be faster.
+    receivers within TOL_CONTRACTED; this library must be faster.
     The figures are printed (and written to $PFDTD_REPORT_DIR when set)."""
     import time
     room = c2_room()
     steps = 200
     recs = room.random_air_nodes(8, seed=9)
     src = room.random_air_nodes(1, seed=8)[0]
+    recs = [src] + recs  # the source node sees the pulse within 200 steps
     X, Y, _ = room.dims
     flat = lambda c: c[2] * X * Y + c[1] * X + c[0]  # noqa: E731
     params = default_params(octave=1).astype(np.float32)
