@@ -19,6 +19,7 @@
 // node's weighted neighbour sum sw (d_iwb_sw), so this pass reads one value
 // per node instead of gathering the 26 neighbours again.
 #include "common.cuh"
+#include "iwb_closure.cuh"
 
 #include <cstdlib>
 
@@ -32,8 +33,6 @@ namespace {
 constexpr int kChunkNodes = 4096;  // nodes per block when listing DIF nodes
 constexpr int kListThreads = 256;
 
-// Per DIF class: a, b, c, g2 and the filter b0..b3, a1..a3 (11 values).
-constexpr int kDifClassVals = 11;
 
 __global__ void k_dif_count(const void* __restrict__ cls, int cls_bytes,
                             const uint8_t* __restrict__ is_dif, int64_t begin, int64_t end,
@@ -198,11 +197,6 @@ __global__ void k_dif_update(const int64_t* __restrict__ list, int64_t n, int ks
 // the field's margins (at least X + 64 elements each side), and a closed
 // neighbour's value (outside the grid or in a margin) is replaced by a
 // select, never used in arithmetic.
-struct ClosureRec {
-  int64_t idx;
-  uint32_t mask;
-  uint32_t cls;
-};
 
 __global__ void k_closure_records(const int64_t* __restrict__ list, int64_t n,
                                   const void* __restrict__ cls, int cls_bytes,
@@ -245,7 +239,6 @@ k_iwb_closure(const ClosureRec* __restrict__ recs, int64_t n, ClassTab<float> ta
               const S* __restrict__ P, S* __restrict__ Pp, int64_t X, int64_t XY, float l2,
               float* __restrict__ iwb_sw, const int32_t* __restrict__ dif_slot,
               const float* __restrict__ dtab, float* __restrict__ dstate) {
-  using R = Rn<float>;
   using Sto = Store<S>;
   for (int64_t k = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; k < n;
        k += (int64_t)gridDim.x * blockDim.x) {
@@ -260,44 +253,31 @@ k_iwb_closure(const ClosureRec* __restrict__ recs, int64_t n, ClassTab<float> ta
         for (int dx = -1; dx <= 1; ++dx)
           m[dz + 1][dy + 1][dx + 1] = Sto::load(__ldg(P + i + dz * XY + dy * X + dx));
     const float pp = Sto::load(Pp[i]);
-    const float p = m[1][1][1];
-    int kk = 0;
-#pragma unroll
-    for (int a = 0; a < 3; ++a)
-#pragma unroll
-      for (int b = 0; b < 3; ++b)
-#pragma unroll
-        for (int e = 0; e < 3; ++e) {
-          if (a == 1 && b == 1 && e == 1) continue;
-          m[a][b][e] = ((r.mask >> kk) & 1u) ? p : m[a][b][e];
-          ++kk;
-        }
-    float s1, s2, s3;
-    iwb_sums(m, s1, s2, s3);
-    const float sw = R::mul(l2, R::add(R::add(R::mul(s1, 0.25f), R::mul(s2, 0.125f)),
-                                       R::mul(s3, 0.0625f)));
-    const unsigned c = r.cls;
     const int32_t slot = dif_slot != nullptr ? dif_slot[k] : -1;
-    if (slot >= 0) {
-      const float* t = dtab + (int64_t)kDifClassVals * c;
-      float* st = dstate + 4 * (int64_t)slot;
-      const float s1d = st[0], ppd = st[3];
-      const float num = R::sub(R::sub(R::add(sw, R::mul(t[1], p)), R::mul(t[2], ppd)),
-                               R::mul(t[3], s1d));
-      const float out = R::mul(t[0], num);
-      const float xx = R::mul(R::sub(out, ppd), 0.5f);
-      const float yy = R::add(R::mul(t[4], xx), s1d);
-      st[0] = R::add(R::sub(R::mul(t[5], xx), R::mul(t[8], yy)), st[1]);
-      st[1] = R::add(R::sub(R::mul(t[6], xx), R::mul(t[9], yy)), st[2]);
-      st[2] = R::sub(R::mul(t[7], xx), R::mul(t[10], yy));
-      st[3] = p;
-      Pp[i] = Sto::store(out);
+    iwb_closure_apply<S>(m, r.mask, r.cls, pp, tab, l2, slot, dtab, dstate, iwb_sw, i, Pp);
+  }
+}
+
+// For each 128-node tile row (t = (z * Y + y) * ntx + x / 128) the first
+// closure record at or after the row's start: a binary search in the
+// records' ascending flat indices; ctile[T] = n.
+__global__ void k_closure_tile_rows(const ClosureRec* __restrict__ recs, int64_t n, int64_t X,
+                                    int64_t Y, int ntx, int64_t T, int32_t* __restrict__ ctile) {
+  for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t <= T;
+       t += (int64_t)gridDim.x * blockDim.x) {
+    if (t == T) {
+      ctile[t] = (int32_t)n;
       continue;
     }
-    if (iwb_sw != nullptr && (__ldg(tab.pos + c) >> 31)) iwb_sw[i] = sw;
-    const float out = R::mul(__ldg(tab.a + c), R::sub(R::add(sw, R::mul(__ldg(tab.b + c), p)),
-                                                      R::mul(__ldg(tab.c + c), pp)));
-    Pp[i] = Sto::store(out);
+    const int64_t row = t / ntx, tx = t - row * ntx;
+    const int64_t start = row * X + tx * kClosureTileX;
+    int64_t lo = 0, hi = n;
+    while (lo < hi) {
+      const int64_t mid = lo + (hi - lo) / 2;
+      if (recs[mid].idx < start) lo = mid + 1;
+      else hi = mid;
+    }
+    ctile[t] = (int32_t)lo;
   }
 }
 
@@ -517,6 +497,9 @@ static int32_t* closure_dif_slots(pfdtd_domain* d, int64_t n) {
 int build_iwb_closure(pfdtd_domain* d, const std::vector<uint16_t>& keys) {
   if (d->d_iwb_closure) d->release(d->d_iwb_closure);
   d->d_iwb_closure = nullptr;
+  if (d->d_iwb_ctile) d->release(d->d_iwb_ctile);
+  d->d_iwb_ctile = nullptr;
+  d->iwb_ctile_ntx = 0;
   if (d->d_iwb_closure_dif) d->release(d->d_iwb_closure_dif);
   d->d_iwb_closure_dif = nullptr;
   d->n_iwb_closure = 0;
@@ -547,6 +530,27 @@ int build_iwb_closure(pfdtd_domain* d, const std::vector<uint16_t>& keys) {
     if (d->n_dif > 0 && d->n_dif < ((int64_t)1 << 31) && d->d_dif_list &&
         !(unfused && unfused[0] == '1'))
       d->d_iwb_closure_dif = closure_dif_slots(d, n);
+    // The tile-row index of the in-kernel closure (TMA streaming kernel):
+    // optional, the separate pass stays available without it.
+    const int ntx = (int)((d->X + kClosureTileX - 1) / kClosureTileX);
+    const int64_t T = (int64_t)ntx * d->Y * d->Z;
+    if (n < ((int64_t)1 << 31) && T < ((int64_t)1 << 31)) {
+      int32_t* ct = nullptr;
+      e = d->alloc((void**)&ct, sizeof(int32_t) * (size_t)(T + 1));
+      if (e == cudaSuccess) {
+        k_closure_tile_rows<<<grid_for(T + 1), 256, 0, s>>>((const ClosureRec*)d->d_iwb_closure,
+                                                             n, d->X, d->Y, ntx, T, ct);
+        count_launch();
+        e = cudaGetLastError();
+      }
+      if (e == cudaSuccess) {
+        d->d_iwb_ctile = ct;
+        d->iwb_ctile_ntx = ntx;
+      } else {
+        cudaGetLastError();
+        if (ct) d->release(ct);
+      }
+    }
   }
   d->n_iwb_closure = n;
   d->iwb_closure_ready = true;

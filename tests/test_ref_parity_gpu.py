@@ -201,6 +201,7 @@ def test_reference_kernel_speed(gpu, R):
         d.set_sources([src], [1], samples)
         d.set_receivers(recs)
         d.run(steps)  # warm-up: class build, graph capture
+        d.reset_fields()
         t0 = time.perf_counter()
         out, sec_per_step, st = d.run(steps)
         ours_wall = time.perf_counter() - t0
