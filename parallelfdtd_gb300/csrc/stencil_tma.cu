@@ -438,9 +438,6 @@ k_update_tma(const __grid_constant__ CUtensorMap map_cur, const __grid_constant_
     c_hi = __ldg(ctile + c_t + 1);
     if (c_lo + lane < c_hi) c_pre = crec[c_lo + lane];
   }
-  // IWB: unrolled by three, the period of the plane-sum registers' rotation,
-  // so the rotation is a renaming rather than register moves
-#pragma unroll(SCHEME == 3 ? 3 : 1)
   for (int j = 0; j < nplanes && ok; ++j) {
     int n_lo = 0, n_hi = 0;
     if (crow_on && j + 1 < nplanes) {
