@@ -723,13 +723,25 @@ k_update_tma(const __grid_constant__ CUtensorMap map_cur, const __grid_constant_
           const ClosureRec r = k == c_lo + lane ? c_pre : crec[k];
           const int lxk = (int)(r.idx - row0);
           float m[3][3][3];
+          if (x0 + lxk == 0 || x0 + lxk == X - 1) {
+            // grid x edge: the x neighbour is the flat-index one (the
+            // adjacent row's end), not the stage's zero-filled halo
 #pragma unroll
-          for (int a = 0; a < 3; ++a)
+            for (int a = 0; a < 3; ++a)
 #pragma unroll
-            for (int b = 0; b < 3; ++b)
+              for (int b = 0; b < 3; ++b)
 #pragma unroll
-              for (int c = 0; c < 3; ++c)
-                m[a][b][c] = St::load(Pl[a][(ly + b) * PW + lxk + H + c - 1]);
+                for (int c = 0; c < 3; ++c)
+                  m[a][b][c] = St::load(P[r.idx + (int64_t)(a - 1) * XY + (int64_t)(b - 1) * X + (c - 1)]);
+          } else {
+#pragma unroll
+            for (int a = 0; a < 3; ++a)
+#pragma unroll
+              for (int b = 0; b < 3; ++b)
+#pragma unroll
+                for (int c = 0; c < 3; ++c)
+                  m[a][b][c] = St::load(Pl[a][(ly + b) * PW + lxk + H + c - 1]);
+          }
           const float pq = St::load(Pq[ly * kTX + lxk]);
           iwb_closure_apply<S>(m, r.mask, r.cls, pq, tab, (float)l2,
                                dslot != nullptr ? dslot[k] : -1, dtab, dstate, iwb_sw, r.idx,
