@@ -55,3 +55,37 @@ def test_serving_trace_is_seeded_and_bounded():
     srcs = np.array([t.n_src for t in a])
     assert srcs.min() >= 1 and srcs.max() <= 16
 
+
+
+def test_node_updates_count_source_fields(built):
+    """A request's field count is rounded up to a power of two; only the
+    fields that carry a source count as node-updates (computed_updates keeps
+    the padding fields)."""
+    dims, steps = (32, 24, 20), 50
+    r = Request(dims, steps, fields=16, precision="f32")
+    r.set_voxels(np.zeros(32 * 24 * 20, np.uint8), np.zeros(32 * 24 * 20, np.uint8))
+    pulse = np.zeros((9, steps))
+    r.set_sources([(5, 5, 5)] * 9, [1] * 9, pulse, fields=list(range(9)))
+    per_field = 32 * 24 * 18 * steps
+    assert r.node_updates() == 9 * per_field
+    assert r.computed_updates() == 16 * per_field
+    one = Request(dims, steps, fields=1)
+    one.set_sources([(5, 5, 5)], [1], pulse[:1])
+    assert one.node_updates() == per_field
+
+
+def test_padded_rows_in_footprint(built):
+    """A room whose x extent is not a multiple of 16 and whose x = X-1 face is
+    closed runs on rows padded to 16 nodes: the footprint grows with them."""
+    from parallelfdtd_gb300 import rooms
+    room = rooms.shoebox((60, 32, 24), seed=2)  # solid shell: x = X-1 face closed
+    r = Request(room.dims, 40, precision="f32").set_voxels(room.bid, room.mat)
+    r.set_receivers([(10, 10, 10)])
+    b60 = r.bytes()
+    room64 = rooms.shoebox((64, 32, 24), seed=2)
+    r64 = Request(room64.dims, 40, precision="f32").set_voxels(room64.bid, room64.mat)
+    r64.set_receivers([(10, 10, 10)])
+    assert abs(b60 - r64.bytes()) < 64 * 32 * 24  # the padded domain holds 64-wide rows
+    # a receiver past X keeps the room unpadded
+    r.set_receivers([(61, 10, 10)])
+    assert r.bytes() < b60
