@@ -187,9 +187,10 @@ int pfdtd_set_scheme(pfdtd_domain* d, int scheme);
  *   uniform (pressure offset) mode of a closed room grow step by step; the
  *   difference form has no such term (S - K P is exactly 0 on a uniform
  *   field), and its receiver error against an FP64 run drops by about two
- *   orders of magnitude at the same memory traffic.  Float arithmetic only
- *   (FP32, FP16, BF16 storage); no frequency-dependent boundaries and no
- *   temporal blocking (PFDTD_ERR_UNSUPPORTED at the next run).  */
+ *   orders of magnitude at the same memory traffic.  FP32 fields only (with
+ *   16-bit storage the storage rounding dominates and the form gains
+ *   nothing); no frequency-dependent boundaries and no temporal blocking
+ *   (PFDTD_ERR_UNSUPPORTED at the next run).  */
 /* Bound, in nanoseconds, of each pipeline wait inside the TMA update kernels
  * (no counterpart in the reference; default 2 s, 0 restores it).  A wait that
  * runs out raises the domain's error flag; the kernel stops issuing loads,

@@ -241,13 +241,6 @@ struct pfdtd_domain {
   // a node without a filter; set when every DIF node has a record, and then
   // the closure pass also applies the DIF update (no separate DIF pass)
   int32_t* d_iwb_closure_dif = nullptr;
-  // per 128-node tile row (z, y, x/128) its first closure record, and the
-  // number of tile rows along x: the TMA streaming kernel then updates the
-  // closure nodes of its tile from the staged planes (no separate pass);
-  // PFDTD_IWB_CLOSURE_PASS=1 at domain creation keeps the separate pass
-  int32_t* d_iwb_ctile = nullptr;
-  int iwb_ctile_ntx = 0;
-  bool iwb_closure_pass = false;
   bool iwb_closure_ready = false;
   int64_t class_version = 0;
 
@@ -333,8 +326,6 @@ int launch_iwb_closure(pfdtd_domain* d, const void* cur, void* past, cudaStream_
 // Implemented in stencil_tma.cu: whether the next update runs the IWB
 // closure pass with the DIF update fused into it
 bool iwb_closure_fuses_dif(const pfdtd_domain* d);
-// stencil_tma.cu: whether the IWB TMA kernel updates the closure nodes itself
-bool iwb_in_kernel_closure(const pfdtd_domain* d);
 // Implemented in setup.cu
 int launch_slice_gather(pfdtd_domain* d, int orientation, int64_t slice, float* dp, uint8_t* dq,
                         cudaStream_t s);

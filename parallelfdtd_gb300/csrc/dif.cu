@@ -258,29 +258,6 @@ k_iwb_closure(const ClosureRec* __restrict__ recs, int64_t n, ClassTab<float> ta
   }
 }
 
-// For each 128-node tile row (t = (z * Y + y) * ntx + x / 128) the first
-// closure record at or after the row's start: a binary search in the
-// records' ascending flat indices; ctile[T] = n.
-__global__ void k_closure_tile_rows(const ClosureRec* __restrict__ recs, int64_t n, int64_t X,
-                                    int64_t Y, int ntx, int64_t T, int32_t* __restrict__ ctile) {
-  for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t <= T;
-       t += (int64_t)gridDim.x * blockDim.x) {
-    if (t == T) {
-      ctile[t] = (int32_t)n;
-      continue;
-    }
-    const int64_t row = t / ntx, tx = t - row * ntx;
-    const int64_t start = row * X + tx * kClosureTileX;
-    int64_t lo = 0, hi = n;
-    while (lo < hi) {
-      const int64_t mid = lo + (hi - lo) / 2;
-      if (recs[mid].idx < start) lo = mid + 1;
-      else hi = mid;
-    }
-    ctile[t] = (int32_t)lo;
-  }
-}
-
 // Ordered list of the nodes of planes 1..Z-2 whose class is flagged; *list
 // is allocated (stream-ordered) when there is at least one.
 int build_flagged_list(pfdtd_domain* d, const std::vector<uint8_t>& flag, int64_t** list,
@@ -497,9 +474,6 @@ static int32_t* closure_dif_slots(pfdtd_domain* d, int64_t n) {
 int build_iwb_closure(pfdtd_domain* d, const std::vector<uint16_t>& keys) {
   if (d->d_iwb_closure) d->release(d->d_iwb_closure);
   d->d_iwb_closure = nullptr;
-  if (d->d_iwb_ctile) d->release(d->d_iwb_ctile);
-  d->d_iwb_ctile = nullptr;
-  d->iwb_ctile_ntx = 0;
   if (d->d_iwb_closure_dif) d->release(d->d_iwb_closure_dif);
   d->d_iwb_closure_dif = nullptr;
   d->n_iwb_closure = 0;
@@ -530,27 +504,6 @@ int build_iwb_closure(pfdtd_domain* d, const std::vector<uint16_t>& keys) {
     if (d->n_dif > 0 && d->n_dif < ((int64_t)1 << 31) && d->d_dif_list &&
         !(unfused && unfused[0] == '1'))
       d->d_iwb_closure_dif = closure_dif_slots(d, n);
-    // The tile-row index of the in-kernel closure (TMA streaming kernel):
-    // optional, the separate pass stays available without it.
-    const int ntx = (int)((d->X + kClosureTileX - 1) / kClosureTileX);
-    const int64_t T = (int64_t)ntx * d->Y * d->Z;
-    if (n < ((int64_t)1 << 31) && T < ((int64_t)1 << 31)) {
-      int32_t* ct = nullptr;
-      e = d->alloc((void**)&ct, sizeof(int32_t) * (size_t)(T + 1));
-      if (e == cudaSuccess) {
-        k_closure_tile_rows<<<grid_for(T + 1), 256, 0, s>>>((const ClosureRec*)d->d_iwb_closure,
-                                                             n, d->X, d->Y, ntx, T, ct);
-        count_launch();
-        e = cudaGetLastError();
-      }
-      if (e == cudaSuccess) {
-        d->d_iwb_ctile = ct;
-        d->iwb_ctile_ntx = ntx;
-      } else {
-        cudaGetLastError();
-        if (ct) d->release(ct);
-      }
-    }
   }
   d->n_iwb_closure = n;
   d->iwb_closure_ready = true;

@@ -401,7 +401,6 @@ int pfdtd_create_batched(int64_t dim_x, int64_t dim_y, int64_t dim_z, int fields
   cudaMemsetAsync(d->d_err, 0, sizeof(int), d->stream);
   if (const char* tv = std::getenv("PFDTD_TMA_TILE")) d->tma_tile = std::atoi(tv);
   if (const char* sv = std::getenv("PFDTD_TB_SHAPE")) d->tb_shape = std::atoi(sv);
-  if (const char* cv = std::getenv("PFDTD_IWB_CLOSURE_PASS")) d->iwb_closure_pass = cv[0] == '1';
   if (const char* kv = std::getenv("PFDTD_KERNEL")) {
     if (std::strcmp(kv, "zmarch") == 0) d->kernel_variant = PFDTD_KERNEL_ZMARCH;
     if (std::strcmp(kv, "tma") == 0) d->kernel_variant = PFDTD_KERNEL_TMA;
@@ -421,7 +420,7 @@ int pfdtd_destroy(pfdtd_domain* d) {
                   d->d_ctab, d->d_src_idx, d->d_src_mode, d->d_src_samples, d->d_rec_idx,
                   d->d_step, d->d_rec_out, d->d_err, d->d_dif_list, d->d_dif_tab,
                   d->d_dif_state, d->d_iwb_mask, d->d_iwb_code, d->d_iwb_sw,
-                  d->d_iwb_closure, d->d_iwb_closure_dif, d->d_iwb_ctile};
+                  d->d_iwb_closure, d->d_iwb_closure_dif};
   for (void* p : ptrs)
     d->release(p);
   if (d->stream) cudaStreamDestroy(d->stream);
@@ -492,8 +491,8 @@ int pfdtd_set_update_form(pfdtd_domain* d, int form) {
   if (int rc = check_domain(d)) return rc;
   if (form != PFDTD_FORM_REFERENCE && form != PFDTD_FORM_DIFFERENCE)
     return fail(PFDTD_ERR_ARG, "unknown update form");
-  if (form != PFDTD_FORM_REFERENCE && d->precision == PFDTD_F64)
-    return fail(PFDTD_ERR_UNSUPPORTED, "the difference form is built for float arithmetic");
+  if (form != PFDTD_FORM_REFERENCE && d->precision != PFDTD_F32)
+    return fail(PFDTD_ERR_UNSUPPORTED, "the difference form is built for FP32 fields");
   if (form != d->update_form) {
     d->update_form = form;
     d->classes_dirty = true;

@@ -1,9 +1,7 @@
 // IWB closure nodes (no counterpart in the reference): the inside nodes with
 // a closed neighbour, whose update substitutes the node's own value for every
-// closed neighbour.  The streaming TMA update leaves them alone; they are
-// updated either inside the same kernel from the staged planes (the default)
-// or by the separate pass k_iwb_closure (dif.cu), both through
-// iwb_closure_apply, so both give the same bits.
+// closed neighbour.  The streaming TMA update leaves them alone and the
+// sparse pass k_iwb_closure (dif.cu) updates them with iwb_closure_apply.
 #pragma once
 
 #include "common.cuh"
@@ -20,10 +18,6 @@ struct ClosureRec {
 
 // Per DIF class: a, b, c, g2 and the filter b0..b3, a1..a3 (11 values).
 constexpr int kDifClassVals = 11;
-
-// x extent of the tile rows the in-kernel closure indexes its records by
-// (the width of every maskless IWB tile).
-constexpr int kClosureTileX = 128;
 
 // Update of closure node i from its 3 x 3 x 3 neighbourhood m (raw values,
 // centre included) and P^{n-1} pp: closed neighbours (mask bits in the

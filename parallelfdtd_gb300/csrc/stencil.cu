@@ -10,6 +10,7 @@
 #include "common.cuh"
 
 #include <algorithm>
+#include <type_traits>
 #include <cstring>
 
 namespace pfdtd {
@@ -29,7 +30,7 @@ template <typename S, typename C, int SCHEME>
 __global__ void __launch_bounds__(kBX * kBY)
 k_update_zmarch(const C* __restrict__ cls, const S* __restrict__ P, S* __restrict__ Pp,
                 ClassTab<typename Store<S>::A> tab, int X, int Y, int64_t XY, int z_last,
-                int zc, typename Store<S>::A l2, int ks, int kshift, int form) {
+                int zc, typename Store<S>::A l2, int ks, int kshift) {
   using A = typename Store<S>::A;
   using R = Rn<A>;
   using St = Store<S>;
@@ -72,10 +73,10 @@ k_update_zmarch(const C* __restrict__ cls, const S* __restrict__ P, S* __restric
       ca = __ldg(tab.a + c); cb = __ldg(tab.b + c); cc = __ldg(tab.c + c); cp = __ldg(tab.pos + c);
     }
     A out;
-    if (SCHEME == 0) {
+    if (SCHEME == 0 || SCHEME == 4) {
       // S = P[z+1] + P[z-1] + P[y+1] + P[y-1] + P[x+1] + P[x-1]  (kernels3d.cu:525)
       const A s6 = R::add(R::add(R::add(R::add(R::add(pn, pm), yp), ym), xp), xm);
-      if (sizeof(A) == 4 && form) {
+      if (SCHEME == 4) {
         // difference form: a (((1+beta) p + (1-beta)(p - pp)) + l2 (S - K p)),
         // cb = K and the pos word holds the float 1 + beta
         const A e = (A)__uint_as_float(cp);
@@ -288,7 +289,7 @@ int launch_update_t(pfdtd_domain* d, const void* cur, void* past, cudaStream_t s
                   (const uint32_t*)(tb + 3 * as * d->n_classes), d->n_classes};
   k_update_zmarch<S, C, SCHEME><<<dim3(gx, gy, gz), dim3(kBX, kBY), 0, s>>>(
       (const C*)d->d_cls, (const S*)cur, (S*)past, tab, (int)XE, (int)d->Y, d->XY * d->K,
-      (int)(d->Z - 1), (int)zc, (A)d->params[1], d->K, d->kshift, d->class_form);
+      (int)(d->Z - 1), (int)zc, (A)d->params[1], d->K, d->kshift);
   count_launch();
   PFDTD_CK(cudaGetLastError());
   return PFDTD_OK;
@@ -325,6 +326,11 @@ int launch_update_s(pfdtd_domain* d, const void* cur, void* past, cudaStream_t s
     return d->cls_bytes == 1 ? launch_iwb_t<S, uint8_t>(d, cur, past, s)
                              : launch_iwb_t<S, uint16_t>(d, cur, past, s);
   const bool centred = (d->class_scheme == PFDTD_SRL);
+  if constexpr (std::is_same<S, float>::value) {  // the difference form (FP32 fields)
+    if (d->class_form == PFDTD_FORM_DIFFERENCE)
+      return d->cls_bytes == 1 ? launch_update_t<S, uint8_t, 4>(d, cur, past, s)
+                               : launch_update_t<S, uint16_t, 4>(d, cur, past, s);
+  }
   if (d->cls_bytes == 1)
     return centred ? launch_update_t<S, uint8_t, 1>(d, cur, past, s)
                    : launch_update_t<S, uint8_t, 0>(d, cur, past, s);
@@ -392,8 +398,8 @@ int build_classes(pfdtd_domain* d) {
       if (f)
         return fail(PFDTD_ERR_UNSUPPORTED,
                     "the difference form is not built for frequency-dependent boundaries");
-    if (d->precision == PFDTD_F64)
-      return fail(PFDTD_ERR_UNSUPPORTED, "the difference form is built for float arithmetic");
+    if (d->precision != PFDTD_F32)
+      return fail(PFDTD_ERR_UNSUPPORTED, "the difference form is built for FP32 fields");
   }
   cudaStream_t s = d->stream;
   uint8_t* d_present = nullptr;

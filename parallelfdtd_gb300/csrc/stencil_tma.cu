@@ -24,7 +24,6 @@
 // error flag, stops issuing loads, waits (bounded) for the loads already in
 // flight and returns.
 #include "common.cuh"
-#include "iwb_closure.cuh"
 
 #include <cuda.h>
 
@@ -344,11 +343,8 @@ k_update_tma(const __grid_constant__ CUtensorMap map_cur, const __grid_constant_
              const __grid_constant__ CUtensorMap map_mask, const S* __restrict__ P,
              S* __restrict__ Pp, ClassTab<typename Store<S>::A> tab, int X, int Y, int64_t XY,
              int z_last, int zc, typename Store<S>::A l2, int* __restrict__ err, int kshift = 0,
-             float* __restrict__ iwb_sw = nullptr, float nzf = -0.0f, int form = 0,
-             uint64_t wait_ns = kWaitLimitNs, const ClosureRec* __restrict__ crec = nullptr,
-             const int32_t* __restrict__ ctile = nullptr, int ntx = 0,
-             const int32_t* __restrict__ dslot = nullptr, const float* __restrict__ dtab = nullptr,
-             float* __restrict__ dstate = nullptr) {
+             float* __restrict__ iwb_sw = nullptr, float nzf = -0.0f,
+             uint64_t wait_ns = kWaitLimitNs) {
   using A = typename Store<S>::A;
   using R = Rn<A>;
   using St = Store<S>;
@@ -423,27 +419,7 @@ k_update_tma(const __grid_constant__ CUtensorMap map_cur, const __grid_constant_
                                        g0 + XY, x, X, no_mask, cc0, cc0, cc1, cc2);
     }
   }
-  // IWB closure nodes inside this kernel (maskless tiles, one tile row per
-  // warp): the records of the warp's tile row at each plane, [c_lo, c_hi),
-  // with the bounds and the lane's first record of the next plane loaded one
-  // iteration ahead so that their latency hides behind the streaming work.
-  constexpr bool kInClosure = SCHEME == 3 && !Lay::MASK && kThreadsPerRow == 32;
-  const bool crow_on = kInClosure && crec != nullptr && (y0 + ly) < Y;
-  int64_t c_t = 0;
-  int c_lo = 0, c_hi = 0;
-  ClosureRec c_pre{0, 0u, 0u};
-  if (crow_on) {
-    c_t = ((int64_t)z0 * Y + (y0 + ly)) * ntx + blockIdx.x;
-    c_lo = __ldg(ctile + c_t);
-    c_hi = __ldg(ctile + c_t + 1);
-    if (c_lo + lane < c_hi) c_pre = crec[c_lo + lane];
-  }
   for (int j = 0; j < nplanes && ok; ++j) {
-    int n_lo = 0, n_hi = 0;
-    if (crow_on && j + 1 < nplanes) {
-      n_lo = __ldg(ctile + c_t + (int64_t)Y * ntx);
-      n_hi = __ldg(ctile + c_t + (int64_t)Y * ntx + 1);
-    }
     const int sm = j % NS, sc_ = (j + 1) % NS, sp_ = (j + 2) % NS;
     if (!mbar_wait(bar_full + 8 * sp_, (uint32_t)(((j + 2) / NS) & 1), wait_ns)) {
       ok = false;
@@ -578,7 +554,7 @@ k_update_tma(const __grid_constant__ CUtensorMap map_cur, const __grid_constant_
         const uint2 w = *reinterpret_cast<const uint2*>(Cl + ly * kTX + lx);
         cid[0] = w.x & 0xFFFFu; cid[1] = w.x >> 16; cid[2] = w.y & 0xFFFFu; cid[3] = w.y >> 16;
       }
-      if constexpr (SCHEME == 0 && sizeof(A) == 4) {
+      if constexpr ((SCHEME == 0 || SCHEME == 4) && sizeof(A) == 4) {
         // Forward update of the thread's 4 elements as two packed pairs: the
         // same operations and rounding as the scalar loop below, with every
         // product formed as fma(x, y, -0) so that none is contracted.
@@ -634,7 +610,7 @@ k_update_tma(const __grid_constant__ CUtensorMap map_cur, const __grid_constant_
           const f2 s6 = add2(add2(add2(add2(add2(pr(vzp, h), pr(vzm, h)), pr(vyp, h)),
                                       pr(vym, h)), xp2[h]), xm2[h]);
           f2 o;
-          if (form) {
+          if constexpr (SCHEME == 4) {
             // difference form: a (((1+beta) p + (1-beta)(p - pp)) + l2 (S - K p))
             const f2 pc2 = pr(vc, h);
             o = mul2(aa[h], add2(add2(fma2(ee[h], pc2, nz), fma2(cc[h], sub2(pc2, pr(vpp, h)), nz)),
@@ -683,9 +659,9 @@ k_update_tma(const __grid_constant__ CUtensorMap map_cur, const __grid_constant_
                             __ldg(tab.pos + cid[e])};
         }
         A out;
-        if (SCHEME == 0) {
+        if (SCHEME == 0 || SCHEME == 4) {
           const A s6 = R::add(R::add(R::add(R::add(R::add(pn, pm), yp), ym), xp), xm);
-          if (sizeof(A) == 4 && form) {
+          if (SCHEME == 4 && sizeof(A) == 4) {
             const A e = (A)__uint_as_float(k.pos);
             out = R::mul(k.a, R::add(R::add(R::mul(e, pc), R::mul(k.c, R::sub(pc, pp))),
                                      R::mul(l2, R::sub(s6, R::mul(k.b, pc)))));
@@ -705,52 +681,6 @@ k_update_tma(const __grid_constant__ CUtensorMap map_cur, const __grid_constant_
         res[e] = St::store(out);
       }
       stg4(Pp + idx, res);
-      }
-    }
-    if constexpr (kInClosure) {
-      if (crow_on) {
-        // The warp's stores of this plane (closure nodes keep P^{n-1}) come
-        // first; then its tile row's closure nodes are updated from the
-        // staged planes z-1, z, z+1 (rows y-1..y+1 and the x halo are there).
-        __syncwarp();
-        const int zq = z0 + j;
-        const int64_t row0 = (int64_t)zq * XY + (int64_t)(y0 + ly) * X + x0;
-        const S* Pl[3] = {(const S*)(smem + sm * Lay::STAGE + Lay::P_OFF),
-                          (const S*)(smem + sc_ * Lay::STAGE + Lay::P_OFF),
-                          (const S*)(smem + sp_ * Lay::STAGE + Lay::P_OFF)};
-        const S* Pq = (const S*)(smem + sp_ * Lay::STAGE + Lay::PP_OFF);
-        for (int k = c_lo + lane; k < c_hi; k += 32) {
-          const ClosureRec r = k == c_lo + lane ? c_pre : crec[k];
-          const int lxk = (int)(r.idx - row0);
-          float m[3][3][3];
-          if (x0 + lxk == 0 || x0 + lxk == X - 1) {
-            // grid x edge: the x neighbour is the flat-index one (the
-            // adjacent row's end), not the stage's zero-filled halo
-#pragma unroll
-            for (int a = 0; a < 3; ++a)
-#pragma unroll
-              for (int b = 0; b < 3; ++b)
-#pragma unroll
-                for (int c = 0; c < 3; ++c)
-                  m[a][b][c] = St::load(P[r.idx + (int64_t)(a - 1) * XY + (int64_t)(b - 1) * X + (c - 1)]);
-          } else {
-#pragma unroll
-            for (int a = 0; a < 3; ++a)
-#pragma unroll
-              for (int b = 0; b < 3; ++b)
-#pragma unroll
-                for (int c = 0; c < 3; ++c)
-                  m[a][b][c] = St::load(Pl[a][(ly + b) * PW + lxk + H + c - 1]);
-          }
-          const float pq = St::load(Pq[ly * kTX + lxk]);
-          iwb_closure_apply<S>(m, r.mask, r.cls, pq, tab, (float)l2,
-                               dslot != nullptr ? dslot[k] : -1, dtab, dstate, iwb_sw, r.idx,
-                               Pp);
-        }
-        c_t += (int64_t)Y * ntx;
-        c_lo = n_lo;
-        c_hi = n_hi;
-        if (c_lo + lane < c_hi) c_pre = crec[c_lo + lane];
       }
     }
     __syncwarp();
@@ -884,21 +814,11 @@ int launch_tma_t(pfdtd_domain* d, const void* cur, void* past, cudaStream_t s) {
   ClassTab<A> tab{(const A*)tb, (const A*)(tb + as * d->n_classes),
                   (const A*)(tb + 2 * as * d->n_classes),
                   (const uint32_t*)(tb + 3 * as * d->n_classes), d->n_classes};
-  // IWB without masks: the closure nodes are updated in this kernel (records,
-  // their tile-row index and, with the DIF update fused, the DIF tables)
-  const bool in_closure = SCHEME == 3 && !Lay::MASK && Lay::TX == kClosureTileX &&
-                          iwb_in_kernel_closure(d);
-  const bool fuse = in_closure && iwb_closure_fuses_dif(d);
-  float* sw_out = nullptr;
-  if (SCHEME == 3) sw_out = Lay::MASK ? d->d_iwb_sw : (d->n_dif > 0 && !fuse ? d->d_iwb_sw : nullptr);
   k_update_tma<S, C, SCHEME, Lay, BATCHED><<<dim3(gx, gy, gz), Lay::THREADS, Lay::SMEM, s>>>(
       ts.halo[cur_i], ts.tile[past_i], ts.cls, Lay::MASK ? ts.mask : ts.cls, (const S*)cur,
       (S*)past, tab, (int)XE, (int)d->Y, d->XY * d->K, (int)(d->Z - 1), (int)zc,
-      (A)d->params[1], d->d_err, d->kshift, sw_out, -0.0f, d->class_form, d->wait_ns,
-      in_closure ? (const ClosureRec*)d->d_iwb_closure : nullptr,
-      in_closure ? d->d_iwb_ctile : nullptr, in_closure ? d->iwb_ctile_ntx : 0,
-      fuse ? d->d_iwb_closure_dif : nullptr, fuse ? (const float*)d->d_dif_tab : nullptr,
-      fuse ? (float*)d->d_dif_state : nullptr);
+      (A)d->params[1], d->d_err, d->kshift, SCHEME == 3 ? d->d_iwb_sw : nullptr, -0.0f,
+      d->wait_ns);
   count_launch();
   PFDTD_CK(cudaGetLastError());
   return PFDTD_OK;
@@ -907,6 +827,11 @@ int launch_tma_t(pfdtd_domain* d, const void* cur, void* past, cudaStream_t s) {
 template <typename S, typename Lay8, typename Lay16>
 int launch_tma_batched(pfdtd_domain* d, const void* cur, void* past, cudaStream_t s) {
   const bool centred = (d->class_scheme == PFDTD_SRL);
+  if constexpr (std::is_same<S, float>::value) {  // the difference form (FP32 fields)
+    if (d->class_form == PFDTD_FORM_DIFFERENCE)
+      return d->cls_bytes == 1 ? launch_tma_t<S, uint8_t, 4, Lay8, true>(d, cur, past, s)
+                               : launch_tma_t<S, uint16_t, 4, Lay16, true>(d, cur, past, s);
+  }
   if (d->cls_bytes == 1)
     return centred ? launch_tma_t<S, uint8_t, 1, Lay8, true>(d, cur, past, s)
                    : launch_tma_t<S, uint8_t, 0, Lay8, true>(d, cur, past, s);
@@ -917,6 +842,11 @@ int launch_tma_batched(pfdtd_domain* d, const void* cur, void* past, cudaStream_
 template <typename S, typename Lay8, typename Lay16>
 int launch_tma_l(pfdtd_domain* d, const void* cur, void* past, cudaStream_t s) {
   const bool centred = (d->class_scheme == PFDTD_SRL);
+  if constexpr (std::is_same<S, float>::value) {  // the difference form (FP32 fields)
+    if (d->class_form == PFDTD_FORM_DIFFERENCE)
+      return d->cls_bytes == 1 ? launch_tma_t<S, uint8_t, 4, Lay8>(d, cur, past, s)
+                               : launch_tma_t<S, uint16_t, 4, Lay16>(d, cur, past, s);
+  }
   if (d->cls_bytes == 1)
     return centred ? launch_tma_t<S, uint8_t, 1, Lay8>(d, cur, past, s)
                    : launch_tma_t<S, uint8_t, 0, Lay8>(d, cur, past, s);
@@ -1044,7 +974,6 @@ int launch_iwb_l(pfdtd_domain* d, const void* cur, void* past, cudaStream_t s) {
     if (!d->iwb_closure_ready) return fail(PFDTD_ERR_STATE, "IWB closure list not built");
     if (int rc = launch_tma_t<S, C, 3, Layout<S, C, TX, TY, NS, true, false, MINB>>(d, cur, past, s))
       return rc;
-    if (TX == kClosureTileX && iwb_in_kernel_closure(d)) return PFDTD_OK;  // done in the kernel
     return launch_iwb_closure(d, cur, past, s);
   }
 }
@@ -1083,11 +1012,6 @@ int launch_iwb_tma(pfdtd_domain* d, const void* cur, void* past, cudaStream_t s)
     case PFDTD_BF16: return launch_iwb_tma_s<__nv_bfloat16>(d, cur, past, s);
   }
   return fail(PFDTD_ERR_UNSUPPORTED, "IWB on the TMA path needs FP32, FP16 or BF16 fields");
-}
-
-bool iwb_in_kernel_closure(const pfdtd_domain* d) {
-  return d->class_scheme == PFDTD_IWB && d->iwb_closure_ready && d->n_iwb_closure > 0 &&
-         d->d_iwb_ctile != nullptr && !d->iwb_closure_pass;
 }
 
 bool iwb_closure_fuses_dif(const pfdtd_domain* d) {

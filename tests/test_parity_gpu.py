@@ -971,47 +971,3 @@ def test_batched_16bit_tile_shapes(gpu, O, monkeypatch, tile, fields, prec):
                         [room.flat(*srcs[f])], [1], samples[f:f + 1], [room.flat(*recs[f])],
                         steps, storage=prec)
         assert np.array_equal(g[f], r[0]), f"field {f}"
-
-
-@pytest.mark.parametrize("prec", ["f32", "bf16"])
-@pytest.mark.parametrize("shape", [6, 10])
-def test_iwb_closure_in_kernel_equals_separate_pass(gpu, O, monkeypatch, prec, shape):
-    """The maskless IWB tiles update the closure nodes inside the streaming
-    kernel from the staged planes; PFDTD_IWB_CLOSURE_PASS=1 keeps the
-    separate gather pass.  Both equal the oracle bit for bit, with DIF walls
-    (DIF update fused into the closure)."""
-    room, flags, table = _iwb_dif_room()
-    steps = 80
-    srcs = room.random_air_nodes(2, seed=1)
-    rec = room.random_air_nodes(4, seed=2)
-    pulse = rooms.gaussian_pulse(steps, 3.0)
-    params = default_params(scheme="iwb")
-    out = {}
-    for sep in (False, True):
-        if sep:
-            monkeypatch.setenv("PFDTD_IWB_CLOSURE_PASS", "1")
-        else:
-            monkeypatch.delenv("PFDTD_IWB_CLOSURE_PASS", raising=False)
-        with Domain(room.dims, prec) as d:
-            d.set_voxels(room.bid, room.mat, centred=True)
-            d.set_materials(room.admittance)
-            d.set_params(params)
-            d.set_scheme("iwb")
-            d.set_dif_filters(flags, table)
-            d.set_kernel("tma")
-            L.call("pfdtd_set_tile", d.handle, shape)
-            d.set_sources(srcs, [1, 1], np.stack([pulse, -0.5 * pulse]))
-            d.set_receivers(rec)
-            g, _, st = d.run(steps)
-            assert st == 0
-            out[sep] = (g, d.download_field(L.FIELD_CURRENT))
-    monkeypatch.delenv("PFDTD_IWB_CLOSURE_PASS", raising=False)
-    assert np.array_equal(out[False][0], out[True][0])
-    view = (lambda a: a.view(np.uint16)) if prec == "bf16" else (lambda a: a)
-    assert np.array_equal(view(out[False][1]), view(out[True][1]))
-    pos, mat = O.encode_nodes(room.bid, room.mat, True)
-    r, _, _ = O.run(pos, mat, room.dims, room.admittance, params, [room.flat(*s) for s in srcs],
-                    [1, 1], np.stack([pulse, -0.5 * pulse]), [room.flat(*x) for x in rec], steps,
-                    scheme=3, storage=(prec if prec == "bf16" else None), dif=(flags, table))
-    assert np.abs(r).max() > 1e-4
-    assert np.array_equal(out[False][0], r)

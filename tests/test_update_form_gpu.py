@@ -3,7 +3,8 @@
 The form is an addition with no counterpart in the reference: the same
 forward update, equal in exact arithmetic, written so that a uniform field
 gives an exactly zero Laplacian.  It is checked bit for bit against the
-oracle's statement of the same form, on every kernel path that runs it, and
+oracle's statement of the same form, on every kernel path that runs it (FP32
+fields, the one storage it is built for), and
 its receiver error against an FP64 run is checked against the 1e-4 relative
 L2 bound of the contract, which the reference form misses in FP32.
 """
@@ -48,7 +49,7 @@ def test_oracle_difference_form_meets_fp64_bound(O):
 
 
 @pytest.mark.gpu
-@pytest.mark.parametrize("prec", ["f32", "f16", "bf16"])
+@pytest.mark.parametrize("prec", ["f32"])
 @pytest.mark.parametrize("variant", ["auto", "zmarch"])
 def test_difference_form_equals_oracle(gpu, O, prec, variant):
     room = rooms.boxes_room((96, 64, 48), n_boxes=6, edge=(5, 14), n_materials=6, seed=41)
@@ -83,7 +84,7 @@ def test_difference_form_equals_oracle(gpu, O, prec, variant):
 
 
 @pytest.mark.gpu
-@pytest.mark.parametrize("prec", ["f32", "f16"])
+@pytest.mark.parametrize("prec", ["f32"])
 def test_difference_form_batched_fields(gpu, O, prec):
     """K = 8 fields sharing the room: each field equals an oracle run of it
     alone in the difference form."""
@@ -134,9 +135,10 @@ def test_difference_form_c1_error_against_fp64(gpu, O):
 @pytest.mark.gpu
 def test_difference_form_refusals(gpu):
     from parallelfdtd_gb300 import materials
-    with Domain((32, 16, 16), "f64") as d:
-        with pytest.raises(Exception):
-            d.set_update_form("difference")
+    for prec in ("f64", "f16", "bf16"):  # built for FP32 fields only
+        with Domain((32, 16, 16), prec) as d:
+            with pytest.raises(Exception):
+                d.set_update_form("difference")
     room = rooms.shoebox((32, 16, 16), n_materials=6, seed=1)
     with Domain(room.dims, "f32") as d:
         d.set_voxels(room.bid, room.mat, centred=False)
