@@ -567,19 +567,8 @@ k_update_tma(const __grid_constant__ CUtensorMap map_cur, const __grid_constant_
                                __ldg(tab.c + cid[e]), __ldg(tab.pos + cid[e])};
         };
         const f2 l22 = pk2(l2, l2), nz = pk2(nzf, nzf);
-        // elements 2h, 2h+1 as a float pair; a 16-bit pair is converted as
-        // one 32-bit word (both conversions are exact)
         auto pr = [](const V4<S>& v, int h) -> f2 {
-          if constexpr (std::is_same<S, __half>::value) {
-            const float2 f = __half22float2(__halves2half2(v.v[2 * h], v.v[2 * h + 1]));
-            return pk2(f.x, f.y);
-          } else if constexpr (std::is_same<S, __nv_bfloat16>::value) {
-            const uint32_t w = (uint32_t)__bfloat16_as_ushort(v.v[2 * h]) |
-                               ((uint32_t)__bfloat16_as_ushort(v.v[2 * h + 1]) << 16);
-            return pk2(__uint_as_float(w << 16), __uint_as_float(w & 0xFFFF0000u));
-          } else {
-            return pk2(St::load(v.v[2 * h]), St::load(v.v[2 * h + 1]));
-          }
+          return pk2(St::load(v.v[2 * h]), St::load(v.v[2 * h + 1]));
         };
         f2 aa[2], bb[2], cc[2], ee[2], xm2[2], xp2[2];
         if constexpr (BATCHED) {
