@@ -359,7 +359,8 @@ def run_serving(a, world, rank, local):
                                             "queue_p99_s", "service_p50_s", "service_p99_s")},
             "e2e": {"value": res["node_updates"] * world / wall, "unit": METRIC,
                     "h2d_bytes_per_step": None, "d2h_bytes_per_step": None},
-            "server": {k: st[k] for k in ("completed", "failed", "max_running", "bytes_peak")},
+            "server": {k: st[k] for k in ("completed", "failed", "max_running", "bytes_peak",
+                                             "setup_seconds", "retire_seconds")},
             "work": {"requests": res["requests"],
                      "node_updates": res["node_updates"],
                      "computed_node_updates": res["computed_updates"],

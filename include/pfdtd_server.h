@@ -7,9 +7,12 @@
  * in arrival order.  A scheduler thread admits the request at the head of
  * the queue as soon as an active slot is free and the request's estimated
  * device footprint fits the HBM budget next to the requests already running
- * (continuous batching): it creates the request's domain on its own stream,
- * queues the whole run there without waiting (pfdtd_run_async), and goes on
- * admitting.  Admitted requests therefore run concurrently on the device.
+ * (continuous batching): it reserves the slot and the bytes and hands the
+ * request to one of up to four set-up threads, which creates the request's
+ * domain on its own stream and queues the whole run there without waiting
+ * (pfdtd_run_async); the scheduler goes on admitting meanwhile.  Admitted
+ * requests therefore run concurrently on the device, and the host set-up of
+ * one overlaps the others' runs.
  * When a request's stream has drained, its receivers are copied to the host,
  * its domain is destroyed (stream-ordered frees, no device-wide
  * synchronisation) and its memory returns to the budget.
@@ -86,6 +89,8 @@ typedef struct {
   uint64_t bytes_in_use, bytes_peak;
   int max_running;       /* most requests running at once so far */
   double node_updates;   /* interior node-updates x fields of completed requests */
+  double setup_seconds;  /* host time spent setting requests up, summed over the workers */
+  double retire_seconds; /* host time spent retiring requests (receivers out, domain freed) */
 } pfdtd_server_stats;
 int pfdtd_server_stats_get(pfdtd_server* s, pfdtd_server_stats* st);
 /* Wait until no request is queued or running (timeout_s < 0: no limit). */

@@ -1,14 +1,19 @@
 // Request loop with continuous batching over the C ABI (pfdtd_server.h).
 //
-// One scheduler thread per server.  It keeps a FIFO of submitted requests
-// and a set of running ones.  Each pass it (1) retires running requests
-// whose domain stream has drained: receivers to the host, domain destroyed,
-// memory back to the budget; (2) admits queued requests in arrival order
-// while a slot is free and the head request's estimated bytes fit beside
-// the running ones: domain created and set up on its own stream, the whole
-// run queued with pfdtd_run_async.  The scheduler never waits on the device
-// as a whole: queries are per stream and allocations are stream-ordered, so
-// admitted requests overlap on the GPU while the host admits and retires.
+// One scheduler thread per server and a few set-up workers.  The scheduler
+// keeps a FIFO of submitted requests and a set of running ones.  Each pass it
+// (1) retires running requests whose domain stream has drained: receivers to
+// the host, domain destroyed, memory back to the budget; (2) admits queued
+// requests in arrival order while a slot is free and the head request's
+// estimated bytes fit beside the running and admitted ones: it reserves the
+// bytes and the slot and hands the request to a set-up worker, which creates
+// the domain on its own stream, uploads the room, builds the node classes and
+// queues the whole run with pfdtd_run_async, then makes the request running.
+// Set-up is host work (node bytes re-laid, class tables, graph capture) of up
+// to seconds for the largest rooms; on the workers it overlaps the running
+// requests, the retirements and the other set-ups.  Nothing waits on the
+// device as a whole: queries and synchronisations are per stream and
+// allocations are stream-ordered.
 #include <algorithm>
 #include <chrono>
 #include <cmath>
@@ -57,6 +62,9 @@ namespace {
 
 using Clock = std::chrono::steady_clock;
 
+// Requests set up at once (each on its own worker thread).
+constexpr int kSetupWorkers = 4;
+
 size_t storage_size(int precision) {
   return precision == PFDTD_F64 ? 8 : (precision == PFDTD_F32 ? 4 : 2);
 }
@@ -100,8 +108,13 @@ struct pfdtd_server {
   std::map<int64_t, Job> jobs;
   int64_t next_ticket = 1;
   bool stop = false;
-  int in_transit = 0;  // requests being admitted or retired with the lock released
+  int in_transit = 0;  // requests being retired with the lock released
+  int admitting = 0;   // requests handed to a set-up worker and not yet running
+  std::deque<int64_t> to_admit;
+  std::condition_variable cv_work;
+  bool workers_stop = false;
   std::thread thread;
+  std::vector<std::thread> workers;
   pfdtd_server_stats st{};
 };
 
@@ -214,6 +227,39 @@ int retire(Job& j) {
   return rc;
 }
 
+// Set-up worker: takes admitted requests in order, sets each up with the
+// lock released, then makes it running (or failed).
+void setup_worker(pfdtd_server* s) {
+  std::unique_lock<std::mutex> lk(s->mu);
+  for (;;) {
+    s->cv_work.wait(lk, [&] { return !s->to_admit.empty() || s->workers_stop; });
+    if (s->to_admit.empty()) break;
+    const int64_t t = s->to_admit.front();
+    s->to_admit.pop_front();
+    Job& j = s->jobs[t];  // std::map: the reference stays valid while unlocked
+    lk.unlock();
+    const Clock::time_point t0 = Clock::now();
+    const int rc = admit(s, j);
+    const double dt = std::chrono::duration<double>(Clock::now() - t0).count();
+    lk.lock();
+    s->admitting--;
+    s->st.setup_seconds += dt;
+    if (rc) {
+      j.state = PFDTD_REQ_FAILED;
+      j.t_done = Clock::now();
+      s->st.bytes_in_use -= j.bytes;
+      s->st.failed++;
+      s->cv_done.notify_all();
+    } else {
+      s->active.push_back(t);
+      s->st.admitted++;
+      s->st.running = (int64_t)s->active.size();
+      s->st.max_running = std::max<int>(s->st.max_running, (int)s->active.size());
+    }
+    s->cv_sched.notify_one();
+  }
+}
+
 void scheduler(pfdtd_server* s) {
   std::unique_lock<std::mutex> lk(s->mu);
   for (;;) {
@@ -230,9 +276,12 @@ void scheduler(pfdtd_server* s) {
       s->active.erase(s->active.begin() + (ptrdiff_t)i);
       s->in_transit++;
       lk.unlock();
+      const Clock::time_point t0 = Clock::now();
       const int rc = retire(j);
+      const double dt = std::chrono::duration<double>(Clock::now() - t0).count();
       lk.lock();
       s->in_transit--;
+      s->st.retire_seconds += dt;
       j.t_done = Clock::now();
       j.state = rc == PFDTD_OK && q == PFDTD_OK ? PFDTD_REQ_DONE : PFDTD_REQ_FAILED;
       s->st.bytes_in_use -= j.bytes;
@@ -248,8 +297,10 @@ void scheduler(pfdtd_server* s) {
       progress = true;
       s->cv_done.notify_all();
     }
-    // admit in arrival order while a slot and the memory are free
-    while (!s->stop && !s->queue.empty() && (int)s->active.size() < s->max_active) {
+    // admit in arrival order while a slot and the memory are free: reserve
+    // both and hand the request to a set-up worker
+    while (!s->stop && !s->queue.empty() &&
+           (int)s->active.size() + s->admitting < s->max_active) {
       const int64_t t = s->queue.front();
       Job& j = s->jobs[t];
       if (s->st.bytes_in_use + j.bytes > s->budget) break;
@@ -259,26 +310,12 @@ void scheduler(pfdtd_server* s) {
       s->st.bytes_peak = std::max(s->st.bytes_peak, s->st.bytes_in_use);
       j.state = PFDTD_REQ_RUNNING;
       j.t_admit = Clock::now();
-      s->in_transit++;
-      lk.unlock();
-      const int rc = admit(s, j);
-      lk.lock();
-      s->in_transit--;
-      if (rc) {
-        j.state = PFDTD_REQ_FAILED;
-        j.t_done = Clock::now();
-        s->st.bytes_in_use -= j.bytes;
-        s->st.failed++;
-        s->cv_done.notify_all();
-      } else {
-        s->active.push_back(t);
-        s->st.admitted++;
-        s->st.running = (int64_t)s->active.size();
-        s->st.max_running = std::max<int>(s->st.max_running, (int)s->active.size());
-      }
+      s->admitting++;
+      s->to_admit.push_back(t);
+      s->cv_work.notify_one();
       progress = true;
     }
-    if (s->stop && s->active.empty()) break;
+    if (s->stop && s->active.empty() && s->admitting == 0) break;
     if (!progress) s->cv_sched.wait_for(lk, std::chrono::microseconds(200));
   }
   // queued requests left at shutdown fail
@@ -431,6 +468,8 @@ int pfdtd_server_create(int device, uint64_t hbm_budget, int max_active, pfdtd_s
   s->device = device;
   s->budget = hbm_budget;
   s->max_active = max_active;
+  for (int i = 0; i < std::min(max_active, kSetupWorkers); ++i)
+    s->workers.emplace_back(setup_worker, s);
   s->thread = std::thread(scheduler, s);
   *out = s;
   return PFDTD_OK;
@@ -526,7 +565,9 @@ int pfdtd_server_stats_get(pfdtd_server* s, pfdtd_server_stats* st) {
 int pfdtd_server_drain(pfdtd_server* s, double timeout_s) {
   if (!s) return fail(PFDTD_ERR_ARG, "null server");
   std::unique_lock<std::mutex> lk(s->mu);
-  auto idle = [&] { return s->queue.empty() && s->active.empty() && s->in_transit == 0; };
+  auto idle = [&] {
+    return s->queue.empty() && s->active.empty() && s->in_transit == 0 && s->admitting == 0;
+  };
   if (timeout_s < 0) s->cv_done.wait(lk, idle);
   else if (!s->cv_done.wait_for(lk, std::chrono::duration<double>(timeout_s), idle))
     return fail(PFDTD_ERR_STATE, "requests still pending after the timeout");
@@ -541,6 +582,13 @@ int pfdtd_server_destroy(pfdtd_server* s) {
     s->cv_sched.notify_all();
   }
   if (s->thread.joinable()) s->thread.join();
+  {
+    // the scheduler has ended with no request left to set up
+    std::lock_guard<std::mutex> g(s->mu);
+    s->workers_stop = true;
+    s->cv_work.notify_all();
+  }
+  for (std::thread& w : s->workers) w.join();
   for (auto& kv : s->jobs) delete kv.second.req;
   delete s;
   return PFDTD_OK;

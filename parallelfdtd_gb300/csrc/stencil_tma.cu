@@ -28,7 +28,9 @@
 #include <cuda.h>
 
 #include <algorithm>
+#include <atomic>
 #include <cstring>
+#include <mutex>
 #include <type_traits>
 
 namespace pfdtd {
@@ -692,20 +694,19 @@ typedef CUresult (*EncodeTiledFn)(CUtensorMap*, CUtensorMapDataType, cuuint32_t,
                                   const cuuint32_t*, CUtensorMapInterleave, CUtensorMapSwizzle,
                                   CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
 
+// Looked up once per process (a function-local static: thread-safe, since
+// domains may be set up from several threads at once).
 EncodeTiledFn encode_fn() {
-  static EncodeTiledFn fn = nullptr;
-  static bool tried = false;
-  if (!tried) {
-    tried = true;
+  static const EncodeTiledFn fn = [] {
     void* p = nullptr;
     cudaDriverEntryPointQueryResult q;
     if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault,
                                          &q) == cudaSuccess &&
         q == cudaDriverEntryPointSuccess)
-      fn = (EncodeTiledFn)p;
-    else
-      cudaGetLastError();
-  }
+      return (EncodeTiledFn)p;
+    cudaGetLastError();
+    return (EncodeTiledFn) nullptr;
+  }();
   return fn;
 }
 
@@ -763,26 +764,34 @@ int launch_tma_t(pfdtd_domain* d, const void* cur, void* past, cudaStream_t s) {
     ts.ready = true;
   }
   // the shared-memory opt-in, once per instantiation and device
-  // (IWB: and its resident CTAs per SM, which registers limit as well)
-  static bool attr_done[64] = {};
-  static int occupancy[64] = {};
+  // (IWB: and its resident CTAs per SM, which registers limit as well);
+  // several threads may launch at once (a request loop sets up its domains
+  // concurrently), so the first one does it under a lock
+  static std::atomic<bool> attr_done[64];
+  static std::atomic<int> occupancy[64];
+  static std::mutex attr_mu;
   if (d->device >= 64) return fail(PFDTD_ERR_UNSUPPORTED, "device index above 63");
-  if (!attr_done[d->device]) {
-    PFDTD_CK(cudaFuncSetAttribute(k_update_tma<S, C, SCHEME, Lay, BATCHED>,
-                                  cudaFuncAttributeMaxDynamicSharedMemorySize, Lay::SMEM));
-    if (SCHEME == 3)
-      PFDTD_CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(
-          &occupancy[d->device], k_update_tma<S, C, SCHEME, Lay, BATCHED>, Lay::THREADS,
-          Lay::SMEM));
-    attr_done[d->device] = true;
+  if (!attr_done[d->device].load(std::memory_order_acquire)) {
+    std::lock_guard<std::mutex> lock(attr_mu);
+    if (!attr_done[d->device].load(std::memory_order_relaxed)) {
+      PFDTD_CK(cudaFuncSetAttribute(k_update_tma<S, C, SCHEME, Lay, BATCHED>,
+                                    cudaFuncAttributeMaxDynamicSharedMemorySize, Lay::SMEM));
+      int occ = 0;
+      if (SCHEME == 3)
+        PFDTD_CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(
+            &occ, k_update_tma<S, C, SCHEME, Lay, BATCHED>, Lay::THREADS, Lay::SMEM));
+      occupancy[d->device].store(occ, std::memory_order_relaxed);
+      attr_done[d->device].store(true, std::memory_order_release);
+    }
   }
+  const int occ = occupancy[d->device].load(std::memory_order_relaxed);
   const int gx = (int)((XE + kTX - 1) / kTX);
   const int gy = (int)((d->Y + Lay::TY - 1) / Lay::TY);
   // z-chunks: several per tile so that the grid fills the machine in whole
   // waves of (SMs x resident CTAs), each chunk at least 16 planes long.
   const int64_t per_sm =
-      occupancy[d->device] > 0
-          ? occupancy[d->device]
+      occ > 0
+          ? occ
           : std::max<int64_t>(1, (228 * 1024) / (Lay::SMEM + 1024 + 8192));
   const int64_t resident = (int64_t)d->sm_count * per_sm;
   const int64_t tiles = (int64_t)gx * gy;

@@ -29,7 +29,8 @@ class _Stats(C.Structure):
     _fields_ = [("submitted", C.c_int64), ("admitted", C.c_int64), ("completed", C.c_int64),
                 ("failed", C.c_int64), ("queued", C.c_int64), ("running", C.c_int64),
                 ("bytes_in_use", C.c_uint64), ("bytes_peak", C.c_uint64),
-                ("max_running", C.c_int), ("node_updates", C.c_double)]
+                ("max_running", C.c_int), ("node_updates", C.c_double),
+                ("setup_seconds", C.c_double), ("retire_seconds", C.c_double)]
 
 
 def _p(a, t):
