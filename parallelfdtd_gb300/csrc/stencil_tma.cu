@@ -36,7 +36,7 @@
 namespace pfdtd {
 namespace {
 
-constexpr int kVec = 4;             // consecutive x nodes per consumer thread
+constexpr int kVec = 4;             // consecutive x elements per consumer thread (default)
 constexpr uint64_t kWaitLimitNs = 2000000000ull;  // 2 s per wait, far above any real wait
 
 
@@ -49,11 +49,14 @@ __host__ __device__ constexpr int round128(int b) { return (b + 127) / 128 * 128
 // Tile shape: TX nodes along x (box inner extent TX + 2H <= 256), TY rows,
 // NS pipeline stages; MASK: each stage also carries the plane's IWB
 // closed-neighbour masks (4 bytes per node); MINB: CTAs per SM the register
-// allocation must allow.
+// allocation must allow; VEC: consecutive x elements per consumer thread (4,
+// or 8 for 16-bit fields: one 16-byte shared-memory load per row vector, and
+// the per-thread index and barrier work spread over twice the updates).
 template <typename S, typename C, int TX_, int TY_, int NS_, bool XHALO_ = true, bool MASK_ = false,
-          int MINB_ = 1>
+          int MINB_ = 1, int VEC_ = kVec>
 struct Layout {
-  static constexpr int TX = TX_, TY = TY_, NS = NS_, MINB = MINB_;
+  static constexpr int TX = TX_, TY = TY_, NS = NS_, MINB = MINB_, VEC = VEC_;
+  static_assert(VEC == 4 || (VEC == 8 && sizeof(S) == 2), "8-element vectors: 16-bit fields");
   // With XHALO the box carries a 16-byte x halo on both sides; without it the
   // box is exactly TX wide (up to 256) and the threads at the tile's x edges
   // read their outside neighbour from global memory (an L2 hit: the
@@ -74,10 +77,10 @@ struct Layout {
   static constexpr int BAR_OFF = STAGE * NS;
   // full + empty barriers + abort flag, plus 128 B to align the dynamic base
   static constexpr int SMEM = BAR_OFF + 2 * NS * 8 + 16 + 128;
-  static constexpr int ROW_THREADS = TX / kVec;                // threads per tile row
-  static constexpr int CONSUMER_WARPS = TX * TY / kVec / 32;
+  static constexpr int ROW_THREADS = TX / VEC;                 // threads per tile row
+  static constexpr int CONSUMER_WARPS = TX * TY / VEC / 32;
   static constexpr int THREADS = (CONSUMER_WARPS + 1) * 32;
-  static_assert(CONSUMER_WARPS * 32 * kVec == TX * TY, "consumer mapping");
+  static_assert(CONSUMER_WARPS * 32 * VEC == TX * TY, "consumer mapping");
   static_assert(PW <= 256 && (PW * (int)sizeof(S)) % 16 == 0, "TMA box row");
 };
 
@@ -117,35 +120,42 @@ __device__ __forceinline__ bool mbar_test(uint32_t bar, uint32_t parity) {
   return done != 0;
 }
 
-// Wait for the phase with the given parity, for at most limit_ns; false on
-// expiry.  A bound under 1 ms (a watchdog set short) polls without blocking
-// and reads the clock at every poll, since a blocking try_wait may itself
-// sleep longer than such a bound.
-__device__ __forceinline__ bool mbar_wait(uint32_t bar, uint32_t parity,
-                                          uint64_t limit_ns = kWaitLimitNs) {
+__device__ __forceinline__ bool mbar_try(uint32_t bar, uint32_t parity) {
+  uint32_t done;
+  asm volatile(
+      "{\n\t.reg .pred p;\n\t"
+      "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+      "selp.u32 %0, 1, 0, p;\n\t}"
+      : "=r"(done)
+      : "r"(bar), "r"(parity)
+      : "memory");
+  return done != 0;
+}
+
+// The waiting part of mbar_wait.  A bound under 1 ms (a watchdog set short)
+// polls without blocking and reads the clock at every poll, since a blocking
+// try_wait may itself sleep longer than such a bound; a longer bound blocks
+// in try_wait and reads the clock every 256 polls.
+__device__ __forceinline__ bool mbar_wait_slow(uint32_t bar, uint32_t parity, uint64_t limit_ns) {
+  const uint64_t t0 = global_ns();
   if (limit_ns < 1000000ull) {
-    const uint64_t t0 = global_ns();
     while (!mbar_test(bar, parity))
       if (global_ns() - t0 > limit_ns) return false;
     return true;
   }
-  uint64_t start = 0;
-  for (uint32_t i = 0;; ++i) {
-    uint32_t done;
-    asm volatile(
-        "{\n\t.reg .pred p;\n\t"
-        "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
-        "selp.u32 %0, 1, 0, p;\n\t}"
-        : "=r"(done)
-        : "r"(bar), "r"(parity)
-        : "memory");
-    if (done) return true;
-    if ((i & 255) == 0) {
-      const uint64_t now = global_ns();
-      if (i == 0) start = now;
-      else if (now - start > limit_ns) return false;
-    }
+  for (uint32_t i = 1;; ++i) {
+    if (mbar_try(bar, parity)) return true;
+    if ((i & 255) == 0 && global_ns() - t0 > limit_ns) return false;
   }
+}
+
+// Wait for the phase with the given parity, for at most limit_ns; false on
+// expiry.  The common case in a streaming consumer, a phase already complete,
+// costs one non-blocking test.
+__device__ __forceinline__ bool mbar_wait(uint32_t bar, uint32_t parity,
+                                          uint64_t limit_ns = kWaitLimitNs) {
+  if (mbar_test(bar, parity)) return true;
+  return mbar_wait_slow(bar, parity, limit_ns);
 }
 
 __device__ __forceinline__ void tma_load_2d(uint32_t dst, const CUtensorMap* map, int x, int y,
@@ -157,8 +167,10 @@ __device__ __forceinline__ void tma_load_2d(uint32_t dst, const CUtensorMap* map
       : "memory");
 }
 
-// Four consecutive elements of a 16-byte aligned shared-memory row.
-template <typename S> struct V4 { S v[4]; };
+// N consecutive elements of a shared-memory row (16-byte aligned for a
+// 16-byte vector).
+template <typename S, int N> struct Vn { S v[N]; };
+template <typename S> using V4 = Vn<S, 4>;
 __device__ __forceinline__ V4<float> lds4(const float* p) {
   const float4 t = *reinterpret_cast<const float4*>(p);
   return V4<float>{{t.x, t.y, t.z, t.w}};
@@ -216,6 +228,53 @@ __device__ __forceinline__ void stg4(float* p, const float (&v)[4]) {
 __device__ __forceinline__ void stg4(double* p, const double (&v)[4]) {
   reinterpret_cast<double2*>(p)[0] = make_double2(v[0], v[1]);
   reinterpret_cast<double2*>(p)[1] = make_double2(v[2], v[3]);
+}
+
+// Eight consecutive 16-bit elements: one 16-byte load or store.
+template <typename H2, typename S>
+__device__ __forceinline__ Vn<S, 8> unpack8_16(const uint4 t) {
+  H2 a, b, c, e;
+  memcpy(&a, &t.x, 4);
+  memcpy(&b, &t.y, 4);
+  memcpy(&c, &t.z, 4);
+  memcpy(&e, &t.w, 4);
+  return Vn<S, 8>{{a.x, a.y, b.x, b.y, c.x, c.y, e.x, e.y}};
+}
+template <typename S> struct Half2Of;
+template <> struct Half2Of<__half> { using T = __half2; };
+template <> struct Half2Of<__nv_bfloat16> { using T = __nv_bfloat162; };
+
+// Vector loads and stores of N = 4 or 8 elements (8: 16-bit types only).
+template <int N, typename S>
+__device__ __forceinline__ Vn<S, N> ldsv(const S* p) {
+  if constexpr (N == 4) {
+    return lds4(p);
+  } else {
+    static_assert(N == 8 && sizeof(S) == 2, "8-element vectors are 16-bit");
+    return unpack8_16<typename Half2Of<S>::T, S>(*reinterpret_cast<const uint4*>(p));
+  }
+}
+template <int N, typename S>
+__device__ __forceinline__ Vn<S, N> ldgv(const S* p) {
+  if constexpr (N == 4) {
+    return ldg4(p);
+  } else {
+    static_assert(N == 8 && sizeof(S) == 2, "8-element vectors are 16-bit");
+    return unpack8_16<typename Half2Of<S>::T, S>(__ldg(reinterpret_cast<const uint4*>(p)));
+  }
+}
+template <int N, typename S>
+__device__ __forceinline__ void stgv(S* p, const S (&v)[N]) {
+  if constexpr (N == 4) {
+    stg4(p, v);
+  } else {
+    static_assert(N == 8 && sizeof(S) == 2, "8-element vectors are 16-bit");
+    uint16_t u[8];
+    memcpy(u, v, 16);
+    *reinterpret_cast<uint4*>(p) =
+        make_uint4(u[0] | ((uint32_t)u[1] << 16), u[2] | ((uint32_t)u[3] << 16),
+                   u[4] | ((uint32_t)u[5] << 16), u[6] | ((uint32_t)u[7] << 16));
+  }
 }
 
 // IWB 27-point update (no counterpart in the reference), a consumer thread's
@@ -398,14 +457,16 @@ k_update_tma(const __grid_constant__ CUtensorMap map_cur, const __grid_constant_
   }
 
   // ---------------- consumers ----------------
-  // Thread -> 4 consecutive x nodes of one tile row: 16 threads per row, two
-  // rows per warp.
+  // Thread -> VEC consecutive x elements of one tile row (TX / VEC threads
+  // per row).
+  constexpr int VEC = Lay::VEC;
+  static_assert(SCHEME != 3 || VEC == kVec, "the IWB consumer works on 4-node vectors");
   const int t = threadIdx.x;
-  const int lx = (t % kThreadsPerRow) * kVec;
+  const int lx = (t % kThreadsPerRow) * VEC;
   const int ly = t / kThreadsPerRow;
   const int x = x0 + lx;
   const int y = y0 + ly;
-  const bool active = (x < X) && (y < Y);  // X is a multiple of 4: all 4 or none
+  const bool active = (x < X) && (y < Y);  // X is a multiple of VEC: all VEC or none
   const int si = (ly + 1) * PW + lx + H;   // centre of the thread's first node
   bool ok = mbar_wait(bar_full, 0, wait_ns) && mbar_wait(bar_full + 8, 0, wait_ns);
   // IWB: raw in-plane sums of planes z-1 (m) and z (c) carried along the
@@ -516,6 +577,7 @@ k_update_tma(const __grid_constant__ CUtensorMap map_cur, const __grid_constant_
         }
       }
     } else if (active) {
+      using Vec = Vn<S, VEC>;
       const S* Pm = (const S*)(smem + sm * Lay::STAGE + Lay::P_OFF);
       const S* Pc = (const S*)(smem + sc_ * Lay::STAGE + Lay::P_OFF);
       const S* Pn = (const S*)(smem + sp_ * Lay::STAGE + Lay::P_OFF);
@@ -523,81 +585,96 @@ k_update_tma(const __grid_constant__ CUtensorMap map_cur, const __grid_constant_
       const C* Cl = (const C*)(smem + sp_ * Lay::STAGE + Lay::CL_OFF);
       const int z = z0 + j;
       const int64_t idx = (int64_t)z * XY + (int64_t)y * X + x;
-      const V4<S> vc = lds4(Pc + si);
-      const V4<S> vym = lds4(Pc + si - PW);
-      const V4<S> vyp = lds4(Pc + si + PW);
-      const V4<S> vzm = lds4(Pm + si);
-      const V4<S> vzp = lds4(Pn + si);
-      const V4<S> vpp = lds4(Pq + ly * kTX + lx);
+      const Vec vc = ldsv<VEC>(Pc + si);
+      const Vec vym = ldsv<VEC>(Pc + si - PW);
+      const Vec vyp = ldsv<VEC>(Pc + si + PW);
+      const Vec vzm = ldsv<VEC>(Pm + si);
+      const Vec vzp = ldsv<VEC>(Pn + si);
+      const Vec vpp = ldsv<VEC>(Pq + ly * kTX + lx);
       A left = (A)0, right = (A)0;
-      V4<S> vxm, vxp;
-      unsigned cid[kVec];
+      Vec vxm, vxp;
+      unsigned cid[VEC];
       if (BATCHED) {
         const int kk = 1 << kshift;
-        vxm = lx >= kk ? lds4(Pc + si - kk) : ldg4(P + idx - kk);
+        vxm = lx >= kk ? ldsv<VEC>(Pc + si - kk) : ldgv<VEC>(P + idx - kk);
         // the last node of a row reads its flat-index neighbour (the next
         // row's first node) from global memory, also in a partly filled tile
-        vxp = (lx + kk < kTX && x + kk < X) ? lds4(Pc + si + kk) : ldg4(P + idx + kk);
+        vxp = (lx + kk < kTX && x + kk < X) ? ldsv<VEC>(Pc + si + kk) : ldgv<VEC>(P + idx + kk);
         const unsigned c = Cl[ly * (kTX >> kshift) + (lx >> kshift)];
 #pragma unroll
-        for (int e = 0; e < kVec; ++e) cid[e] = c;
+        for (int e = 0; e < VEC; ++e) cid[e] = c;
       } else {
         if (x == 0 || (!Lay::XHALO && lx == 0)) left = St::load(P[idx - 1]);
         else left = St::load(Pc[si - 1]);
-        if (x + kVec == X || (!Lay::XHALO && lx + kVec == kTX)) right = St::load(P[idx + kVec]);
-        else right = St::load(Pc[si + kVec]);
+        if (x + VEC == X || (!Lay::XHALO && lx + VEC == kTX)) right = St::load(P[idx + VEC]);
+        else right = St::load(Pc[si + VEC]);
       }
       if (BATCHED) {
-      } else if (sizeof(C) == 1) {
+      } else if (sizeof(C) * VEC == 4) {
         const uint32_t w = *reinterpret_cast<const uint32_t*>(Cl + ly * kTX + lx);
 #pragma unroll
-        for (int e = 0; e < kVec; ++e) cid[e] = (w >> (8 * e)) & 0xFFu;
-      } else {
+        for (int e = 0; e < 4; ++e) cid[e] = (w >> (8 * e)) & 0xFFu;
+      } else if (sizeof(C) * VEC == 8) {
         const uint2 w = *reinterpret_cast<const uint2*>(Cl + ly * kTX + lx);
-        cid[0] = w.x & 0xFFFFu; cid[1] = w.x >> 16; cid[2] = w.y & 0xFFFFu; cid[3] = w.y >> 16;
+        const uint32_t ws[2] = {w.x, w.y};
+#pragma unroll
+        for (int e = 0; e < VEC; ++e)
+          cid[e] = sizeof(C) == 1 ? (ws[e >> 2] >> (8 * (e & 3))) & 0xFFu
+                                  : (ws[e >> 1] >> (16 * (e & 1))) & 0xFFFFu;
+      } else {
+        const uint4 w = *reinterpret_cast<const uint4*>(Cl + ly * kTX + lx);
+        const uint32_t ws[4] = {w.x, w.y, w.z, w.w};
+#pragma unroll
+        for (int e = 0; e < VEC; ++e) cid[e] = (ws[e >> 1] >> (16 * (e & 1))) & 0xFFFFu;
       }
       if constexpr ((SCHEME == 0 || SCHEME == 4) && sizeof(A) == 4) {
-        // Forward update of the thread's 4 elements as two packed pairs: the
-        // same operations and rounding as the scalar loop below, with every
+        // Forward update of the thread's elements as packed pairs: the same
+        // operations and rounding as the scalar loop below, with every
         // product formed as fma(x, y, -0) so that none is contracted.
         // Batched: the pairs are fields of one node (one class); otherwise
         // adjacent x nodes (a class each).
         using namespace px;
+        constexpr int NP = VEC / 2;
         auto coef = [&](int e) -> PackedCoef<A> {
           if (kSmemTab) return stab[cid[e]];
           return PackedCoef<A>{__ldg(tab.a + cid[e]), __ldg(tab.b + cid[e]),
                                __ldg(tab.c + cid[e]), __ldg(tab.pos + cid[e])};
         };
         const f2 l22 = pk2(l2, l2), nz = pk2(nzf, nzf);
-        auto pr = [](const V4<S>& v, int h) -> f2 {
+        auto pr = [](const Vec& v, int h) -> f2 {
           return pk2(St::load(v.v[2 * h]), St::load(v.v[2 * h + 1]));
         };
-        f2 aa[2], bb[2], cc[2], ee[2], xm2[2], xp2[2];
+        f2 aa[NP], bb[NP], cc[NP], ee[NP], xm2[NP], xp2[NP];
         if constexpr (BATCHED) {
           const PackedCoef<A> k = coef(0);
-          aa[0] = aa[1] = pk2(k.a, k.a);
-          bb[0] = bb[1] = pk2(k.b, k.b);
-          cc[0] = cc[1] = pk2(k.c, k.c);
-          ee[0] = ee[1] = pk2(__uint_as_float(k.pos), __uint_as_float(k.pos));
-          xm2[0] = pr(vxm, 0); xm2[1] = pr(vxm, 1);
-          xp2[0] = pr(vxp, 0); xp2[1] = pr(vxp, 1);
-        } else {
 #pragma unroll
-          for (int h = 0; h < 2; ++h) {
+          for (int h = 0; h < NP; ++h) {
+            aa[h] = pk2(k.a, k.a);
+            bb[h] = pk2(k.b, k.b);
+            cc[h] = pk2(k.c, k.c);
+            ee[h] = pk2(__uint_as_float(k.pos), __uint_as_float(k.pos));
+            xm2[h] = pr(vxm, h);
+            xp2[h] = pr(vxp, h);
+          }
+        } else {
+          A cv[VEC];
+#pragma unroll
+          for (int e = 0; e < VEC; ++e) cv[e] = St::load(vc.v[e]);
+#pragma unroll
+          for (int h = 0; h < NP; ++h) {
             const PackedCoef<A> k0 = coef(2 * h), k1 = coef(2 * h + 1);
             aa[h] = pk2(k0.a, k1.a);
             bb[h] = pk2(k0.b, k1.b);
             cc[h] = pk2(k0.c, k1.c);
             ee[h] = pk2(__uint_as_float(k0.pos), __uint_as_float(k1.pos));
+            // node e reads x[e-1] and x[e+1]; x[-1] = left, x[VEC] = right
+            xm2[h] = pk2(h == 0 ? left : cv[2 * h - 1], cv[2 * h]);
+            xp2[h] = pk2(cv[2 * h + 1], h == NP - 1 ? right : cv[2 * h + 2]);
           }
-          const A c0 = St::load(vc.v[0]), c1 = St::load(vc.v[1]), c2 = St::load(vc.v[2]),
-                  c3 = St::load(vc.v[3]);
-          xm2[0] = pk2(left, c0); xm2[1] = pk2(c1, c2);
-          xp2[0] = pk2(c1, c2); xp2[1] = pk2(c3, right);
         }
-        S res[kVec];
+        S res[VEC];
 #pragma unroll
-        for (int h = 0; h < 2; ++h) {
+        for (int h = 0; h < NP; ++h) {
           const f2 s6 = add2(add2(add2(add2(add2(pr(vzp, h), pr(vzm, h)), pr(vyp, h)),
                                       pr(vym, h)), xp2[h]), xm2[h]);
           f2 o;
@@ -625,11 +702,11 @@ k_update_tma(const __grid_constant__ CUtensorMap map_cur, const __grid_constant_
             res[2 * h + 1] = __high2bfloat16(t);
           }
         }
-        stg4(Pp + idx, res);
+        stgv<VEC>(Pp + idx, res);
       } else {
-      S res[kVec];
+      S res[VEC];
 #pragma unroll
-      for (int e = 0; e < kVec; ++e) {
+      for (int e = 0; e < VEC; ++e) {
         const A pc = St::load(vc.v[e]);
         A xm, xp;
         if (BATCHED) {
@@ -637,7 +714,7 @@ k_update_tma(const __grid_constant__ CUtensorMap map_cur, const __grid_constant_
           xp = St::load(vxp.v[e]);
         } else {
           xm = e == 0 ? left : St::load(vc.v[e - 1]);
-          xp = e == kVec - 1 ? right : St::load(vc.v[e + 1]);
+          xp = e == VEC - 1 ? right : St::load(vc.v[e + 1]);
         }
         const A ym = St::load(vym.v[e]), yp = St::load(vyp.v[e]);
         const A pm = St::load(vzm.v[e]), pn = St::load(vzp.v[e]);
@@ -671,7 +748,7 @@ k_update_tma(const __grid_constant__ CUtensorMap map_cur, const __grid_constant_
         }
         res[e] = St::store(out);
       }
-      stg4(Pp + idx, res);
+      stgv<VEC>(Pp + idx, res);
       }
     }
     __syncwarp();
@@ -890,9 +967,14 @@ int launch_tma_s<float>(pfdtd_domain* d, const void* cur, void* past, cudaStream
   return fail(PFDTD_ERR_ARG, "unknown TMA tile shape");
 }
 
-// 16-bit storage tiles: 0 64x16 (halo in box), 1 128x8, 2 256x8, 3 256x4.
-#define PFDTD_F16_TILES(X) \
-  X(0, 64, 16, 8, true) X(1, 128, 8, 8, false) X(2, 256, 8, 8, false) X(3, 256, 4, 8, false)
+// 16-bit storage tiles (id, TX, TY, stages, x halo in the box, CTAs per SM,
+// elements per thread): 0 64x16 (halo in box), 1 128x8, 2 256x8, 3 256x4, with
+// 4 elements per thread; 4 256x8, 5 256x8 (6 stages, three CTAs per SM),
+// 6 256x4 (four CTAs), 7 128x8 with 8 elements per thread.
+#define PFDTD_F16_TILES(X)                                                                    \
+  X(0, 64, 16, 8, true, 2, 4) X(1, 128, 8, 8, false, 2, 4) X(2, 256, 8, 8, false, 2, 4)         \
+  X(3, 256, 4, 8, false, 2, 4) X(4, 256, 8, 8, false, 2, 8) X(5, 256, 8, 6, false, 3, 8)       \
+  X(6, 256, 4, 8, false, 4, 8) X(7, 128, 8, 8, false, 2, 8)
 
 int auto_tile16(const pfdtd_domain* d) {
   if (d->X % 256 == 0) return 2;
@@ -907,7 +989,15 @@ int launch_tma_16(pfdtd_domain* d, const void* cur, void* past, cudaStream_t s) 
   // too few loads in flight to stream at HBM speed.
   if (d->K > 1) {
     // batched tiles: default 256 x 8 elements, 8 stages, two CTAs per SM;
-    // 1 = 256 x 4, 8 stages, four CTAs; 2 = 256 x 8, 6 stages, two CTAs
+    // 1 = 256 x 4, 8 stages, four CTAs; 2 = 256 x 8, 6 stages, two CTAs;
+    // with 8 elements (fields of one node) per thread, for K a multiple of 8:
+    // 3 = 256 x 8, 8 stages, two CTAs; 4 = 256 x 4, 8 stages, four CTAs
+    if (d->K % 8 == 0 && d->tma_tile == 3)
+      return launch_tma_batched<S, Layout<S, uint8_t, 256, 8, 8, false, false, 2, 8>,
+                                Layout<S, uint16_t, 256, 8, 8, false, false, 2, 8>>(d, cur, past, s);
+    if (d->K % 8 == 0 && d->tma_tile == 4)
+      return launch_tma_batched<S, Layout<S, uint8_t, 256, 4, 8, false, false, 4, 8>,
+                                Layout<S, uint16_t, 256, 4, 8, false, false, 4, 8>>(d, cur, past, s);
     if (d->tma_tile == 1)
       return launch_tma_batched<S, Layout<S, uint8_t, 256, 4, 8, false, false, 4>,
                                 Layout<S, uint16_t, 256, 4, 8, false, false, 4>>(d, cur, past, s);
@@ -917,15 +1007,15 @@ int launch_tma_16(pfdtd_domain* d, const void* cur, void* past, cudaStream_t s) 
     return launch_tma_batched<S, Layout<S, uint8_t, 256, 8, 8, false, false, 2>,
                               Layout<S, uint16_t, 256, 8, 8, false, false, 2>>(d, cur, past, s);
   }
-  switch (d->tma_tile < 0 || d->tma_tile > 3 ? auto_tile16(d) : d->tma_tile) {
-#define PFDTD_CASE16(id, tx, ty, ns, xh)                                                  \
+  switch (d->tma_tile < 0 || d->tma_tile > 7 ? auto_tile16(d) : d->tma_tile) {
+#define PFDTD_CASE16(id, tx, ty, ns, xh, minb, vec)                                       \
   case id:                                                                                \
-    return launch_tma_l<S, Layout<S, uint8_t, tx, ty, ns, xh, false, 2>,                   \
-                        Layout<S, uint16_t, tx, ty, ns, xh, false, 2>>(d, cur, past, s);
+    return launch_tma_l<S, Layout<S, uint8_t, tx, ty, ns, xh, false, minb, vec>,           \
+                        Layout<S, uint16_t, tx, ty, ns, xh, false, minb, vec>>(d, cur, past, s);
     PFDTD_F16_TILES(PFDTD_CASE16)
 #undef PFDTD_CASE16
   }
-  return fail(PFDTD_ERR_ARG, "unknown TMA tile shape for 16-bit fields (0..3)");
+  return fail(PFDTD_ERR_ARG, "unknown TMA tile shape for 16-bit fields (0..7)");
 }
 
 template <>

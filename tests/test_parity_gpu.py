@@ -403,8 +403,14 @@ def test_tma_wrap_neighbours_on_outer_faces(gpu, O):
 
 @pytest.mark.parametrize("tile", list(range(9)))
 @pytest.mark.parametrize("centred", [False, True])
-def test_tma_tile_shapes_bit_identical(gpu, O, tile, centred):
-    room = rooms.boxes_room((208, 52, 40), n_boxes=6, edge=(5, 16), n_materials=9, seed=14)
+@pytest.mark.parametrize("wide", [False, True])
+def test_tma_tile_shapes_bit_identical(gpu, O, tile, centred, wide):
+    """FP32 tile shapes; wide: materials drawn per voxel, more than 256 node
+    classes, so the class ids are 16-bit."""
+    room = rooms.boxes_room((208, 52, 40), n_boxes=6, edge=(5, 16), n_materials=150 if wide else 9,
+                            seed=14)
+    if wide:
+        room.mat[...] = np.random.default_rng(5).integers(0, 150, room.mat.shape, dtype=np.uint8)
     steps = 60
     src = room.random_air_nodes(1, seed=3)
     rec = room.random_air_nodes(4, seed=4)
@@ -425,6 +431,47 @@ def test_tma_tile_shapes_bit_identical(gpu, O, tile, centred):
                      [1], pulse[None], [room.flat(*x) for x in rec], steps, scheme=2 if centred else 0)
     assert_parity(g, r, "f32")
     assert np.array_equal(P, rP)
+
+
+@pytest.mark.parametrize("tile", list(range(8)))
+@pytest.mark.parametrize("prec", ["f16", "bf16"])
+@pytest.mark.parametrize("centred,wide", [(False, False), (True, False), (False, True),
+                                          (True, True)])
+def test_16bit_tile_shapes_bit_identical(gpu, O, tile, prec, centred, wide):
+    """Every 16-bit tile shape (4 and 8 elements per thread), forward and
+    centred, with 8-bit class ids and (wide: materials drawn per voxel, more
+    than 256 node classes) 16-bit class ids; X = 208 leaves partly filled
+    tiles.  Bit-identical to the oracle with the same storage rounding."""
+    room = rooms.boxes_room((208, 52, 40), n_boxes=6, edge=(5, 16), n_materials=150 if wide else 9,
+                            seed=16)
+    if wide:
+        room.mat[...] = np.random.default_rng(5).integers(0, 150, room.mat.shape, dtype=np.uint8)
+    steps = 60
+    src = room.random_air_nodes(1, seed=3)
+    rec = room.random_air_nodes(4, seed=4)
+    pulse = rooms.gaussian_pulse(steps, 3.0)
+    pos, mat = O.encode_nodes(room.bid, room.mat, centred)
+    X, Y, Z = room.dims
+    keys = np.unique(pos.reshape(Z, -1)[1:Z - 1].astype(np.int32) * 256 + mat.reshape(Z, -1)[1:Z - 1])
+    assert (len(keys) > 256) == wide
+    with Domain(room.dims, prec) as d:
+        d.set_voxels(room.bid, room.mat, centred=centred)
+        d.set_materials(room.admittance)
+        d.set_params()
+        d.set_scheme("centred" if centred else "forward")
+        d.set_kernel("tma")
+        L.call("pfdtd_set_tile", d.handle, tile)
+        d.set_sources(src, [1], pulse[None])
+        d.set_receivers(rec)
+        g, _, _ = d.run(steps)
+        assert d.kernel() == "tma"
+        P = d.download_field(L.FIELD_CURRENT)
+    r, rP, _ = O.run(pos, mat, room.dims, room.admittance, default_params(), [room.flat(*src[0])],
+                     [1], pulse[None], [room.flat(*x) for x in rec], steps,
+                     scheme=2 if centred else 0, storage=prec)
+    assert np.abs(r).max() > 1e-4
+    assert np.array_equal(g, r)
+    assert np.array_equal(P.view(np.uint16), rP.view(np.uint16))
 
 
 @pytest.mark.parametrize("variant", ["zmarch", "tma"])
@@ -944,11 +991,13 @@ def test_batched_partly_filled_tiles(gpu, O, fields, prec):
         assert np.array_equal(g[f], r[0]), f"field {f}"
 
 
-@pytest.mark.parametrize("tile", [1, 2])
-@pytest.mark.parametrize("fields,prec", [(16, "f16"), (8, "bf16")])
-def test_batched_16bit_tile_shapes(gpu, O, monkeypatch, tile, fields, prec):
+@pytest.mark.parametrize("tile", [1, 2, 3, 4])
+@pytest.mark.parametrize("fields,prec", [(16, "f16"), (8, "bf16"), (4, "f16")])
+@pytest.mark.parametrize("centred", [False, True])
+def test_batched_16bit_tile_shapes(gpu, O, monkeypatch, tile, fields, prec, centred):
     """The batched 16-bit tile shapes (1: 256 x 4 elements, four CTAs per SM;
-    2: 256 x 8, six stages) equal an oracle run of each field alone."""
+    2: 256 x 8, six stages; 3 and 4: 8 fields per thread, K a multiple of 8,
+    else the default shape) equal an oracle run of each field alone."""
     monkeypatch.setenv("PFDTD_TMA_TILE", str(tile))
     room = rooms.boxes_room((64, 48, 40), n_boxes=5, edge=(5, 14), n_materials=6, seed=45)
     steps = 90
@@ -957,17 +1006,19 @@ def test_batched_16bit_tile_shapes(gpu, O, monkeypatch, tile, fields, prec):
     recs = room.random_air_nodes(fields, seed=6)
     samples = np.stack([pulse * (1 + 0.1 * f) for f in range(fields)])
     with Domain(room.dims, prec, fields=fields) as d:
-        d.set_voxels(room.bid, room.mat, centred=False)
+        d.set_voxels(room.bid, room.mat, centred=centred)
         d.set_materials(room.admittance)
         d.set_params()
+        d.set_scheme("centred" if centred else "forward")
         d.set_sources(srcs, [1] * fields, samples, fields=list(range(fields)))
         d.set_receivers(recs, fields=list(range(fields)))
         g, _, st = d.run(steps)
         assert st == 0 and d.kernel() == "tma"
     monkeypatch.delenv("PFDTD_TMA_TILE", raising=False)
-    pos, mat = O.encode_nodes(room.bid, room.mat, False)
+    pos, mat = O.encode_nodes(room.bid, room.mat, centred)
     for f in (0, fields - 1):
         r, _, _ = O.run(pos, mat, room.dims, room.admittance, default_params(),
                         [room.flat(*srcs[f])], [1], samples[f:f + 1], [room.flat(*recs[f])],
-                        steps, storage=prec)
+                        steps, storage=prec, scheme=2 if centred else 0)
+        assert np.abs(r).max() > 1e-6
         assert np.array_equal(g[f], r[0]), f"field {f}"
