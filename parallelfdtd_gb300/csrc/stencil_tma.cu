@@ -51,11 +51,13 @@ __host__ __device__ constexpr int round128(int b) { return (b + 127) / 128 * 128
 // closed-neighbour masks (4 bytes per node); MINB: CTAs per SM the register
 // allocation must allow; VEC: consecutive x elements per consumer thread (4,
 // or 8 for 16-bit fields: one 16-byte shared-memory load per row vector, and
-// the per-thread index and barrier work spread over twice the updates).
+// the per-thread index and barrier work spread over twice the updates); ZC:
+// the 7-point consumer keeps planes z-1 and z in registers along the z-march.
 template <typename S, typename C, int TX_, int TY_, int NS_, bool XHALO_ = true, bool MASK_ = false,
-          int MINB_ = 1, int VEC_ = kVec>
+          int MINB_ = 1, int VEC_ = kVec, bool ZC_ = false>
 struct Layout {
   static constexpr int TX = TX_, TY = TY_, NS = NS_, MINB = MINB_, VEC = VEC_;
+  static constexpr bool ZC = ZC_;
   static_assert(VEC == 4 || (VEC == 8 && sizeof(S) == 2), "8-element vectors: 16-bit fields");
   // With XHALO the box carries a 16-byte x halo on both sides; without it the
   // box is exactly TX wide (up to 256) and the threads at the tile's x edges
@@ -482,7 +484,218 @@ k_update_tma(const __grid_constant__ CUtensorMap map_cur, const __grid_constant_
                                        g0 + XY, x, X, no_mask, cc0, cc0, cc1, cc2);
     }
   }
-  for (int j = 0; j < nplanes && ok; ++j) {
+  // The 7-point update of the thread's VEC elements of plane z = z0 + j from
+  // the values of planes z-1 (fm), z (fc) and z+1 (fn) and the stage of
+  // plane z (rows y -+ 1, the x neighbours, P^{n-1}, class ids).
+  using Vec = Vn<S, VEC>;
+  auto srl_update = [&](int j, const A (&fm)[VEC], const A (&fc)[VEC], const A (&fn)[VEC]) {
+      const int sc_ = (j + 1) % NS, sp_ = (j + 2) % NS;
+      const S* Pc = (const S*)(smem + sc_ * Lay::STAGE + Lay::P_OFF);
+      const S* Pq = (const S*)(smem + sp_ * Lay::STAGE + Lay::PP_OFF);
+      const C* Cl = (const C*)(smem + sp_ * Lay::STAGE + Lay::CL_OFF);
+      const int z = z0 + j;
+      const int64_t idx = (int64_t)z * XY + (int64_t)y * X + x;
+      const Vec vym = ldsv<VEC>(Pc + si - PW);
+      const Vec vyp = ldsv<VEC>(Pc + si + PW);
+      const Vec vpp = ldsv<VEC>(Pq + ly * kTX + lx);
+      A left = (A)0, right = (A)0;
+      Vec vxm, vxp;
+      unsigned cid[VEC];
+      if (BATCHED) {
+        const int kk = 1 << kshift;
+        vxm = lx >= kk ? ldsv<VEC>(Pc + si - kk) : ldgv<VEC>(P + idx - kk);
+        // the last node of a row reads its flat-index neighbour (the next
+        // row's first node) from global memory, also in a partly filled tile
+        vxp = (lx + kk < kTX && x + kk < X) ? ldsv<VEC>(Pc + si + kk) : ldgv<VEC>(P + idx + kk);
+        const unsigned c = Cl[ly * (kTX >> kshift) + (lx >> kshift)];
+#pragma unroll
+        for (int e = 0; e < VEC; ++e) cid[e] = c;
+      } else {
+        if (x == 0 || (!Lay::XHALO && lx == 0)) left = St::load(P[idx - 1]);
+        else left = St::load(Pc[si - 1]);
+        if (x + VEC == X || (!Lay::XHALO && lx + VEC == kTX)) right = St::load(P[idx + VEC]);
+        else right = St::load(Pc[si + VEC]);
+      }
+      if (BATCHED) {
+      } else if (sizeof(C) * VEC == 4) {
+        const uint32_t w = *reinterpret_cast<const uint32_t*>(Cl + ly * kTX + lx);
+#pragma unroll
+        for (int e = 0; e < 4; ++e) cid[e] = (w >> (8 * e)) & 0xFFu;
+      } else if (sizeof(C) * VEC == 8) {
+        const uint2 w = *reinterpret_cast<const uint2*>(Cl + ly * kTX + lx);
+        const uint32_t ws[2] = {w.x, w.y};
+#pragma unroll
+        for (int e = 0; e < VEC; ++e)
+          cid[e] = sizeof(C) == 1 ? (ws[e >> 2] >> (8 * (e & 3))) & 0xFFu
+                                  : (ws[e >> 1] >> (16 * (e & 1))) & 0xFFFFu;
+      } else {
+        const uint4 w = *reinterpret_cast<const uint4*>(Cl + ly * kTX + lx);
+        const uint32_t ws[4] = {w.x, w.y, w.z, w.w};
+#pragma unroll
+        for (int e = 0; e < VEC; ++e) cid[e] = (ws[e >> 1] >> (16 * (e & 1))) & 0xFFFFu;
+      }
+      if constexpr ((SCHEME == 0 || SCHEME == 4) && sizeof(A) == 4) {
+        // Forward update of the thread's elements as packed pairs: the same
+        // operations and rounding as the scalar loop below, with every
+        // product formed as fma(x, y, -0) so that none is contracted.
+        // Batched: the pairs are fields of one node (one class); otherwise
+        // adjacent x nodes (a class each).
+        using namespace px;
+        constexpr int NP = VEC / 2;
+        auto coef = [&](int e) -> PackedCoef<A> {
+          if (kSmemTab) return stab[cid[e]];
+          return PackedCoef<A>{__ldg(tab.a + cid[e]), __ldg(tab.b + cid[e]),
+                               __ldg(tab.c + cid[e]), __ldg(tab.pos + cid[e])};
+        };
+        const f2 l22 = pk2(l2, l2), nz = pk2(nzf, nzf);
+        auto pr = [](const Vec& v, int h) -> f2 {
+          return pk2(St::load(v.v[2 * h]), St::load(v.v[2 * h + 1]));
+        };
+        f2 aa[NP], bb[NP], cc[NP], ee[NP], xm2[NP], xp2[NP];
+        if constexpr (BATCHED) {
+          const PackedCoef<A> k = coef(0);
+#pragma unroll
+          for (int h = 0; h < NP; ++h) {
+            aa[h] = pk2(k.a, k.a);
+            bb[h] = pk2(k.b, k.b);
+            cc[h] = pk2(k.c, k.c);
+            ee[h] = pk2(__uint_as_float(k.pos), __uint_as_float(k.pos));
+            xm2[h] = pr(vxm, h);
+            xp2[h] = pr(vxp, h);
+          }
+        } else {
+#pragma unroll
+          for (int h = 0; h < NP; ++h) {
+            const PackedCoef<A> k0 = coef(2 * h), k1 = coef(2 * h + 1);
+            aa[h] = pk2(k0.a, k1.a);
+            bb[h] = pk2(k0.b, k1.b);
+            cc[h] = pk2(k0.c, k1.c);
+            ee[h] = pk2(__uint_as_float(k0.pos), __uint_as_float(k1.pos));
+            // node e reads x[e-1] and x[e+1]; x[-1] = left, x[VEC] = right
+            xm2[h] = pk2(h == 0 ? left : fc[2 * h - 1], fc[2 * h]);
+            xp2[h] = pk2(fc[2 * h + 1], h == NP - 1 ? right : fc[2 * h + 2]);
+          }
+        }
+        S res[VEC];
+#pragma unroll
+        for (int h = 0; h < NP; ++h) {
+          const f2 pc2 = pk2(fc[2 * h], fc[2 * h + 1]);
+          const f2 s6 = add2(add2(add2(add2(add2(pk2(fn[2 * h], fn[2 * h + 1]),
+                                                 pk2(fm[2 * h], fm[2 * h + 1])),
+                                            pr(vyp, h)),
+                                       pr(vym, h)),
+                                  xp2[h]),
+                             xm2[h]);
+          f2 o;
+          if constexpr (SCHEME == 4) {
+            // difference form: a (((1+beta) p + (1-beta)(p - pp)) + l2 (S - K p))
+            o = mul2(aa[h], add2(add2(fma2(ee[h], pc2, nz), fma2(cc[h], sub2(pc2, pr(vpp, h)), nz)),
+                                 fma2(l22, sub2(s6, fma2(bb[h], pc2, nz)), nz)));
+          } else {
+            o = mul2(aa[h], sub2(add2(fma2(bb[h], pc2, nz), fma2(l22, s6, nz)),
+                                 fma2(cc[h], pr(vpp, h), nz)));
+          }
+          float lo, hi;
+          up2(o, lo, hi);
+          if constexpr (sizeof(S) == 4) {
+            res[2 * h] = lo;
+            res[2 * h + 1] = hi;
+          } else if constexpr (std::is_same<S, __half>::value) {
+            const __half2 t = __floats2half2_rn(lo, hi);  // each half rounded to nearest even
+            res[2 * h] = __low2half(t);
+            res[2 * h + 1] = __high2half(t);
+          } else {
+            const __nv_bfloat162 t = __floats2bfloat162_rn(lo, hi);
+            res[2 * h] = __low2bfloat16(t);
+            res[2 * h + 1] = __high2bfloat16(t);
+          }
+        }
+        stgv<VEC>(Pp + idx, res);
+      } else {
+      S res[VEC];
+#pragma unroll
+      for (int e = 0; e < VEC; ++e) {
+        const A pc = fc[e];
+        A xm, xp;
+        if (BATCHED) {
+          xm = St::load(vxm.v[e]);
+          xp = St::load(vxp.v[e]);
+        } else {
+          xm = e == 0 ? left : fc[e - 1];
+          xp = e == VEC - 1 ? right : fc[e + 1];
+        }
+        const A ym = St::load(vym.v[e]), yp = St::load(vyp.v[e]);
+        const A pm = fm[e], pn = fn[e];
+        const A pp = St::load(vpp.v[e]);
+        PackedCoef<A> k;
+        if (kSmemTab) {
+          k = stab[cid[e]];
+        } else {
+          k = PackedCoef<A>{__ldg(tab.a + cid[e]), __ldg(tab.b + cid[e]), __ldg(tab.c + cid[e]),
+                            __ldg(tab.pos + cid[e])};
+        }
+        A out;
+        if (SCHEME == 0 || SCHEME == 4) {
+          const A s6 = R::add(R::add(R::add(R::add(R::add(pn, pm), yp), ym), xp), xm);
+          if (SCHEME == 4 && sizeof(A) == 4) {
+            const A e = (A)__uint_as_float(k.pos);
+            out = R::mul(k.a, R::add(R::add(R::mul(e, pc), R::mul(k.c, R::sub(pc, pp))),
+                                     R::mul(l2, R::sub(s6, R::mul(k.b, pc)))));
+          } else {
+            out = R::mul(k.a, R::sub(R::add(R::mul(k.b, pc), R::mul(l2, s6)), R::mul(k.c, pp)));
+          }
+        } else {
+          const uint32_t cp = k.pos;
+          const A dx = (A)(cp & 1u), dy = (A)((cp >> 1) & 1u), dz = (A)((cp >> 2) & 1u);
+          const A bx = (cp & 0x10u) ? xp : xm;
+          const A by = (cp & 0x20u) ? yp : ym;
+          const A bz = (cp & 0x40u) ? pm : pn;
+          const A sb6 = R::add(R::add(R::mul(bx, dx), R::mul(by, dy)), R::mul(bz, dz));
+          const A s7 = R::add(R::add(R::add(R::add(R::add(R::add(xm, xp), ym), yp), pn), pm), sb6);
+          out = R::mul(k.a, R::add(R::sub(R::mul(s7, l2), R::mul(k.b, pc)), R::mul(k.c, pp)));
+        }
+        res[e] = St::store(out);
+      }
+      stgv<VEC>(Pp + idx, res);
+      }
+  };
+  // One plane's elements of the thread, from stage st.
+  auto load_plane = [&](int st, A (&f)[VEC]) {
+    const Vec v = ldsv<VEC>((const S*)(smem + st * Lay::STAGE + Lay::P_OFF) + si);
+#pragma unroll
+    for (int e = 0; e < VEC; ++e) f[e] = St::load(v.v[e]);
+  };
+  if constexpr (Lay::ZC) {
+    // The 7-point update with the thread's values of planes z-1 and z kept
+    // in registers from the two planes before: each plane is loaded and
+    // converted once, for three updates.  Three planes per trip, the arrays'
+    // roles rotating, so that no value is copied.
+    static_assert(SCHEME != 3, "the IWB consumer carries its own sums");
+    A F0[VEC], F1[VEC], F2[VEC];
+    if (ok && active) {
+      load_plane(0, F0);
+      load_plane(1, F1);
+    }
+    auto step = [&](int j, A (&fm)[VEC], A (&fc)[VEC], A (&fn)[VEC]) -> bool {
+      const int sm = j % NS, sp_ = (j + 2) % NS;
+      if (!mbar_wait(bar_full + 8 * sp_, (uint32_t)(((j + 2) / NS) & 1), wait_ns)) return false;
+      if (active) {
+        load_plane(sp_, fn);
+        srl_update(j, fm, fc, fn);
+      }
+      __syncwarp();
+      if (lane == 0) mbar_arrive(bar_empty + 8 * sm);
+      return true;
+    };
+    for (int j = 0; j < nplanes && ok; j += 3) {
+      ok = step(j, F0, F1, F2);
+      if (!ok || j + 1 >= nplanes) break;
+      ok = step(j + 1, F1, F2, F0);
+      if (!ok || j + 2 >= nplanes) break;
+      ok = step(j + 2, F2, F0, F1);
+    }
+  }
+  for (int j = 0; j < nplanes && ok && !Lay::ZC; ++j) {
     const int sm = j % NS, sc_ = (j + 1) % NS, sp_ = (j + 2) % NS;
     if (!mbar_wait(bar_full + 8 * sp_, (uint32_t)(((j + 2) / NS) & 1), wait_ns)) {
       ok = false;
@@ -577,179 +790,11 @@ k_update_tma(const __grid_constant__ CUtensorMap map_cur, const __grid_constant_
         }
       }
     } else if (active) {
-      using Vec = Vn<S, VEC>;
-      const S* Pm = (const S*)(smem + sm * Lay::STAGE + Lay::P_OFF);
-      const S* Pc = (const S*)(smem + sc_ * Lay::STAGE + Lay::P_OFF);
-      const S* Pn = (const S*)(smem + sp_ * Lay::STAGE + Lay::P_OFF);
-      const S* Pq = (const S*)(smem + sp_ * Lay::STAGE + Lay::PP_OFF);
-      const C* Cl = (const C*)(smem + sp_ * Lay::STAGE + Lay::CL_OFF);
-      const int z = z0 + j;
-      const int64_t idx = (int64_t)z * XY + (int64_t)y * X + x;
-      const Vec vc = ldsv<VEC>(Pc + si);
-      const Vec vym = ldsv<VEC>(Pc + si - PW);
-      const Vec vyp = ldsv<VEC>(Pc + si + PW);
-      const Vec vzm = ldsv<VEC>(Pm + si);
-      const Vec vzp = ldsv<VEC>(Pn + si);
-      const Vec vpp = ldsv<VEC>(Pq + ly * kTX + lx);
-      A left = (A)0, right = (A)0;
-      Vec vxm, vxp;
-      unsigned cid[VEC];
-      if (BATCHED) {
-        const int kk = 1 << kshift;
-        vxm = lx >= kk ? ldsv<VEC>(Pc + si - kk) : ldgv<VEC>(P + idx - kk);
-        // the last node of a row reads its flat-index neighbour (the next
-        // row's first node) from global memory, also in a partly filled tile
-        vxp = (lx + kk < kTX && x + kk < X) ? ldsv<VEC>(Pc + si + kk) : ldgv<VEC>(P + idx + kk);
-        const unsigned c = Cl[ly * (kTX >> kshift) + (lx >> kshift)];
-#pragma unroll
-        for (int e = 0; e < VEC; ++e) cid[e] = c;
-      } else {
-        if (x == 0 || (!Lay::XHALO && lx == 0)) left = St::load(P[idx - 1]);
-        else left = St::load(Pc[si - 1]);
-        if (x + VEC == X || (!Lay::XHALO && lx + VEC == kTX)) right = St::load(P[idx + VEC]);
-        else right = St::load(Pc[si + VEC]);
-      }
-      if (BATCHED) {
-      } else if (sizeof(C) * VEC == 4) {
-        const uint32_t w = *reinterpret_cast<const uint32_t*>(Cl + ly * kTX + lx);
-#pragma unroll
-        for (int e = 0; e < 4; ++e) cid[e] = (w >> (8 * e)) & 0xFFu;
-      } else if (sizeof(C) * VEC == 8) {
-        const uint2 w = *reinterpret_cast<const uint2*>(Cl + ly * kTX + lx);
-        const uint32_t ws[2] = {w.x, w.y};
-#pragma unroll
-        for (int e = 0; e < VEC; ++e)
-          cid[e] = sizeof(C) == 1 ? (ws[e >> 2] >> (8 * (e & 3))) & 0xFFu
-                                  : (ws[e >> 1] >> (16 * (e & 1))) & 0xFFFFu;
-      } else {
-        const uint4 w = *reinterpret_cast<const uint4*>(Cl + ly * kTX + lx);
-        const uint32_t ws[4] = {w.x, w.y, w.z, w.w};
-#pragma unroll
-        for (int e = 0; e < VEC; ++e) cid[e] = (ws[e >> 1] >> (16 * (e & 1))) & 0xFFFFu;
-      }
-      if constexpr ((SCHEME == 0 || SCHEME == 4) && sizeof(A) == 4) {
-        // Forward update of the thread's elements as packed pairs: the same
-        // operations and rounding as the scalar loop below, with every
-        // product formed as fma(x, y, -0) so that none is contracted.
-        // Batched: the pairs are fields of one node (one class); otherwise
-        // adjacent x nodes (a class each).
-        using namespace px;
-        constexpr int NP = VEC / 2;
-        auto coef = [&](int e) -> PackedCoef<A> {
-          if (kSmemTab) return stab[cid[e]];
-          return PackedCoef<A>{__ldg(tab.a + cid[e]), __ldg(tab.b + cid[e]),
-                               __ldg(tab.c + cid[e]), __ldg(tab.pos + cid[e])};
-        };
-        const f2 l22 = pk2(l2, l2), nz = pk2(nzf, nzf);
-        auto pr = [](const Vec& v, int h) -> f2 {
-          return pk2(St::load(v.v[2 * h]), St::load(v.v[2 * h + 1]));
-        };
-        f2 aa[NP], bb[NP], cc[NP], ee[NP], xm2[NP], xp2[NP];
-        if constexpr (BATCHED) {
-          const PackedCoef<A> k = coef(0);
-#pragma unroll
-          for (int h = 0; h < NP; ++h) {
-            aa[h] = pk2(k.a, k.a);
-            bb[h] = pk2(k.b, k.b);
-            cc[h] = pk2(k.c, k.c);
-            ee[h] = pk2(__uint_as_float(k.pos), __uint_as_float(k.pos));
-            xm2[h] = pr(vxm, h);
-            xp2[h] = pr(vxp, h);
-          }
-        } else {
-          A cv[VEC];
-#pragma unroll
-          for (int e = 0; e < VEC; ++e) cv[e] = St::load(vc.v[e]);
-#pragma unroll
-          for (int h = 0; h < NP; ++h) {
-            const PackedCoef<A> k0 = coef(2 * h), k1 = coef(2 * h + 1);
-            aa[h] = pk2(k0.a, k1.a);
-            bb[h] = pk2(k0.b, k1.b);
-            cc[h] = pk2(k0.c, k1.c);
-            ee[h] = pk2(__uint_as_float(k0.pos), __uint_as_float(k1.pos));
-            // node e reads x[e-1] and x[e+1]; x[-1] = left, x[VEC] = right
-            xm2[h] = pk2(h == 0 ? left : cv[2 * h - 1], cv[2 * h]);
-            xp2[h] = pk2(cv[2 * h + 1], h == NP - 1 ? right : cv[2 * h + 2]);
-          }
-        }
-        S res[VEC];
-#pragma unroll
-        for (int h = 0; h < NP; ++h) {
-          const f2 s6 = add2(add2(add2(add2(add2(pr(vzp, h), pr(vzm, h)), pr(vyp, h)),
-                                      pr(vym, h)), xp2[h]), xm2[h]);
-          f2 o;
-          if constexpr (SCHEME == 4) {
-            // difference form: a (((1+beta) p + (1-beta)(p - pp)) + l2 (S - K p))
-            const f2 pc2 = pr(vc, h);
-            o = mul2(aa[h], add2(add2(fma2(ee[h], pc2, nz), fma2(cc[h], sub2(pc2, pr(vpp, h)), nz)),
-                                 fma2(l22, sub2(s6, fma2(bb[h], pc2, nz)), nz)));
-          } else {
-            o = mul2(aa[h], sub2(add2(fma2(bb[h], pr(vc, h), nz), fma2(l22, s6, nz)),
-                                 fma2(cc[h], pr(vpp, h), nz)));
-          }
-          float lo, hi;
-          up2(o, lo, hi);
-          if constexpr (sizeof(S) == 4) {
-            res[2 * h] = lo;
-            res[2 * h + 1] = hi;
-          } else if constexpr (std::is_same<S, __half>::value) {
-            const __half2 t = __floats2half2_rn(lo, hi);  // each half rounded to nearest even
-            res[2 * h] = __low2half(t);
-            res[2 * h + 1] = __high2half(t);
-          } else {
-            const __nv_bfloat162 t = __floats2bfloat162_rn(lo, hi);
-            res[2 * h] = __low2bfloat16(t);
-            res[2 * h + 1] = __high2bfloat16(t);
-          }
-        }
-        stgv<VEC>(Pp + idx, res);
-      } else {
-      S res[VEC];
-#pragma unroll
-      for (int e = 0; e < VEC; ++e) {
-        const A pc = St::load(vc.v[e]);
-        A xm, xp;
-        if (BATCHED) {
-          xm = St::load(vxm.v[e]);
-          xp = St::load(vxp.v[e]);
-        } else {
-          xm = e == 0 ? left : St::load(vc.v[e - 1]);
-          xp = e == VEC - 1 ? right : St::load(vc.v[e + 1]);
-        }
-        const A ym = St::load(vym.v[e]), yp = St::load(vyp.v[e]);
-        const A pm = St::load(vzm.v[e]), pn = St::load(vzp.v[e]);
-        const A pp = St::load(vpp.v[e]);
-        PackedCoef<A> k;
-        if (kSmemTab) {
-          k = stab[cid[e]];
-        } else {
-          k = PackedCoef<A>{__ldg(tab.a + cid[e]), __ldg(tab.b + cid[e]), __ldg(tab.c + cid[e]),
-                            __ldg(tab.pos + cid[e])};
-        }
-        A out;
-        if (SCHEME == 0 || SCHEME == 4) {
-          const A s6 = R::add(R::add(R::add(R::add(R::add(pn, pm), yp), ym), xp), xm);
-          if (SCHEME == 4 && sizeof(A) == 4) {
-            const A e = (A)__uint_as_float(k.pos);
-            out = R::mul(k.a, R::add(R::add(R::mul(e, pc), R::mul(k.c, R::sub(pc, pp))),
-                                     R::mul(l2, R::sub(s6, R::mul(k.b, pc)))));
-          } else {
-            out = R::mul(k.a, R::sub(R::add(R::mul(k.b, pc), R::mul(l2, s6)), R::mul(k.c, pp)));
-          }
-        } else {
-          const uint32_t cp = k.pos;
-          const A dx = (A)(cp & 1u), dy = (A)((cp >> 1) & 1u), dz = (A)((cp >> 2) & 1u);
-          const A bx = (cp & 0x10u) ? xp : xm;
-          const A by = (cp & 0x20u) ? yp : ym;
-          const A bz = (cp & 0x40u) ? pm : pn;
-          const A sb6 = R::add(R::add(R::mul(bx, dx), R::mul(by, dy)), R::mul(bz, dz));
-          const A s7 = R::add(R::add(R::add(R::add(R::add(R::add(xm, xp), ym), yp), pn), pm), sb6);
-          out = R::mul(k.a, R::add(R::sub(R::mul(s7, l2), R::mul(k.b, pc)), R::mul(k.c, pp)));
-        }
-        res[e] = St::store(out);
-      }
-      stgv<VEC>(Pp + idx, res);
-      }
+      A fm[VEC], fc[VEC], fn[VEC];
+      load_plane(sm, fm);
+      load_plane(sc_, fc);
+      load_plane(sp_, fn);
+      srl_update(j, fm, fc, fn);
     }
     __syncwarp();
     if (lane == 0) mbar_arrive(bar_empty + 8 * sm);
@@ -970,11 +1015,15 @@ int launch_tma_s<float>(pfdtd_domain* d, const void* cur, void* past, cudaStream
 // 16-bit storage tiles (id, TX, TY, stages, x halo in the box, CTAs per SM,
 // elements per thread): 0 64x16 (halo in box), 1 128x8, 2 256x8, 3 256x4, with
 // 4 elements per thread; 4 256x8, 5 256x8 (6 stages, three CTAs per SM),
-// 6 256x4 (four CTAs), 7 128x8 with 8 elements per thread.
+// 6 256x4 (four CTAs), 7 128x8 with 8 elements per thread; 8 256x8 and
+// 9 256x4 (four CTAs) with 8 elements per thread and planes z-1, z carried
+// in registers.
 #define PFDTD_F16_TILES(X)                                                                    \
-  X(0, 64, 16, 8, true, 2, 4) X(1, 128, 8, 8, false, 2, 4) X(2, 256, 8, 8, false, 2, 4)         \
-  X(3, 256, 4, 8, false, 2, 4) X(4, 256, 8, 8, false, 2, 8) X(5, 256, 8, 6, false, 3, 8)       \
-  X(6, 256, 4, 8, false, 4, 8) X(7, 128, 8, 8, false, 2, 8)
+  X(0, 64, 16, 8, true, 2, 4, false) X(1, 128, 8, 8, false, 2, 4, false)                       \
+  X(2, 256, 8, 8, false, 2, 4, false) X(3, 256, 4, 8, false, 2, 4, false)                      \
+  X(4, 256, 8, 8, false, 2, 8, false) X(5, 256, 8, 6, false, 3, 8, false)                      \
+  X(6, 256, 4, 8, false, 4, 8, false) X(7, 128, 8, 8, false, 2, 8, false)                      \
+  X(8, 256, 8, 8, false, 2, 8, true) X(9, 256, 4, 8, false, 4, 8, true)
 
 int auto_tile16(const pfdtd_domain* d) {
   if (d->X % 256 == 0) return 2;
@@ -991,13 +1040,17 @@ int launch_tma_16(pfdtd_domain* d, const void* cur, void* past, cudaStream_t s) 
     // batched tiles: default 256 x 8 elements, 8 stages, two CTAs per SM;
     // 1 = 256 x 4, 8 stages, four CTAs; 2 = 256 x 8, 6 stages, two CTAs;
     // with 8 elements (fields of one node) per thread, for K a multiple of 8:
-    // 3 = 256 x 8, 8 stages, two CTAs; 4 = 256 x 4, 8 stages, four CTAs
+    // 3 = 256 x 8, 8 stages, two CTAs; 4 = 256 x 4, 8 stages, four CTAs;
+    // 5 = as 3 with planes z-1, z carried in registers
     if (d->K % 8 == 0 && d->tma_tile == 3)
       return launch_tma_batched<S, Layout<S, uint8_t, 256, 8, 8, false, false, 2, 8>,
                                 Layout<S, uint16_t, 256, 8, 8, false, false, 2, 8>>(d, cur, past, s);
     if (d->K % 8 == 0 && d->tma_tile == 4)
       return launch_tma_batched<S, Layout<S, uint8_t, 256, 4, 8, false, false, 4, 8>,
                                 Layout<S, uint16_t, 256, 4, 8, false, false, 4, 8>>(d, cur, past, s);
+    if (d->K % 8 == 0 && d->tma_tile == 5)
+      return launch_tma_batched<S, Layout<S, uint8_t, 256, 8, 8, false, false, 2, 8, true>,
+                                Layout<S, uint16_t, 256, 8, 8, false, false, 2, 8, true>>(d, cur, past, s);
     if (d->tma_tile == 1)
       return launch_tma_batched<S, Layout<S, uint8_t, 256, 4, 8, false, false, 4>,
                                 Layout<S, uint16_t, 256, 4, 8, false, false, 4>>(d, cur, past, s);
@@ -1007,15 +1060,15 @@ int launch_tma_16(pfdtd_domain* d, const void* cur, void* past, cudaStream_t s) 
     return launch_tma_batched<S, Layout<S, uint8_t, 256, 8, 8, false, false, 2>,
                               Layout<S, uint16_t, 256, 8, 8, false, false, 2>>(d, cur, past, s);
   }
-  switch (d->tma_tile < 0 || d->tma_tile > 7 ? auto_tile16(d) : d->tma_tile) {
-#define PFDTD_CASE16(id, tx, ty, ns, xh, minb, vec)                                       \
+  switch (d->tma_tile < 0 || d->tma_tile > 9 ? auto_tile16(d) : d->tma_tile) {
+#define PFDTD_CASE16(id, tx, ty, ns, xh, minb, vec, zc)                                   \
   case id:                                                                                \
-    return launch_tma_l<S, Layout<S, uint8_t, tx, ty, ns, xh, false, minb, vec>,           \
-                        Layout<S, uint16_t, tx, ty, ns, xh, false, minb, vec>>(d, cur, past, s);
+    return launch_tma_l<S, Layout<S, uint8_t, tx, ty, ns, xh, false, minb, vec, zc>,       \
+                        Layout<S, uint16_t, tx, ty, ns, xh, false, minb, vec, zc>>(d, cur, past, s);
     PFDTD_F16_TILES(PFDTD_CASE16)
 #undef PFDTD_CASE16
   }
-  return fail(PFDTD_ERR_ARG, "unknown TMA tile shape for 16-bit fields (0..7)");
+  return fail(PFDTD_ERR_ARG, "unknown TMA tile shape for 16-bit fields (0..9)");
 }
 
 template <>

@@ -433,22 +433,24 @@ def test_tma_tile_shapes_bit_identical(gpu, O, tile, centred, wide):
     assert np.array_equal(P, rP)
 
 
-@pytest.mark.parametrize("tile", list(range(8)))
+@pytest.mark.parametrize("tile", list(range(10)))
 @pytest.mark.parametrize("prec", ["f16", "bf16"])
 @pytest.mark.parametrize("centred,wide", [(False, False), (True, False), (False, True),
                                           (True, True)])
 def test_16bit_tile_shapes_bit_identical(gpu, O, tile, prec, centred, wide):
-    """Every 16-bit tile shape (4 and 8 elements per thread), forward and
-    centred, with 8-bit class ids and (wide: materials drawn per voxel, more
-    than 256 node classes) 16-bit class ids; X = 208 leaves partly filled
-    tiles.  Bit-identical to the oracle with the same storage rounding."""
+    """Every 16-bit tile shape (4 and 8 elements per thread, planes carried
+    in registers or reloaded), forward and centred, with 8-bit class ids and
+    (wide: materials drawn per voxel, more than 256 node classes) 16-bit
+    class ids; X = 208 leaves partly filled tiles, Z = 40 a z-chunk whose
+    plane count is not a multiple of three.  Bit-identical to the oracle with
+    the same storage rounding."""
     room = rooms.boxes_room((208, 52, 40), n_boxes=6, edge=(5, 16), n_materials=150 if wide else 9,
                             seed=16)
     if wide:
         room.mat[...] = np.random.default_rng(5).integers(0, 150, room.mat.shape, dtype=np.uint8)
     steps = 60
     src = room.random_air_nodes(1, seed=3)
-    rec = room.random_air_nodes(4, seed=4)
+    rec = [src[0]] + room.random_air_nodes(3, seed=4)  # the source node sees the pulse
     pulse = rooms.gaussian_pulse(steps, 3.0)
     pos, mat = O.encode_nodes(room.bid, room.mat, centred)
     X, Y, Z = room.dims
@@ -991,13 +993,14 @@ def test_batched_partly_filled_tiles(gpu, O, fields, prec):
         assert np.array_equal(g[f], r[0]), f"field {f}"
 
 
-@pytest.mark.parametrize("tile", [1, 2, 3, 4])
+@pytest.mark.parametrize("tile", [1, 2, 3, 4, 5])
 @pytest.mark.parametrize("fields,prec", [(16, "f16"), (8, "bf16"), (4, "f16")])
 @pytest.mark.parametrize("centred", [False, True])
 def test_batched_16bit_tile_shapes(gpu, O, monkeypatch, tile, fields, prec, centred):
     """The batched 16-bit tile shapes (1: 256 x 4 elements, four CTAs per SM;
-    2: 256 x 8, six stages; 3 and 4: 8 fields per thread, K a multiple of 8,
-    else the default shape) equal an oracle run of each field alone."""
+    2: 256 x 8, six stages; 3 and 4: 8 fields per thread, 5: the same with
+    planes carried in registers, for K a multiple of 8, else the default
+    shape) equal an oracle run of each field alone."""
     monkeypatch.setenv("PFDTD_TMA_TILE", str(tile))
     room = rooms.boxes_room((64, 48, 40), n_boxes=5, edge=(5, 14), n_materials=6, seed=45)
     steps = 90
