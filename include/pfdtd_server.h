@@ -66,10 +66,7 @@ int pfdtd_request_bytes(const pfdtd_request* r, uint64_t* bytes);
 int pfdtd_request_destroy(pfdtd_request* r);
 
 /* Server on `device` admitting requests while their summed estimated bytes
- * stay within hbm_budget and at most max_active run at once.  It sets the
- * release threshold of the device's default memory pool (process-wide) to
- * hbm_budget, so that memory freed by a finished request stays mapped for
- * the next one instead of returning to the system at each synchronisation. */
+ * stay within hbm_budget and at most max_active run at once. */
 int pfdtd_server_create(int device, uint64_t hbm_budget, int max_active, pfdtd_server** out);
 /* Queue a request; the server takes ownership of it (do not destroy it).
  * A request larger than the whole budget fails at once (PFDTD_ERR_NOMEM). */

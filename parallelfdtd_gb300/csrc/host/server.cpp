@@ -26,8 +26,6 @@
 #include <thread>
 #include <vector>
 
-#include <cuda_runtime.h>
-
 #include "pfdtd.h"
 #include "pfdtd_server.h"
 
@@ -466,23 +464,6 @@ int pfdtd_server_create(int device, uint64_t hbm_budget, int max_active, pfdtd_s
   int n = 0;
   if (int rc = pfdtd_device_count(&n)) return rc;
   if (device < 0 || device >= n) return fail(PFDTD_ERR_ARG, "device index out of range");
-  // Domains allocate from the device's default stream-ordered pool.  Its
-  // release threshold (0 by default) returns freed memory to the system at
-  // every synchronisation, so each request would map its gigabytes afresh
-  // and the retirement of another unmap them; up to the budget, freed memory
-  // stays in the pool for the next request instead.
-  {
-    int prev = 0;
-    cudaMemPool_t pool = nullptr;
-    if (cudaGetDevice(&prev) == cudaSuccess && cudaSetDevice(device) == cudaSuccess) {
-      if (cudaDeviceGetDefaultMemPool(&pool, device) == cudaSuccess) {
-        uint64_t keep = hbm_budget;
-        cudaMemPoolSetAttribute(pool, cudaMemPoolAttrReleaseThreshold, &keep);
-      }
-      cudaSetDevice(prev);
-    }
-    cudaGetLastError();
-  }
   pfdtd_server* s = new pfdtd_server();
   s->device = device;
   s->budget = hbm_budget;

@@ -1015,19 +1015,22 @@ int launch_tma_s<float>(pfdtd_domain* d, const void* cur, void* past, cudaStream
 // 16-bit storage tiles (id, TX, TY, stages, x halo in the box, CTAs per SM,
 // elements per thread): 0 64x16 (halo in box), 1 128x8, 2 256x8, 3 256x4, with
 // 4 elements per thread; 4 256x8, 5 256x8 (6 stages, three CTAs per SM),
-// 6 256x4 (four CTAs), 7 128x8 with 8 elements per thread; 8 256x8 and
-// 9 256x4 (four CTAs) with 8 elements per thread and planes z-1, z carried
-// in registers.
+// 6 256x4 (four CTAs), 7 128x8 with 8 elements per thread; 8 256x8,
+// 9 256x4 (four CTAs) and 10 128x8 with 8 elements per thread and planes
+// z-1, z carried in registers.  Measured on the 512 x 384 x 256 room, FP16
+// (node-updates/s): 2 655 G, 4 753 G, 5 720 G, 6 677 G, 7 699 G, 8 808 G,
+// 9 703 G; BF16: 2 626 G, 4 744 G, 8 777 G, 9 683 G.
 #define PFDTD_F16_TILES(X)                                                                    \
   X(0, 64, 16, 8, true, 2, 4, false) X(1, 128, 8, 8, false, 2, 4, false)                       \
   X(2, 256, 8, 8, false, 2, 4, false) X(3, 256, 4, 8, false, 2, 4, false)                      \
   X(4, 256, 8, 8, false, 2, 8, false) X(5, 256, 8, 6, false, 3, 8, false)                      \
   X(6, 256, 4, 8, false, 4, 8, false) X(7, 128, 8, 8, false, 2, 8, false)                      \
-  X(8, 256, 8, 8, false, 2, 8, true) X(9, 256, 4, 8, false, 4, 8, true)
+  X(8, 256, 8, 8, false, 2, 8, true) X(9, 256, 4, 8, false, 4, 8, true)                       \
+  X(10, 128, 8, 8, false, 2, 8, true)
 
 int auto_tile16(const pfdtd_domain* d) {
-  if (d->X % 256 == 0) return 2;
-  if (d->X % 128 == 0) return 1;
+  if (d->X % 256 == 0) return 8;
+  if (d->X % 128 == 0) return 10;
   return 0;
 }
 
@@ -1037,30 +1040,33 @@ int launch_tma_16(pfdtd_domain* d, const void* cur, void* past, cudaStream_t s) 
   // fields holds half the bytes of the FP32 tile, and one CTA per SM leaves
   // too few loads in flight to stream at HBM speed.
   if (d->K > 1) {
-    // batched tiles: default 256 x 8 elements, 8 stages, two CTAs per SM;
-    // 1 = 256 x 4, 8 stages, four CTAs; 2 = 256 x 8, 6 stages, two CTAs;
-    // with 8 elements (fields of one node) per thread, for K a multiple of 8:
-    // 3 = 256 x 8, 8 stages, two CTAs; 4 = 256 x 4, 8 stages, four CTAs;
-    // 5 = as 3 with planes z-1, z carried in registers
-    if (d->K % 8 == 0 && d->tma_tile == 3)
-      return launch_tma_batched<S, Layout<S, uint8_t, 256, 8, 8, false, false, 2, 8>,
-                                Layout<S, uint16_t, 256, 8, 8, false, false, 2, 8>>(d, cur, past, s);
-    if (d->K % 8 == 0 && d->tma_tile == 4)
-      return launch_tma_batched<S, Layout<S, uint8_t, 256, 4, 8, false, false, 4, 8>,
-                                Layout<S, uint16_t, 256, 4, 8, false, false, 4, 8>>(d, cur, past, s);
-    if (d->K % 8 == 0 && d->tma_tile == 5)
+    // batched tiles: 0 (K not a multiple of 8: the default) 256 x 8
+    // elements, 8 stages, two CTAs per SM; 1 = 256 x 4, 8 stages, four CTAs;
+    // 2 = 256 x 8, 6 stages, two CTAs; with 8 elements (fields of one node)
+    // per thread, for K a multiple of 8: 3 = 256 x 8, 8 stages, two CTAs;
+    // 4 = 256 x 4, 8 stages, four CTAs; 5 (the default) = as 3 with planes
+    // z-1, z carried in registers.  Measured on the 384 x 320 x 256 room,
+    // K = 16, FP16 (field-updates/s): 0 710 G, 3 896 G, 4 900 G, 5 928 G.
+    const int tile = d->tma_tile < 0 || d->tma_tile > 5 ? 5 : d->tma_tile;
+    if (d->K % 8 == 0 && tile == 5)
       return launch_tma_batched<S, Layout<S, uint8_t, 256, 8, 8, false, false, 2, 8, true>,
                                 Layout<S, uint16_t, 256, 8, 8, false, false, 2, 8, true>>(d, cur, past, s);
-    if (d->tma_tile == 1)
+    if (d->K % 8 == 0 && tile == 3)
+      return launch_tma_batched<S, Layout<S, uint8_t, 256, 8, 8, false, false, 2, 8>,
+                                Layout<S, uint16_t, 256, 8, 8, false, false, 2, 8>>(d, cur, past, s);
+    if (d->K % 8 == 0 && tile == 4)
+      return launch_tma_batched<S, Layout<S, uint8_t, 256, 4, 8, false, false, 4, 8>,
+                                Layout<S, uint16_t, 256, 4, 8, false, false, 4, 8>>(d, cur, past, s);
+    if (tile == 1)
       return launch_tma_batched<S, Layout<S, uint8_t, 256, 4, 8, false, false, 4>,
                                 Layout<S, uint16_t, 256, 4, 8, false, false, 4>>(d, cur, past, s);
-    if (d->tma_tile == 2)
+    if (tile == 2)
       return launch_tma_batched<S, Layout<S, uint8_t, 256, 8, 6, false, false, 2>,
                                 Layout<S, uint16_t, 256, 8, 6, false, false, 2>>(d, cur, past, s);
     return launch_tma_batched<S, Layout<S, uint8_t, 256, 8, 8, false, false, 2>,
                               Layout<S, uint16_t, 256, 8, 8, false, false, 2>>(d, cur, past, s);
   }
-  switch (d->tma_tile < 0 || d->tma_tile > 9 ? auto_tile16(d) : d->tma_tile) {
+  switch (d->tma_tile < 0 || d->tma_tile > 10 ? auto_tile16(d) : d->tma_tile) {
 #define PFDTD_CASE16(id, tx, ty, ns, xh, minb, vec, zc)                                   \
   case id:                                                                                \
     return launch_tma_l<S, Layout<S, uint8_t, tx, ty, ns, xh, false, minb, vec, zc>,       \
@@ -1068,7 +1074,7 @@ int launch_tma_16(pfdtd_domain* d, const void* cur, void* past, cudaStream_t s) 
     PFDTD_F16_TILES(PFDTD_CASE16)
 #undef PFDTD_CASE16
   }
-  return fail(PFDTD_ERR_ARG, "unknown TMA tile shape for 16-bit fields (0..9)");
+  return fail(PFDTD_ERR_ARG, "unknown TMA tile shape for 16-bit fields (0..10)");
 }
 
 template <>

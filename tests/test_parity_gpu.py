@@ -433,7 +433,7 @@ def test_tma_tile_shapes_bit_identical(gpu, O, tile, centred, wide):
     assert np.array_equal(P, rP)
 
 
-@pytest.mark.parametrize("tile", list(range(10)))
+@pytest.mark.parametrize("tile", list(range(11)))
 @pytest.mark.parametrize("prec", ["f16", "bf16"])
 @pytest.mark.parametrize("centred,wide", [(False, False), (True, False), (False, True),
                                           (True, True)])
@@ -993,7 +993,7 @@ def test_batched_partly_filled_tiles(gpu, O, fields, prec):
         assert np.array_equal(g[f], r[0]), f"field {f}"
 
 
-@pytest.mark.parametrize("tile", [1, 2, 3, 4, 5])
+@pytest.mark.parametrize("tile", [0, 1, 2, 3, 4, 5])
 @pytest.mark.parametrize("fields,prec", [(16, "f16"), (8, "bf16"), (4, "f16")])
 @pytest.mark.parametrize("centred", [False, True])
 def test_batched_16bit_tile_shapes(gpu, O, monkeypatch, tile, fields, prec, centred):
