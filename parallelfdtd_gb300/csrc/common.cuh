@@ -163,7 +163,7 @@ struct TmaState {
   CUtensorMap tile[4];
   CUtensorMap cls;
   CUtensorMap mask;  // IWB closed-neighbour masks (4 bytes per node)
-  int64_t key[6] = {0, 0, 0, 0, 0, 0};
+  int64_t key[7] = {0, 0, 0, 0, 0, 0, 0};
   bool ready = false;
   bool attr_set[2][2][2] = {{{false, false}, {false, false}}, {{false, false}, {false, false}}};
 };
@@ -222,6 +222,12 @@ struct pfdtd_domain {
   int n_classes = 0;
   int cls_bytes = 1;
   void* d_cls = nullptr;     // per node class id (uint8 or uint16)
+  // The class ids with every row padded to a multiple of 16 bytes, for the
+  // TMA kernels' tensor map when X * cls_bytes is not (cls_pitch: row length
+  // in ids; 0 when the TMA kernels read d_cls itself)
+  void* d_cls_tma = nullptr;
+  size_t cls_tma_bytes = 0;
+  int64_t cls_pitch = 0;
   void* d_ctab = nullptr;    // coefficient arrays (a|b|c in arithmetic type, then pos u32)
   // IWB: per node the closed-neighbour mask (26 bits) and the class code
   // that stands for the position byte in the IWB class key (stencil.cu)

@@ -420,7 +420,7 @@ int pfdtd_destroy(pfdtd_domain* d) {
                   d->d_ctab, d->d_src_idx, d->d_src_mode, d->d_src_samples, d->d_rec_idx,
                   d->d_step, d->d_rec_out, d->d_err, d->d_dif_list, d->d_dif_tab,
                   d->d_dif_state, d->d_iwb_mask, d->d_iwb_code, d->d_iwb_sw,
-                  d->d_iwb_closure, d->d_iwb_closure_dif};
+                  d->d_iwb_closure, d->d_iwb_closure_dif, d->d_cls_tma};
   for (void* p : ptrs)
     d->release(p);
   if (d->stream) cudaStreamDestroy(d->stream);

@@ -88,7 +88,11 @@ int source_fields(const pfdtd_request* r) {
 struct Job {
   pfdtd_request* req = nullptr;
   int state = PFDTD_REQ_QUEUED;
-  pfdtd_domain* dom = nullptr;
+  // The request's domains: one with all its fields, or (an IWB request with
+  // several fields, see split_fields) one single-field domain per field that
+  // carries a source, part_field[i] naming the field of doms[i].
+  std::vector<pfdtd_domain*> doms;
+  std::vector<int> part_field;
   uint64_t bytes = 0;
   Clock::time_point t_submit, t_admit, t_done;
   std::vector<uint8_t> result;
@@ -120,17 +124,21 @@ struct pfdtd_server {
 
 namespace {
 
-// x extent of the domain a request runs on.  The TMA update kernels need the
-// rows of node bytes 16-byte aligned (X a multiple of 16); other rooms run the
-// slower z-march kernel.  A request whose x = X-1 face holds no inside node,
-// and whose sources and receivers lie below X, runs on a domain padded with
-// outside nodes up to the next multiple of 16, as the reference pads its
-// meshes to the block size (cudaMesh.cu:253-304).  No inside node then reads
-// a different neighbour (the padding and the x = X-1 face are outside and
-// stay 0), so the receivers are those of the unpadded room.
+// x extent of the domain a request runs on.  The TMA update kernels need
+// 16-byte aligned field rows (X * fields * element size a multiple of 16);
+// other rooms run the slower z-march kernel.  A request whose rows are not
+// aligned, whose x = X-1 face holds no inside node, and whose sources and
+// receivers lie below X, runs on a domain padded with outside nodes up to the
+// next multiple of 16, as the reference pads its meshes to the block size
+// (cudaMesh.cu:253-304).  No inside node then reads a different neighbour
+// (the padding and the x = X-1 face are outside and stay 0), so the
+// receivers are those of the unpadded room.
+bool split_fields(const pfdtd_request* r);
 int64_t domain_x(const pfdtd_request* r) {
   const int64_t X = r->X, Xp = (X + 15) / 16 * 16;
-  if (Xp == X || !r->nodes_set) return X;
+  const int64_t K = split_fields(r) ? 1 : r->fields;
+  if (Xp == X || (X * K * (int64_t)storage_size(r->precision)) % 16 == 0 || !r->nodes_set)
+    return X;
   for (int i = 0; i < r->n_src; ++i)
     if (r->src_xyz[3 * (size_t)i] >= X) return X;
   for (int i = 0; i < r->n_rec; ++i)
@@ -140,17 +148,26 @@ int64_t domain_x(const pfdtd_request* r) {
   return Xp;
 }
 
-uint64_t estimate_bytes(const pfdtd_request* r) {
+// An IWB request with several fields runs as one single-field domain per
+// field that carries a source: the IWB update has its streaming TMA kernel and
+// closure pass for single-field domains only (batched IWB fields take the
+// column z-march), and every field of a batched domain is bit-identical to
+// the same field run alone, so the receivers do not change.  Fields without
+// a source stay zero and are not run.
+bool split_fields(const pfdtd_request* r) { return r->scheme == PFDTD_IWB && r->fields > 1; }
+
+uint64_t estimate_domain_bytes(const pfdtd_request* r, uint64_t K, int n_src, int n_rec) {
   const uint64_t es = storage_size(r->precision), as = arith_size(r->precision);
   const uint64_t DX = (uint64_t)domain_x(r);
-  const uint64_t N = (uint64_t)(DX * r->Y * r->Z), K = (uint64_t)r->fields;
+  const uint64_t N = (uint64_t)(DX * r->Y * r->Z);
   const uint64_t align = 256 / es;
   const uint64_t margin = ((DX + 64) * K + align - 1) / align * align;
   const uint64_t nfields = r->tb_depth >= 2 ? 4 : 2;
   uint64_t b = nfields * (N * K + 2 * margin) * es;
   b += 2 * (N + 1 + DX) + N + 64;                              // node bytes, class ids
-  b += (uint64_t)r->n_rec * (uint64_t)r->steps * as;         // receiver buffer
-  b += (uint64_t)r->n_src * (uint64_t)r->n_samples * as + 4096;  // sources
+  if (DX % 16 != 0 && (DX * K * es) % 16 == 0) b += 2 * N;  // class ids, 16-byte rows (TMA)
+  b += (uint64_t)n_rec * (uint64_t)r->steps * as;            // receiver buffer
+  b += (uint64_t)n_src * (uint64_t)r->n_samples * as + 4096;  // sources
   bool dif = false;
   for (int32_t f : r->dif_flags) dif |= f != 0;
   if (dif) b += (uint64_t)r->n_boundary * (K * 4 * as + 8);   // filter states + node list
@@ -166,14 +183,79 @@ uint64_t estimate_bytes(const pfdtd_request* r) {
   return b + (4u << 20);                                     // tables, graphs, scratch
 }
 
-// Create and set up the request's domain and queue its run.  Returns the
-// status; on failure the domain is destroyed and the message kept.
+uint64_t estimate_bytes(const pfdtd_request* r) {
+  if (!split_fields(r)) return estimate_domain_bytes(r, (uint64_t)r->fields, r->n_src, r->n_rec);
+  // one single-field domain per source field, each with its own sources and
+  // receivers; the summed source and receiver buffers are those of the request
+  const int parts = source_fields(r);
+  return (uint64_t)parts * estimate_domain_bytes(r, 1, 0, 0) +
+         estimate_domain_bytes(r, 1, r->n_src, r->n_rec) - estimate_domain_bytes(r, 1, 0, 0);
+}
+
+// Create and set up one domain of the request with K fields and the given
+// sources and receivers (indices into the request's), and queue its run.
+// part_field: the request field that a single-field domain runs, its sources
+// and receivers moved to field 0 (-1: every field, numbered as the request
+// numbers them).
+int setup_domain(pfdtd_server* s, const pfdtd_request* r, int K, int part_field,
+                 const std::vector<int>& src_ids, const std::vector<int>& rec_ids,
+                 const std::vector<uint8_t>& ppos, const std::vector<uint8_t>& pmat,
+                 pfdtd_domain** out) {
+  const int64_t DX = domain_x(r);
+  pfdtd_domain* d = nullptr;
+  int rc = pfdtd_create_batched(DX, r->Y, r->Z, K, r->precision, s->device, &d);
+  if (rc) return rc;
+  const size_t as = arith_size(r->precision);
+  const size_t ns = (size_t)r->n_samples;
+  std::vector<uint8_t> samples(src_ids.size() * ns * as);
+  std::vector<int64_t> sxyz, rxyz;
+  std::vector<int32_t> sfield, stype, rfield;
+  for (size_t k = 0; k < src_ids.size(); ++k) {
+    const int i = src_ids[k];
+    for (int c = 0; c < 3; ++c) sxyz.push_back(r->src_xyz[3 * (size_t)i + c]);
+    sfield.push_back(part_field < 0 ? r->src_field[(size_t)i] : 0);
+    stype.push_back(r->src_type[(size_t)i]);
+    const double* v = r->samples.data() + (size_t)i * ns;
+    for (size_t t = 0; t < ns; ++t) {
+      if (as == 8) {
+        std::memcpy(samples.data() + (k * ns + t) * 8, v + t, 8);
+      } else {
+        const float f = (float)v[t];
+        std::memcpy(samples.data() + (k * ns + t) * 4, &f, 4);
+      }
+    }
+  }
+  for (int i : rec_ids) {
+    for (int c = 0; c < 3; ++c) rxyz.push_back(r->rec_xyz[3 * (size_t)i + c]);
+    rfield.push_back(part_field < 0 ? r->rec_field[(size_t)i] : 0);
+  }
+  rc = DX != r->X ? pfdtd_set_nodes(d, ppos.data(), pmat.data(), 0)
+                  : pfdtd_set_nodes(d, r->pos.data(), r->mat.data(), 0);
+  if (!rc) rc = pfdtd_set_scheme(d, r->scheme);
+  if (!rc) rc = pfdtd_set_materials(d, r->materials.data(), r->n_mat, r->n_coef);
+  if (!rc && !r->dif_flags.empty())
+    rc = pfdtd_set_dif_filters(d, (int)r->dif_flags.size(), r->dif_flags.data(),
+                               r->dif_coefs.data());
+  if (!rc) rc = pfdtd_set_params(d, r->params);
+  if (!rc)
+    rc = pfdtd_set_sources_batched(d, (int)src_ids.size(), sxyz.data(), sfield.data(),
+                                   stype.data(), samples.data(), r->n_samples);
+  if (!rc) rc = pfdtd_set_receivers_batched(d, (int)rec_ids.size(), rxyz.data(), rfield.data());
+  if (!rc) rc = pfdtd_set_temporal_block(d, r->tb_depth);
+  if (!rc) rc = pfdtd_run_async(d, r->steps);
+  if (rc) {
+    pfdtd_destroy(d);
+    return rc;
+  }
+  *out = d;
+  return PFDTD_OK;
+}
+
+// Create and set up the request's domains and queue their runs.  Returns the
+// status; on failure every domain is destroyed and the message kept.
 int admit(pfdtd_server* s, Job& j) {
   pfdtd_request* r = j.req;
-  pfdtd_domain* d = nullptr;
   const int64_t DX = domain_x(r);
-  int rc = pfdtd_create_batched(DX, r->Y, r->Z, r->fields, r->precision, s->device, &d);
-  if (rc) return rc;
   std::vector<uint8_t> ppos, pmat;  // node bytes re-laid on the padded rows
   if (DX != r->X) {
     ppos.assign((size_t)(DX * r->Y * r->Z), 0);
@@ -183,47 +265,80 @@ int admit(pfdtd_server* s, Job& j) {
       std::memcpy(&pmat[(size_t)(row * DX)], &r->mat[(size_t)(row * r->X)], (size_t)r->X);
     }
   }
-  const size_t as = arith_size(r->precision);
-  std::vector<uint8_t> samples(r->samples.size() * as);
-  if (as == 8) {
-    std::memcpy(samples.data(), r->samples.data(), samples.size());
-  } else {
-    for (size_t i = 0; i < r->samples.size(); ++i) {
-      const float v = (float)r->samples[i];
-      std::memcpy(samples.data() + 4 * i, &v, 4);
+  std::vector<int> fields;  // -1: one domain with every field
+  if (split_fields(r)) {
+    std::vector<bool> seen((size_t)r->fields, false);
+    for (int i = 0; i < r->n_src; ++i) {
+      const int f = r->src_field[(size_t)i];
+      if (f >= 0 && f < r->fields && !seen[(size_t)f]) {
+        seen[(size_t)f] = true;
+        fields.push_back(f);
+      }
     }
+    std::sort(fields.begin(), fields.end());
   }
-  if (!rc)
-    rc = DX != r->X ? pfdtd_set_nodes(d, ppos.data(), pmat.data(), 0)
-                    : pfdtd_set_nodes(d, r->pos.data(), r->mat.data(), 0);
-  if (!rc) rc = pfdtd_set_scheme(d, r->scheme);
-  if (!rc) rc = pfdtd_set_materials(d, r->materials.data(), r->n_mat, r->n_coef);
-  if (!rc && !r->dif_flags.empty())
-    rc = pfdtd_set_dif_filters(d, (int)r->dif_flags.size(), r->dif_flags.data(),
-                               r->dif_coefs.data());
-  if (!rc) rc = pfdtd_set_params(d, r->params);
-  if (!rc)
-    rc = pfdtd_set_sources_batched(d, r->n_src, r->src_xyz.data(), r->src_field.data(),
-                                   r->src_type.data(), samples.data(), r->n_samples);
-  if (!rc) rc = pfdtd_set_receivers_batched(d, r->n_rec, r->rec_xyz.data(), r->rec_field.data());
-  if (!rc) rc = pfdtd_set_temporal_block(d, r->tb_depth);
-  if (!rc) rc = pfdtd_run_async(d, r->steps);
+  if (fields.empty()) fields.push_back(-1);
+  int rc = PFDTD_OK;
+  for (int f : fields) {
+    std::vector<int> src_ids, rec_ids;
+    for (int i = 0; i < r->n_src; ++i)
+      if (f < 0 || r->src_field[(size_t)i] == f) src_ids.push_back(i);
+    for (int i = 0; i < r->n_rec; ++i)
+      if (f < 0 || r->rec_field[(size_t)i] == f) rec_ids.push_back(i);
+    pfdtd_domain* d = nullptr;
+    rc = setup_domain(s, r, f < 0 ? r->fields : 1, f, src_ids, rec_ids, ppos, pmat, &d);
+    if (rc) break;
+    j.doms.push_back(d);
+    j.part_field.push_back(f);
+  }
   if (rc) {
     j.error = pfdtd_last_error();
-    pfdtd_destroy(d);
+    for (pfdtd_domain* d : j.doms) pfdtd_destroy(d);
+    j.doms.clear();
+    j.part_field.clear();
     return rc;
   }
-  j.dom = d;
   return PFDTD_OK;
 }
 
+// Whether every domain of the job has drained; the first query error, if any.
+int query_job(Job& j, int* done) {
+  *done = 1;
+  for (pfdtd_domain* d : j.doms) {
+    int dd = 0;
+    if (int q = pfdtd_query(d, &dd)) return q;
+    if (!dd) *done = 0;
+  }
+  return PFDTD_OK;
+}
+
+// Receivers to the host (a split request's domains scattered back into the
+// request's receiver order; receivers on fields without a source stay 0, as
+// in a batched run) and the domains destroyed.
 int retire(Job& j) {
   pfdtd_request* r = j.req;
-  j.result.assign((size_t)r->n_rec * (size_t)r->steps * arith_size(r->precision), 0);
-  int rc = pfdtd_fetch_receivers(j.dom, j.result.data());
-  if (rc) j.error = pfdtd_last_error();
-  pfdtd_destroy(j.dom);
-  j.dom = nullptr;
+  const size_t as = arith_size(r->precision), row = (size_t)r->steps * as;
+  j.result.assign((size_t)r->n_rec * row, 0);
+  int rc = PFDTD_OK;
+  for (size_t p = 0; p < j.doms.size(); ++p) {
+    const int f = j.part_field[p];
+    if (f < 0) {
+      if (!rc && (rc = pfdtd_fetch_receivers(j.doms[p], j.result.data()))) j.error = pfdtd_last_error();
+    } else {
+      std::vector<int> rec_ids;
+      for (int i = 0; i < r->n_rec; ++i)
+        if (r->rec_field[(size_t)i] == f) rec_ids.push_back(i);
+      std::vector<uint8_t> part(rec_ids.size() * row);
+      if (!rc && !rec_ids.empty() && (rc = pfdtd_fetch_receivers(j.doms[p], part.data())))
+        j.error = pfdtd_last_error();
+      if (!rc)
+        for (size_t k = 0; k < rec_ids.size(); ++k)
+          std::memcpy(j.result.data() + (size_t)rec_ids[k] * row, part.data() + k * row, row);
+    }
+    pfdtd_destroy(j.doms[p]);
+  }
+  j.doms.clear();
+  j.part_field.clear();
   return rc;
 }
 
@@ -268,7 +383,7 @@ void scheduler(pfdtd_server* s) {
     for (size_t i = 0; i < s->active.size();) {
       Job& j = s->jobs[s->active[i]];
       int done = 0;
-      const int q = pfdtd_query(j.dom, &done);
+      const int q = query_job(j, &done);
       if (q == PFDTD_OK && !done) {
         ++i;
         continue;

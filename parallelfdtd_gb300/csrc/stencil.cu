@@ -469,6 +469,28 @@ int build_classes(pfdtd_domain* d) {
   count_launch();
   PFDTD_CK(cudaGetLastError());
   PFDTD_CK(cudaFreeAsync(d_lut, s));
+  // The TMA kernels read the class ids through a 2-D tensor map whose row
+  // stride must be a multiple of 16 bytes.  Where the field rows are 16-byte
+  // aligned but the class-id rows (X ids) are not, they read a copy with each
+  // row padded to 16 bytes.
+  const int64_t cls_row = d->X * cls_bytes;
+  if (cls_row % 16 != 0 && (d->X * d->K * (int64_t)d->esize) % 16 == 0) {
+    const int64_t pitch = (cls_row + 15) / 16 * 16;
+    const size_t need = (size_t)(pitch * d->Y * d->Z);
+    if (!d->d_cls_tma || d->cls_tma_bytes < need) {
+      d->release(d->d_cls_tma);
+      d->d_cls_tma = nullptr;
+      d->cls_tma_bytes = 0;
+      if (d->alloc(&d->d_cls_tma, need) != cudaSuccess)
+        return fail(PFDTD_ERR_NOMEM, "padded class-id allocation failed");
+      d->cls_tma_bytes = need;
+    }
+    PFDTD_CK(cudaMemcpy2DAsync(d->d_cls_tma, (size_t)pitch, d->d_cls, (size_t)cls_row,
+                               (size_t)cls_row, (size_t)(d->Y * d->Z), cudaMemcpyDeviceToDevice, s));
+    d->cls_pitch = pitch / cls_bytes;
+  } else {
+    d->cls_pitch = 0;
+  }
   PFDTD_CK(cudaStreamSynchronize(s));
   d->n_classes = n_classes;
   d->class_scheme = scheme;

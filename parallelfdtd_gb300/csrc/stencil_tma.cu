@@ -832,13 +832,14 @@ EncodeTiledFn encode_fn() {
   return fn;
 }
 
-// 2-D map over the flat array viewed as X-wide rows (Y*Z rows).
+// 2-D map over the flat array viewed as X-wide rows (Y*Z rows), each row
+// `pitch` elements apart (X when 0).
 bool make_map(CUtensorMap* m, CUtensorMapDataType dt, size_t esize, void* base, int64_t X,
-              int64_t rows, int box_x, int box_y) {
+              int64_t rows, int box_x, int box_y, int64_t pitch = 0) {
   EncodeTiledFn fn = encode_fn();
   if (!fn) return false;
   cuuint64_t dims[2] = {(cuuint64_t)X, (cuuint64_t)rows};
-  cuuint64_t strides[1] = {(cuuint64_t)(X * (int64_t)esize)};
+  cuuint64_t strides[1] = {(cuuint64_t)((pitch > 0 ? pitch : X) * (int64_t)esize)};
   cuuint32_t box[2] = {(cuuint32_t)box_x, (cuuint32_t)box_y};
   cuuint32_t es[2] = {1, 1};
   return fn(m, dt, 2, base, dims, strides, box, es, CU_TENSOR_MAP_INTERLEAVE_NONE,
@@ -860,10 +861,12 @@ int launch_tma_t(pfdtd_domain* d, const void* cur, void* past, cudaStream_t s) {
     if (d->field_base[f] && past == d->field(f)) past_i = f;
   }
   if (cur_i < 0 || past_i < 0) return fail(PFDTD_ERR_ARG, "update fields are not domain buffers");
-  const int64_t key[6] = {(int64_t)(intptr_t)d->d_cls, d->cls_bytes, d->precision * 100 + d->K,
+  // class ids: the padded copy when their rows are not 16-byte aligned
+  void* cls_base = d->cls_pitch > 0 ? d->d_cls_tma : d->d_cls;
+  const int64_t key[7] = {(int64_t)(intptr_t)cls_base, d->cls_bytes, d->precision * 100 + d->K,
                           (int64_t)Lay::TX * 10000 + Lay::TY * 10 + (Lay::XHALO ? 1 : 0),
                           (int64_t)(intptr_t)d->field_base[2],
-                          Lay::MASK ? (int64_t)(intptr_t)d->d_iwb_mask : 0};
+                          Lay::MASK ? (int64_t)(intptr_t)d->d_iwb_mask : 0, d->cls_pitch};
   if (!ts.ready || std::memcmp(key, ts.key, sizeof(key)) != 0) {
     const CUtensorMapDataType dt = TmaType<S>::value;
     const CUtensorMapDataType ct =
@@ -875,7 +878,8 @@ int launch_tma_t(pfdtd_domain* d, const void* cur, void* past, cudaStream_t s) {
       ok = ok && make_map(&ts.halo[f], dt, sizeof(S), d->field(f), XE, rows, Lay::PW, Lay::TY + 2);
       ok = ok && make_map(&ts.tile[f], dt, sizeof(S), d->field(f), XE, rows, kTX, Lay::TY);
     }
-    ok = ok && make_map(&ts.cls, ct, sizeof(C), d->d_cls, d->X, rows, kTX >> d->kshift, Lay::TY);
+    ok = ok && make_map(&ts.cls, ct, sizeof(C), cls_base, d->X, rows, kTX >> d->kshift, Lay::TY,
+                        d->cls_pitch);
     if (Lay::MASK) {
       if (!d->d_iwb_mask) return fail(PFDTD_ERR_STATE, "IWB masks not built");
       ok = ok && make_map(&ts.mask, CU_TENSOR_MAP_DATA_TYPE_UINT32, 4, d->d_iwb_mask, d->X, rows,
@@ -1174,7 +1178,7 @@ bool uses_tma(const pfdtd_domain* d) {
   return true;
 }
 
-// The TMA path needs 16-byte aligned rows for the fields and class ids.
+// The TMA path needs 16-byte aligned field rows (the class ids are padded).
 int tma_tile_count() { return 11; }
 
 bool tma_supported(const pfdtd_domain* d) {
@@ -1187,8 +1191,9 @@ bool tma_supported(const pfdtd_domain* d) {
     const int tile = d->precision == PFDTD_F64 ? 128 : 256;
     if (d->K % 4 != 0 || (tile / d->K) * d->cls_bytes < 16) return false;
   }
+  // (rows of class ids that are not 16-byte aligned are read from a padded
+  // copy, d_cls_tma)
   if ((d->X * (int64_t)d->esize) % 16 != 0) return false;
-  if ((d->X * (int64_t)d->cls_bytes) % 16 != 0) return false;
   if (d->Y * d->Z >= ((int64_t)1 << 31)) return false;
   return encode_fn() != nullptr;
 }

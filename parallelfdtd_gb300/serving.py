@@ -124,9 +124,12 @@ class Request:
         return float(X) * Y * (Z - 2) * self.steps * self.source_fields
 
     def computed_updates(self) -> float:
-        """Every field the request computes, padding included."""
+        """Every field the request computes, padding included.  An IWB
+        request with several fields runs one single-field domain per source
+        field, so it computes only those."""
         X, Y, Z = self.dims
-        return float(X) * Y * (Z - 2) * self.steps * self.fields
+        fields = self.source_fields if (self.scheme == L.IWB and self.fields > 1) else self.fields
+        return float(X) * Y * (Z - 2) * self.steps * fields
 
     def close(self) -> None:
         if self._h is not None:

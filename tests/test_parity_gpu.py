@@ -404,10 +404,12 @@ def test_tma_wrap_neighbours_on_outer_faces(gpu, O):
 @pytest.mark.parametrize("tile", list(range(9)))
 @pytest.mark.parametrize("centred", [False, True])
 @pytest.mark.parametrize("wide", [False, True])
-def test_tma_tile_shapes_bit_identical(gpu, O, tile, centred, wide):
+@pytest.mark.parametrize("X", [208, 200])
+def test_tma_tile_shapes_bit_identical(gpu, O, tile, centred, wide, X):
     """FP32 tile shapes; wide: materials drawn per voxel, more than 256 node
-    classes, so the class ids are 16-bit."""
-    room = rooms.boxes_room((208, 52, 40), n_boxes=6, edge=(5, 16), n_materials=150 if wide else 9,
+    classes, so the class ids are 16-bit; X = 200: rows of class ids that are
+    not 16-byte aligned (read from the padded copy)."""
+    room = rooms.boxes_room((X, 52, 40), n_boxes=6, edge=(5, 16), n_materials=150 if wide else 9,
                             seed=14)
     if wide:
         room.mat[...] = np.random.default_rng(5).integers(0, 150, room.mat.shape, dtype=np.uint8)
@@ -425,6 +427,7 @@ def test_tma_tile_shapes_bit_identical(gpu, O, tile, centred, wide):
         d.set_sources(src, [1], pulse[None])
         d.set_receivers(rec)
         g, _, _ = d.run(steps)
+        assert d.kernel() == "tma"
         P = d.download_field(L.FIELD_CURRENT)
     pos, mat = O.encode_nodes(room.bid, room.mat, centred)
     r, rP, _ = O.run(pos, mat, room.dims, room.admittance, default_params(), [room.flat(*src[0])],
@@ -437,14 +440,16 @@ def test_tma_tile_shapes_bit_identical(gpu, O, tile, centred, wide):
 @pytest.mark.parametrize("prec", ["f16", "bf16"])
 @pytest.mark.parametrize("centred,wide", [(False, False), (True, False), (False, True),
                                           (True, True)])
-def test_16bit_tile_shapes_bit_identical(gpu, O, tile, prec, centred, wide):
+@pytest.mark.parametrize("X", [208, 200])
+def test_16bit_tile_shapes_bit_identical(gpu, O, tile, prec, centred, wide, X):
     """Every 16-bit tile shape (4 and 8 elements per thread, planes carried
     in registers or reloaded), forward and centred, with 8-bit class ids and
     (wide: materials drawn per voxel, more than 256 node classes) 16-bit
-    class ids; X = 208 leaves partly filled tiles, Z = 40 a z-chunk whose
-    plane count is not a multiple of three.  Bit-identical to the oracle with
-    the same storage rounding."""
-    room = rooms.boxes_room((208, 52, 40), n_boxes=6, edge=(5, 16), n_materials=150 if wide else 9,
+    class ids; X = 208 leaves partly filled tiles, X = 200 rows of class ids
+    that are not 16-byte aligned, Z = 40 a z-chunk whose plane count is not a
+    multiple of three.  Bit-identical to the oracle with the same storage
+    rounding."""
+    room = rooms.boxes_room((X, 52, 40), n_boxes=6, edge=(5, 16), n_materials=150 if wide else 9,
                             seed=16)
     if wide:
         room.mat[...] = np.random.default_rng(5).integers(0, 150, room.mat.shape, dtype=np.uint8)
@@ -453,7 +458,7 @@ def test_16bit_tile_shapes_bit_identical(gpu, O, tile, prec, centred, wide):
     rec = [src[0]] + room.random_air_nodes(3, seed=4)  # the source node sees the pulse
     pulse = rooms.gaussian_pulse(steps, 3.0)
     pos, mat = O.encode_nodes(room.bid, room.mat, centred)
-    X, Y, Z = room.dims
+    Y, Z = room.dims[1], room.dims[2]
     keys = np.unique(pos.reshape(Z, -1)[1:Z - 1].astype(np.int32) * 256 + mat.reshape(Z, -1)[1:Z - 1])
     assert (len(keys) > 256) == wide
     with Domain(room.dims, prec) as d:
@@ -546,14 +551,16 @@ def test_iwb_open_x_faces(gpu, O, prec, variant):
 
 @pytest.mark.parametrize("prec", ["f32", "bf16"])
 @pytest.mark.parametrize("shape", list(range(11)))
-def test_iwb_tile_shapes(gpu, O, prec, shape):
+@pytest.mark.parametrize("X", [208, 200])
+def test_iwb_tile_shapes(gpu, O, prec, shape, X):
     """Every IWB tile shape on the TMA path equals the oracle, with DIF walls:
     shapes 0..5 run the closure inside the streaming kernel, 6..10 leave the
     nodes with a closed neighbour to the closure pass, which also applies the
     DIF update of those nodes.  The room is not a multiple of the 64- or
-    128-node tiles in x or of the tile rows in y."""
+    128-node tiles in x or of the tile rows in y; X = 200: rows of class ids
+    that are not 16-byte aligned."""
     from parallelfdtd_gb300 import materials
-    room = rooms.boxes_room((208, 44, 36), n_boxes=6, edge=(5, 12), n_materials=6, seed=16)
+    room = rooms.boxes_room((X, 44, 36), n_boxes=6, edge=(5, 12), n_materials=6, seed=16)
     steps = 90
     srcs = room.random_air_nodes(2, seed=1)
     rec = room.random_air_nodes(4, seed=2)

@@ -75,17 +75,23 @@ def test_node_updates_count_source_fields(built):
 
 
 def test_padded_rows_in_footprint(built):
-    """A room whose x extent is not a multiple of 16 and whose x = X-1 face is
-    closed runs on rows padded to 16 nodes: the footprint grows with them."""
+    """A room whose field rows are not 16-byte aligned (FP16, X = 60) and whose
+    x = X-1 face is closed runs on rows padded to 16 nodes: the footprint
+    grows with them.  FP32 rows of 60 nodes are aligned: no padding, only the
+    copy of the class ids with 16-byte rows."""
     from parallelfdtd_gb300 import rooms
     room = rooms.shoebox((60, 32, 24), seed=2)  # solid shell: x = X-1 face closed
-    r = Request(room.dims, 40, precision="f32").set_voxels(room.bid, room.mat)
+    r = Request(room.dims, 40, precision="f16").set_voxels(room.bid, room.mat)
     r.set_receivers([(10, 10, 10)])
     b60 = r.bytes()
     room64 = rooms.shoebox((64, 32, 24), seed=2)
-    r64 = Request(room64.dims, 40, precision="f32").set_voxels(room64.bid, room64.mat)
+    r64 = Request(room64.dims, 40, precision="f16").set_voxels(room64.bid, room64.mat)
     r64.set_receivers([(10, 10, 10)])
     assert abs(b60 - r64.bytes()) < 64 * 32 * 24  # the padded domain holds 64-wide rows
     # a receiver past X keeps the room unpadded
     r.set_receivers([(61, 10, 10)])
     assert r.bytes() < b60
+    f32 = Request(room.dims, 40, precision="f32").set_voxels(room.bid, room.mat)
+    f32_64 = Request(room64.dims, 40, precision="f32").set_voxels(room64.bid, room64.mat)
+    n60 = 60 * 32 * 24
+    assert f32.bytes() - 2 * n60 < f32_64.bytes()  # unpadded, plus the class-id copy

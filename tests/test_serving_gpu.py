@@ -112,3 +112,40 @@ def test_small_trace(gpu):
     assert res["stats"]["completed"] == 6
     assert res["latency_p99_s"] >= res["latency_p50_s"] > 0
     assert res["throughput"] > 0
+
+
+def test_iwb_fields_run_apart(gpu):
+    """An IWB request with 4 fields and sources on fields 0 and 2 only runs as
+    two single-field domains (the single-field IWB kernels); its receivers
+    equal a batched run of the same set-up bit for bit, and the receivers of
+    the fields without a source stay 0."""
+    from parallelfdtd_gb300 import materials
+    dims, steps = (100, 44, 40), 160
+    room = rooms.boxes_room(dims, n_boxes=4, edge=(4, 12), n_materials=5, seed=71)
+    pts = room.random_air_nodes(10, seed=72)
+    srcs, recs = [tuple(p) for p in pts[:2]], [tuple(p) for p in pts[2:10]]
+    src_fields, rec_fields = [0, 2], [0, 0, 1, 1, 2, 2, 3, 3]
+    pulse = rooms.gaussian_pulse(steps, 3.0)
+    samples = np.stack([pulse, -0.7 * pulse])
+    dif = (np.array([m % 2 for m in range(5)], np.int32),
+           materials.dif_table(materials.positive_real_filters(5, 3, seed=73), 3))
+    with Domain(dims, "f32", fields=4) as dom:
+        dom.set_voxels(room.bid, room.mat, centred=True)
+        dom.set_materials(room.admittance)
+        dom.set_dif_filters(*dif)
+        dom.set_params(default_params(scheme="iwb"))
+        dom.set_scheme("iwb")
+        dom.set_sources(srcs, [1, 1], samples, fields=src_fields)
+        dom.set_receivers(recs, fields=rec_fields)
+        ref, _, st = dom.run(steps)
+        assert st == 0
+    req = Request.from_room(room, steps, srcs, recs, samples, precision="f32", scheme="iwb",
+                            fields=4, src_fields=src_fields, rec_fields=rec_fields, dif=dif)
+    assert req.computed_updates() == req.node_updates()
+    with Server(0, hbm_budget=8 << 30, max_active=2) as srv:
+        t = srv.submit(req)
+        assert srv.wait(t, 120.0) == DONE, srv.error(t)
+        out, _ = srv.result(t)
+    assert np.abs(ref[[0, 1, 4, 5]]).max() > 1e-4
+    assert (ref[[2, 3, 6, 7]] == 0).all()
+    assert np.array_equal(out, ref)
