@@ -307,7 +307,8 @@ int pfdtd_query(pfdtd_domain* d, int* done);
 int pfdtd_fetch_receivers(pfdtd_domain* d, void* out);
 
 /* Update kernel variant: 0 automatic (the TMA-pipelined kernel when the
- * grid's rows are 16-byte aligned, i.e. X a multiple of 16, FP32/FP64), 1 the
+ * field rows are 16-byte aligned: X * fields * element size a multiple of 16;
+ * class-id rows that are not are read from a padded copy), 1 the
  * register z-marching kernel, 2 the TMA kernel.  pfdtd_get_kernel reports the
  * variant the next launch will use (1 or 2, or 3 when the temporally blocked
  * kernel of pfdtd_set_temporal_block will run). */
