@@ -12,7 +12,10 @@
  * domain on its own stream and queues the whole run there without waiting
  * (pfdtd_run_async); the scheduler goes on admitting meanwhile.  Admitted
  * requests therefore run concurrently on the device, and the host set-up of
- * one overlaps the others' runs.
+ * one overlaps the others' runs.  An IWB request with several fields runs
+ * the fields that carry a source one after another on one single-field
+ * domain (the IWB update's pipelined kernels are single-field), with the
+ * same receivers as a batched run.
  * When a request's stream has drained, its receivers are copied to the host,
  * its domain is destroyed (stream-ordered frees, no device-wide
  * synchronisation) and its memory returns to the budget.

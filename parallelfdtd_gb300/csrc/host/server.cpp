@@ -88,11 +88,13 @@ int source_fields(const pfdtd_request* r) {
 struct Job {
   pfdtd_request* req = nullptr;
   int state = PFDTD_REQ_QUEUED;
-  // The request's domains: one with all its fields, or (an IWB request with
-  // several fields, see split_fields) one single-field domain per field that
-  // carries a source, part_field[i] naming the field of doms[i].
-  std::vector<pfdtd_domain*> doms;
+  // The request's domain: one with all its fields (part_field {-1}), or (an
+  // IWB request with several fields, see split_fields) one single-field
+  // domain that runs the fields carrying a source one after another,
+  // part_field listing them and phase the one running.
+  pfdtd_domain* dom = nullptr;
   std::vector<int> part_field;
+  size_t phase = 0;
   uint64_t bytes = 0;
   Clock::time_point t_submit, t_admit, t_done;
   std::vector<uint8_t> result;
@@ -148,12 +150,13 @@ int64_t domain_x(const pfdtd_request* r) {
   return Xp;
 }
 
-// An IWB request with several fields runs as one single-field domain per
-// field that carries a source: the IWB update has its streaming TMA kernel and
-// closure pass for single-field domains only (batched IWB fields take the
-// column z-march), and every field of a batched domain is bit-identical to
-// the same field run alone, so the receivers do not change.  Fields without
-// a source stay zero and are not run.
+// An IWB request with several fields runs its fields that carry a source one
+// after another on one single-field domain (fields zeroed between them): the
+// IWB update has its streaming TMA kernel and closure pass for single-field
+// domains only (batched IWB fields take the column z-march), and every field
+// of a batched domain is bit-identical to the same field run alone, so the
+// receivers do not change.  Fields without a source stay zero and are not
+// run.  The domain is set up once for all of them.
 bool split_fields(const pfdtd_request* r) { return r->scheme == PFDTD_IWB && r->fields > 1; }
 
 uint64_t estimate_domain_bytes(const pfdtd_request* r, uint64_t K, int n_src, int n_rec) {
@@ -184,27 +187,24 @@ uint64_t estimate_domain_bytes(const pfdtd_request* r, uint64_t K, int n_src, in
 }
 
 uint64_t estimate_bytes(const pfdtd_request* r) {
-  if (!split_fields(r)) return estimate_domain_bytes(r, (uint64_t)r->fields, r->n_src, r->n_rec);
-  // one single-field domain per source field, each with its own sources and
-  // receivers; the summed source and receiver buffers are those of the request
-  const int parts = source_fields(r);
-  return (uint64_t)parts * estimate_domain_bytes(r, 1, 0, 0) +
-         estimate_domain_bytes(r, 1, r->n_src, r->n_rec) - estimate_domain_bytes(r, 1, 0, 0);
+  return estimate_domain_bytes(r, split_fields(r) ? 1 : (uint64_t)r->fields, r->n_src, r->n_rec);
 }
 
-// Create and set up one domain of the request with K fields and the given
-// sources and receivers (indices into the request's), and queue its run.
-// part_field: the request field that a single-field domain runs, its sources
-// and receivers moved to field 0 (-1: every field, numbered as the request
-// numbers them).
-int setup_domain(pfdtd_server* s, const pfdtd_request* r, int K, int part_field,
-                 const std::vector<int>& src_ids, const std::vector<int>& rec_ids,
-                 const std::vector<uint8_t>& ppos, const std::vector<uint8_t>& pmat,
-                 pfdtd_domain** out) {
-  const int64_t DX = domain_x(r);
-  pfdtd_domain* d = nullptr;
-  int rc = pfdtd_create_batched(DX, r->Y, r->Z, K, r->precision, s->device, &d);
-  if (rc) return rc;
+// The request's sources and receivers on field f (all of them for f < 0).
+void part_ids(const pfdtd_request* r, int f, std::vector<int>& src_ids, std::vector<int>& rec_ids) {
+  src_ids.clear();
+  rec_ids.clear();
+  for (int i = 0; i < r->n_src; ++i)
+    if (f < 0 || r->src_field[(size_t)i] == f) src_ids.push_back(i);
+  for (int i = 0; i < r->n_rec; ++i)
+    if (f < 0 || r->rec_field[(size_t)i] == f) rec_ids.push_back(i);
+}
+
+// Give domain d the sources and receivers of part_field (moved to field 0;
+// -1: every field as the request numbers them).
+int set_part_io(pfdtd_domain* d, const pfdtd_request* r, int part_field) {
+  std::vector<int> src_ids, rec_ids;
+  part_ids(r, part_field, src_ids, rec_ids);
   const size_t as = arith_size(r->precision);
   const size_t ns = (size_t)r->n_samples;
   std::vector<uint8_t> samples(src_ids.size() * ns * as);
@@ -229,30 +229,15 @@ int setup_domain(pfdtd_server* s, const pfdtd_request* r, int K, int part_field,
     for (int c = 0; c < 3; ++c) rxyz.push_back(r->rec_xyz[3 * (size_t)i + c]);
     rfield.push_back(part_field < 0 ? r->rec_field[(size_t)i] : 0);
   }
-  rc = DX != r->X ? pfdtd_set_nodes(d, ppos.data(), pmat.data(), 0)
-                  : pfdtd_set_nodes(d, r->pos.data(), r->mat.data(), 0);
-  if (!rc) rc = pfdtd_set_scheme(d, r->scheme);
-  if (!rc) rc = pfdtd_set_materials(d, r->materials.data(), r->n_mat, r->n_coef);
-  if (!rc && !r->dif_flags.empty())
-    rc = pfdtd_set_dif_filters(d, (int)r->dif_flags.size(), r->dif_flags.data(),
-                               r->dif_coefs.data());
-  if (!rc) rc = pfdtd_set_params(d, r->params);
-  if (!rc)
-    rc = pfdtd_set_sources_batched(d, (int)src_ids.size(), sxyz.data(), sfield.data(),
-                                   stype.data(), samples.data(), r->n_samples);
+  int rc = pfdtd_set_sources_batched(d, (int)src_ids.size(), sxyz.data(), sfield.data(),
+                                     stype.data(), samples.data(), r->n_samples);
   if (!rc) rc = pfdtd_set_receivers_batched(d, (int)rec_ids.size(), rxyz.data(), rfield.data());
-  if (!rc) rc = pfdtd_set_temporal_block(d, r->tb_depth);
-  if (!rc) rc = pfdtd_run_async(d, r->steps);
-  if (rc) {
-    pfdtd_destroy(d);
-    return rc;
-  }
-  *out = d;
-  return PFDTD_OK;
+  return rc;
 }
 
-// Create and set up the request's domains and queue their runs.  Returns the
-// status; on failure every domain is destroyed and the message kept.
+// Create and set up the request's domain and queue the run of its first
+// part.  Returns the status; on failure the domain is destroyed and the
+// message kept.
 int admit(pfdtd_server* s, Job& j) {
   pfdtd_request* r = j.req;
   const int64_t DX = domain_x(r);
@@ -265,85 +250,96 @@ int admit(pfdtd_server* s, Job& j) {
       std::memcpy(&pmat[(size_t)(row * DX)], &r->mat[(size_t)(row * r->X)], (size_t)r->X);
     }
   }
-  std::vector<int> fields;  // -1: one domain with every field
+  j.part_field.clear();
+  j.phase = 0;
   if (split_fields(r)) {
     std::vector<bool> seen((size_t)r->fields, false);
     for (int i = 0; i < r->n_src; ++i) {
       const int f = r->src_field[(size_t)i];
       if (f >= 0 && f < r->fields && !seen[(size_t)f]) {
         seen[(size_t)f] = true;
-        fields.push_back(f);
+        j.part_field.push_back(f);
       }
     }
-    std::sort(fields.begin(), fields.end());
+    std::sort(j.part_field.begin(), j.part_field.end());
   }
-  if (fields.empty()) fields.push_back(-1);
-  int rc = PFDTD_OK;
-  for (int f : fields) {
-    std::vector<int> src_ids, rec_ids;
-    for (int i = 0; i < r->n_src; ++i)
-      if (f < 0 || r->src_field[(size_t)i] == f) src_ids.push_back(i);
-    for (int i = 0; i < r->n_rec; ++i)
-      if (f < 0 || r->rec_field[(size_t)i] == f) rec_ids.push_back(i);
-    pfdtd_domain* d = nullptr;
-    rc = setup_domain(s, r, f < 0 ? r->fields : 1, f, src_ids, rec_ids, ppos, pmat, &d);
-    if (rc) break;
-    j.doms.push_back(d);
-    j.part_field.push_back(f);
-  }
+  if (j.part_field.empty()) j.part_field.push_back(-1);
+  j.result.assign((size_t)r->n_rec * (size_t)r->steps * arith_size(r->precision), 0);
+  const int K = j.part_field[0] < 0 ? r->fields : 1;
+  pfdtd_domain* d = nullptr;
+  int rc = pfdtd_create_batched(DX, r->Y, r->Z, K, r->precision, s->device, &d);
   if (rc) {
     j.error = pfdtd_last_error();
-    for (pfdtd_domain* d : j.doms) pfdtd_destroy(d);
-    j.doms.clear();
-    j.part_field.clear();
     return rc;
   }
+  rc = DX != r->X ? pfdtd_set_nodes(d, ppos.data(), pmat.data(), 0)
+                  : pfdtd_set_nodes(d, r->pos.data(), r->mat.data(), 0);
+  if (!rc) rc = pfdtd_set_scheme(d, r->scheme);
+  if (!rc) rc = pfdtd_set_materials(d, r->materials.data(), r->n_mat, r->n_coef);
+  if (!rc && !r->dif_flags.empty())
+    rc = pfdtd_set_dif_filters(d, (int)r->dif_flags.size(), r->dif_flags.data(),
+                               r->dif_coefs.data());
+  if (!rc) rc = pfdtd_set_params(d, r->params);
+  if (!rc) rc = set_part_io(d, r, j.part_field[0]);
+  if (!rc) rc = pfdtd_set_temporal_block(d, r->tb_depth);
+  if (!rc) rc = pfdtd_run_async(d, r->steps);
+  if (rc) {
+    j.error = pfdtd_last_error();
+    pfdtd_destroy(d);
+    return rc;
+  }
+  j.dom = d;
   return PFDTD_OK;
 }
 
-// Whether every domain of the job has drained; the first query error, if any.
-int query_job(Job& j, int* done) {
-  *done = 1;
-  for (pfdtd_domain* d : j.doms) {
-    int dd = 0;
-    if (int q = pfdtd_query(d, &dd)) return q;
-    if (!dd) *done = 0;
-  }
+// Receivers of the finished part `phase` into the request's receiver order
+// (receivers on fields without a source stay 0, as in a batched run).
+int collect_part(Job& j) {
+  const pfdtd_request* r = j.req;
+  const int f = j.part_field[j.phase];
+  if (f < 0) return pfdtd_fetch_receivers(j.dom, j.result.data());
+  std::vector<int> src_ids, rec_ids;
+  part_ids(r, f, src_ids, rec_ids);
+  if (rec_ids.empty()) return PFDTD_OK;
+  const size_t row = (size_t)r->steps * arith_size(r->precision);
+  std::vector<uint8_t> part(rec_ids.size() * row);
+  if (int rc = pfdtd_fetch_receivers(j.dom, part.data())) return rc;
+  for (size_t k = 0; k < rec_ids.size(); ++k)
+    std::memcpy(j.result.data() + (size_t)rec_ids[k] * row, part.data() + k * row, row);
   return PFDTD_OK;
 }
 
-// Receivers to the host (a split request's domains scattered back into the
-// request's receiver order; receivers on fields without a source stay 0, as
-// in a batched run) and the domains destroyed.
-int retire(Job& j) {
-  pfdtd_request* r = j.req;
-  const size_t as = arith_size(r->precision), row = (size_t)r->steps * as;
-  j.result.assign((size_t)r->n_rec * row, 0);
-  int rc = PFDTD_OK;
-  for (size_t p = 0; p < j.doms.size(); ++p) {
-    const int f = j.part_field[p];
-    if (f < 0) {
-      if (!rc && (rc = pfdtd_fetch_receivers(j.doms[p], j.result.data()))) j.error = pfdtd_last_error();
-    } else {
-      std::vector<int> rec_ids;
-      for (int i = 0; i < r->n_rec; ++i)
-        if (r->rec_field[(size_t)i] == f) rec_ids.push_back(i);
-      std::vector<uint8_t> part(rec_ids.size() * row);
-      if (!rc && !rec_ids.empty() && (rc = pfdtd_fetch_receivers(j.doms[p], part.data())))
-        j.error = pfdtd_last_error();
-      if (!rc)
-        for (size_t k = 0; k < rec_ids.size(); ++k)
-          std::memcpy(j.result.data() + (size_t)rec_ids[k] * row, part.data() + k * row, row);
-    }
-    pfdtd_destroy(j.doms[p]);
+// A part has finished and another follows: its receivers out, fields (and
+// filter states) zeroed, the next part's sources and receivers set, its run
+// queued.  On failure the domain is destroyed and the message kept.
+int advance(Job& j) {
+  int rc = collect_part(j);
+  if (!rc) {
+    j.phase++;
+    rc = pfdtd_reset_fields(j.dom);
   }
-  j.doms.clear();
-  j.part_field.clear();
+  if (!rc) rc = set_part_io(j.dom, j.req, j.part_field[j.phase]);
+  if (!rc) rc = pfdtd_run_async(j.dom, j.req->steps);
+  if (rc) {
+    j.error = pfdtd_last_error();
+    pfdtd_destroy(j.dom);
+    j.dom = nullptr;
+  }
   return rc;
 }
 
-// Set-up worker: takes admitted requests in order, sets each up with the
-// lock released, then makes it running (or failed).
+// Receivers of the last part to the host and the domain destroyed.
+int retire(Job& j) {
+  int rc = collect_part(j);
+  if (rc) j.error = pfdtd_last_error();
+  pfdtd_destroy(j.dom);
+  j.dom = nullptr;
+  return rc;
+}
+
+// Set-up worker: takes admitted requests (no domain yet: set up) and
+// requests between two parts (advance) in order, does that with the lock
+// released, then makes the request running (or failed).
 void setup_worker(pfdtd_server* s) {
   std::unique_lock<std::mutex> lk(s->mu);
   for (;;) {
@@ -352,9 +348,10 @@ void setup_worker(pfdtd_server* s) {
     const int64_t t = s->to_admit.front();
     s->to_admit.pop_front();
     Job& j = s->jobs[t];  // std::map: the reference stays valid while unlocked
+    const bool first = j.dom == nullptr;
     lk.unlock();
     const Clock::time_point t0 = Clock::now();
-    const int rc = admit(s, j);
+    const int rc = first ? admit(s, j) : advance(j);
     const double dt = std::chrono::duration<double>(Clock::now() - t0).count();
     lk.lock();
     s->admitting--;
@@ -367,7 +364,7 @@ void setup_worker(pfdtd_server* s) {
       s->cv_done.notify_all();
     } else {
       s->active.push_back(t);
-      s->st.admitted++;
+      if (first) s->st.admitted++;
       s->st.running = (int64_t)s->active.size();
       s->st.max_running = std::max<int>(s->st.max_running, (int)s->active.size());
     }
@@ -383,12 +380,23 @@ void scheduler(pfdtd_server* s) {
     for (size_t i = 0; i < s->active.size();) {
       Job& j = s->jobs[s->active[i]];
       int done = 0;
-      const int q = query_job(j, &done);
+      const int q = pfdtd_query(j.dom, &done);
       if (q == PFDTD_OK && !done) {
         ++i;
         continue;
       }
+      const int64_t ticket = s->active[i];
       s->active.erase(s->active.begin() + (ptrdiff_t)i);
+      if (q == PFDTD_OK && j.phase + 1 < j.part_field.size()) {
+        // another part follows: a set-up worker queues it; the request keeps
+        // its slot and its memory
+        s->admitting++;
+        s->to_admit.push_back(ticket);
+        s->cv_work.notify_one();
+        s->st.running = (int64_t)s->active.size();
+        progress = true;
+        continue;
+      }
       s->in_transit++;
       lk.unlock();
       const Clock::time_point t0 = Clock::now();

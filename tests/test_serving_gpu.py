@@ -84,9 +84,8 @@ def test_mix_equals_alone(gpu):
 
 def test_budget_bounds_concurrency(gpu):
     """A budget that holds any one of the requests but no two runs them one at
-    a time (the IWB request of SPECS, four single-field domains, is larger
-    than two of the others together and is left out)."""
-    idx = [0, 2, 3]
+    a time."""
+    idx = [0, 1, 2, 3]
     reqs = [make_request(i, SPECS[i]) for i in idx]
     sizes = sorted(r.bytes() for r in reqs)
     budget = int(1.2 * sizes[-1])
@@ -121,10 +120,12 @@ def test_small_trace(gpu):
 
 
 def test_iwb_fields_run_apart(gpu):
-    """An IWB request with 4 fields and sources on fields 0 and 2 only runs as
-    two single-field domains (the single-field IWB kernels); its receivers
-    equal a batched run of the same set-up bit for bit, and the receivers of
-    the fields without a source stay 0."""
+    """An IWB request with 4 fields and sources on fields 0 and 2 only runs
+    those two fields one after the other on one single-field domain (the
+    single-field IWB kernels); its receivers equal a batched run of the same
+    set-up bit for bit, and the receivers of the fields without a source stay
+    0.  Two such requests run at once, so parts of different requests
+    interleave."""
     from parallelfdtd_gb300 import materials
     dims, steps = (100, 44, 40), 160
     room = rooms.boxes_room(dims, n_boxes=4, edge=(4, 12), n_materials=5, seed=71)
@@ -148,10 +149,17 @@ def test_iwb_fields_run_apart(gpu):
     req = Request.from_room(room, steps, srcs, recs, samples, precision="f32", scheme="iwb",
                             fields=4, src_fields=src_fields, rec_fields=rec_fields, dif=dif)
     assert req.computed_updates() == req.node_updates()
+    req2 = Request.from_room(room, steps, srcs, recs, samples, precision="f32", scheme="iwb",
+                             fields=4, src_fields=src_fields, rec_fields=rec_fields, dif=dif)
     with Server(0, hbm_budget=8 << 30, max_active=2) as srv:
-        t = srv.submit(req)
-        assert srv.wait(t, 120.0) == DONE, srv.error(t)
-        out, _ = srv.result(t)
+        tickets = [srv.submit(req), srv.submit(req2)]
+        outs = []
+        for t in tickets:
+            assert srv.wait(t, 120.0) == DONE, srv.error(t)
+            outs.append(srv.result(t)[0])
+        st = srv.stats()
+    assert st["completed"] == 2 and st["admitted"] == 2 and st["bytes_in_use"] == 0
     assert np.abs(ref[[0, 1, 4, 5]]).max() > 1e-4
     assert (ref[[2, 3, 6, 7]] == 0).all()
-    assert np.array_equal(out, ref)
+    for out in outs:
+        assert np.array_equal(out, ref)
