@@ -365,8 +365,9 @@ def run_serving(a, world, rank, local):
                      "node_updates": res["node_updates"],
                      "computed_node_updates": res["computed_updates"],
                      "note": "value counts the fields that carry a source; a request's field "
-                             "count is rounded up to a power of two and the padding fields "
-                             "are computed but not counted"},
+                             "count is rounded up to a power of two, and a request with "
+                             "fields without a source (or IWB, or 2 fields) runs its source "
+                             "fields one after another on a single-field domain"},
             "clocks": clk.summary(),
         }
         print(json.dumps(line), flush=True)

@@ -150,14 +150,20 @@ int64_t domain_x(const pfdtd_request* r) {
   return Xp;
 }
 
-// An IWB request with several fields runs its fields that carry a source one
-// after another on one single-field domain (fields zeroed between them): the
-// IWB update has its streaming TMA kernel and closure pass for single-field
-// domains only (batched IWB fields take the column z-march), and every field
-// of a batched domain is bit-identical to the same field run alone, so the
-// receivers do not change.  Fields without a source stay zero and are not
-// run.  The domain is set up once for all of them.
-bool split_fields(const pfdtd_request* r) { return r->scheme == PFDTD_IWB && r->fields > 1; }
+// A request with several fields runs its fields that carry a source one
+// after another on one single-field domain (fields zeroed between them) when
+// a batched domain would not stream them at the single-field rate: IWB (its
+// streaming TMA kernel and closure pass are single-field; batched IWB fields
+// take the column z-march), a field count that the batched TMA kernel does
+// not take (not a multiple of 4), or fields without a source (computed in a
+// batched domain, skipped here: the batched kernel streams a field at most
+// ~1.1x the single-field rate, so every unused field costs more than it
+// saves).  Every field of a batched domain is bit-identical to the same field
+// run alone, so the receivers do not change.  The domain is set up once.
+bool split_fields(const pfdtd_request* r) {
+  if (r->fields <= 1) return false;
+  return r->scheme == PFDTD_IWB || r->fields % 4 != 0 || source_fields(r) < r->fields;
+}
 
 uint64_t estimate_domain_bytes(const pfdtd_request* r, uint64_t K, int n_src, int n_rec) {
   const uint64_t es = storage_size(r->precision), as = arith_size(r->precision);

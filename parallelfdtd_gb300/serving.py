@@ -124,12 +124,12 @@ class Request:
         return float(X) * Y * (Z - 2) * self.steps * self.source_fields
 
     def computed_updates(self) -> float:
-        """Every field the request computes, padding included.  An IWB
-        request with several fields runs one single-field domain per source
-        field, so it computes only those."""
+        """Every field the request computes.  The server runs the fields that
+        carry a source one after another on a single-field domain whenever
+        some field has none (and for IWB, or a field count the batched kernel
+        does not take), so it computes exactly the source fields."""
         X, Y, Z = self.dims
-        fields = self.source_fields if (self.scheme == L.IWB and self.fields > 1) else self.fields
-        return float(X) * Y * (Z - 2) * self.steps * fields
+        return float(X) * Y * (Z - 2) * self.steps * self.source_fields
 
     def close(self) -> None:
         if self._h is not None:

@@ -59,8 +59,9 @@ def test_serving_trace_is_seeded_and_bounded():
 
 def test_node_updates_count_source_fields(built):
     """A request's field count is rounded up to a power of two; only the
-    fields that carry a source count as node-updates (computed_updates keeps
-    the padding fields)."""
+    fields that carry a source count as node-updates, and a request with
+    fields without a source runs only the others (computed_updates), while a
+    request whose every field carries a source runs them batched."""
     dims, steps = (32, 24, 20), 50
     r = Request(dims, steps, fields=16, precision="f32")
     r.set_voxels(np.zeros(32 * 24 * 20, np.uint8), np.zeros(32 * 24 * 20, np.uint8))
@@ -68,7 +69,10 @@ def test_node_updates_count_source_fields(built):
     r.set_sources([(5, 5, 5)] * 9, [1] * 9, pulse, fields=list(range(9)))
     per_field = 32 * 24 * 18 * steps
     assert r.node_updates() == 9 * per_field
-    assert r.computed_updates() == 16 * per_field
+    assert r.computed_updates() == 9 * per_field
+    full = Request(dims, steps, fields=4, precision="f32")
+    full.set_sources([(5, 5, 5)] * 4, [1] * 4, pulse[:4], fields=list(range(4)))
+    assert full.computed_updates() == full.node_updates() == 4 * per_field
     one = Request(dims, steps, fields=1)
     one.set_sources([(5, 5, 5)], [1], pulse[:1])
     assert one.node_updates() == per_field
