@@ -547,6 +547,9 @@ int pfdtd_request_set_sources(pfdtd_request* r, int n, const int64_t* xyz, const
   if (int rc = check_req(r)) return rc;
   if (n < 0 || n_samples < 0 || (n > 0 && (!xyz || !type || (n_samples > 0 && !samples))))
     return fail(PFDTD_ERR_ARG, "invalid source arrays");
+  if (field)
+    for (int i = 0; i < n; ++i)
+      if (field[i] < 0 || field[i] >= r->fields) return fail(PFDTD_ERR_ARG, "source field out of range");
   r->n_src = n;
   r->n_samples = n_samples;
   r->src_xyz.assign(xyz, xyz + 3 * (size_t)n);
@@ -561,6 +564,10 @@ int pfdtd_request_set_receivers(pfdtd_request* r, int n, const int64_t* xyz,
                                 const int32_t* field) {
   if (int rc = check_req(r)) return rc;
   if (n < 0 || (n > 0 && !xyz)) return fail(PFDTD_ERR_ARG, "invalid receiver array");
+  if (field)
+    for (int i = 0; i < n; ++i)
+      if (field[i] < 0 || field[i] >= r->fields)
+        return fail(PFDTD_ERR_ARG, "receiver field out of range");
   r->n_rec = n;
   r->rec_xyz.assign(xyz, xyz + 3 * (size_t)n);
   if (field) r->rec_field.assign(field, field + n);

@@ -37,6 +37,12 @@ def test_request_validation(built):
     r = Request((16, 16, 16), 10)
     with pytest.raises(L.PfdtdError):
         r.set_temporal_block(5)
+    r4 = Request((16, 16, 16), 10, fields=4)
+    with pytest.raises(L.PfdtdError):  # a field the request does not have
+        r4.set_sources([(5, 5, 5)], [1], np.zeros((1, 10)), fields=[4])
+    with pytest.raises(L.PfdtdError):
+        r4.set_receivers([(5, 5, 5)], fields=[-1])
+    r4.set_sources([(5, 5, 5)], [1], np.zeros((1, 10)), fields=[3])
 
 
 def test_serving_trace_is_seeded_and_bounded():
