@@ -163,7 +163,6 @@ struct TmaState {
   CUtensorMap tile[4];
   CUtensorMap cls;
   CUtensorMap mask;  // IWB closed-neighbour masks (4 bytes per node)
-  CUtensorMap side[4];  // the narrow boxes beside a batched tile's rows
   int64_t key[7] = {0, 0, 0, 0, 0, 0, 0};
   bool ready = false;
   bool attr_set[2][2][2] = {{{false, false}, {false, false}}, {{false, false}, {false, false}}};

@@ -52,16 +52,12 @@ __host__ __device__ constexpr int round128(int b) { return (b + 127) / 128 * 128
 // allocation must allow; VEC: consecutive x elements per consumer thread (4,
 // or 8 for 16-bit fields: one 16-byte shared-memory load per row vector, and
 // the per-thread index and barrier work spread over twice the updates); ZC:
-// the 7-point consumer keeps planes z-1 and z in registers along the z-march;
-// SIDE (batched fields, no x halo in the box): each stage also holds the HS
-// elements left and right of the tile's rows, two narrow boxes, so that the
-// nodes at the tile's x edges read their x neighbours (K <= HS fields away)
-// from shared memory instead of global memory.
+// the 7-point consumer keeps planes z-1 and z in registers along the z-march.
 template <typename S, typename C, int TX_, int TY_, int NS_, bool XHALO_ = true, bool MASK_ = false,
-          int MINB_ = 1, int VEC_ = kVec, bool ZC_ = false, bool SIDE_ = false>
+          int MINB_ = 1, int VEC_ = kVec, bool ZC_ = false>
 struct Layout {
   static constexpr int TX = TX_, TY = TY_, NS = NS_, MINB = MINB_, VEC = VEC_;
-  static constexpr bool ZC = ZC_, SIDE = SIDE_;
+  static constexpr bool ZC = ZC_;
   static_assert(VEC == 4 || (VEC == 8 && sizeof(S) == 2), "8-element vectors: 16-bit fields");
   // With XHALO the box carries a 16-byte x halo on both sides; without it the
   // box is exactly TX wide (up to 256) and the threads at the tile's x edges
@@ -79,12 +75,7 @@ struct Layout {
   static constexpr bool MASK = MASK_;
   static constexpr int MK_BYTES = MASK ? TX * TY * 4 : 0;
   static constexpr int MK_OFF = CL_OFF + round128(CL_BYTES);
-  static constexpr int HS = SIDE ? 32 / (int)sizeof(S) : 0;   // side elements (32 bytes)
-  static constexpr int SD_BYTES = HS * (TY + 2) * (int)sizeof(S);
-  static constexpr int SL_OFF = MK_OFF + round128(MK_BYTES);
-  static constexpr int SR_OFF = SL_OFF + round128(SD_BYTES);
-  static constexpr int STAGE = SR_OFF + round128(SD_BYTES);
-  static_assert(!(SIDE && (XHALO || MASK)), "side boxes replace the in-box x halo");
+  static constexpr int STAGE = MK_OFF + round128(MK_BYTES);
   static constexpr int BAR_OFF = STAGE * NS;
   // full + empty barriers + abort flag, plus 128 B to align the dynamic base
   static constexpr int SMEM = BAR_OFF + 2 * NS * 8 + 16 + 128;
@@ -357,9 +348,8 @@ __device__ __forceinline__ void iwb_plane_sums(const S* pl, int si, const S* __r
 }
 
 // Producer of the stage ring (one thread): stage k receives the P^n plane
-// z0-1+k of the tile with its halo (SIDE: and the side boxes, through
-// map_mask) and, from k = 2 on, the P^{n-1} plane and the class ids of plane
-// z0+k-2.  Every wait is bounded (wait_ns for a free
+// z0-1+k of the tile with its halo and, from k = 2 on, the P^{n-1} plane and
+// the class ids of plane z0+k-2.  Every wait is bounded (wait_ns for a free
 // stage); on expiry it raises the error flag and the abort flag, then waits
 // for the loads it already issued, with the full kWaitLimitNs whatever
 // wait_ns is, so that no bulk copy is in flight when the CTA exits.
@@ -387,14 +377,10 @@ __device__ __forceinline__ void tma_producer(const CUtensorMap* map_cur,
     unsigned char* st = smem + slot * Lay::STAGE;
     const uint32_t bar = bar_full + 8 * slot;
     const int zp = z0 - 1 + k;
-    uint32_t bytes = Lay::P_BYTES + 2 * Lay::SD_BYTES;
+    uint32_t bytes = Lay::P_BYTES;
     if (k >= 2) bytes += Lay::PP_BYTES + (Lay::CL_BYTES >> kshift) + Lay::MK_BYTES;
     mbar_expect_tx(bar, bytes);
     tma_load_2d(smem_u32(st + Lay::P_OFF), map_cur, x0 - H, zp * Y + y0 - 1, bar);
-    if constexpr (Lay::SIDE) {  // map_mask is the side map here
-      tma_load_2d(smem_u32(st + Lay::SL_OFF), map_mask, x0 - Lay::HS, zp * Y + y0 - 1, bar);
-      tma_load_2d(smem_u32(st + Lay::SR_OFF), map_mask, x0 + Lay::TX, zp * Y + y0 - 1, bar);
-    }
     if (k >= 2) {
       const int zc_ = z0 + k - 2;
       tma_load_2d(smem_u32(st + Lay::PP_OFF), map_past, x0, zc_ * Y + y0, bar);
@@ -517,20 +503,10 @@ k_update_tma(const __grid_constant__ CUtensorMap map_cur, const __grid_constant_
       unsigned cid[VEC];
       if (BATCHED) {
         const int kk = 1 << kshift;
-        // the first and last node of a row read their flat-index neighbours
-        // (the previous row's last node, the next row's first node) from
-        // global memory, also in a partly filled tile
-        if (Lay::SIDE && kk <= Lay::HS) {
-          const S* Sl = (const S*)(smem + sc_ * Lay::STAGE + Lay::SL_OFF) + (ly + 1) * Lay::HS;
-          const S* Sr = (const S*)(smem + sc_ * Lay::STAGE + Lay::SR_OFF) + (ly + 1) * Lay::HS;
-          vxm = x < kk ? ldgv<VEC>(P + idx - kk)
-                       : ldsv<VEC>(lx >= kk ? Pc + si - kk : Sl + Lay::HS - kk + lx);
-          vxp = x + kk >= X ? ldgv<VEC>(P + idx + kk)
-                            : ldsv<VEC>(lx + kk < kTX ? Pc + si + kk : Sr + lx + kk - kTX);
-        } else {
-          vxm = lx >= kk ? ldsv<VEC>(Pc + si - kk) : ldgv<VEC>(P + idx - kk);
-          vxp = (lx + kk < kTX && x + kk < X) ? ldsv<VEC>(Pc + si + kk) : ldgv<VEC>(P + idx + kk);
-        }
+        vxm = lx >= kk ? ldsv<VEC>(Pc + si - kk) : ldgv<VEC>(P + idx - kk);
+        // the last node of a row reads its flat-index neighbour (the next
+        // row's first node) from global memory, also in a partly filled tile
+        vxp = (lx + kk < kTX && x + kk < X) ? ldsv<VEC>(Pc + si + kk) : ldgv<VEC>(P + idx + kk);
         const unsigned c = Cl[ly * (kTX >> kshift) + (lx >> kshift)];
 #pragma unroll
         for (int e = 0; e < VEC; ++e) cid[e] = c;
@@ -888,8 +864,7 @@ int launch_tma_t(pfdtd_domain* d, const void* cur, void* past, cudaStream_t s) {
   // class ids: the padded copy when their rows are not 16-byte aligned
   void* cls_base = d->cls_pitch > 0 ? d->d_cls_tma : d->d_cls;
   const int64_t key[7] = {(int64_t)(intptr_t)cls_base, d->cls_bytes, d->precision * 100 + d->K,
-                          (int64_t)Lay::TX * 10000 + Lay::TY * 10 + (Lay::XHALO ? 1 : 0) +
-                              (Lay::SIDE ? 2 : 0),
+                          (int64_t)Lay::TX * 10000 + Lay::TY * 10 + (Lay::XHALO ? 1 : 0),
                           (int64_t)(intptr_t)d->field_base[2],
                           Lay::MASK ? (int64_t)(intptr_t)d->d_iwb_mask : 0, d->cls_pitch};
   if (!ts.ready || std::memcmp(key, ts.key, sizeof(key)) != 0) {
@@ -902,8 +877,6 @@ int launch_tma_t(pfdtd_domain* d, const void* cur, void* past, cudaStream_t s) {
       if (!d->field_base[f]) continue;
       ok = ok && make_map(&ts.halo[f], dt, sizeof(S), d->field(f), XE, rows, Lay::PW, Lay::TY + 2);
       ok = ok && make_map(&ts.tile[f], dt, sizeof(S), d->field(f), XE, rows, kTX, Lay::TY);
-      if (Lay::SIDE)
-        ok = ok && make_map(&ts.side[f], dt, sizeof(S), d->field(f), XE, rows, Lay::HS, Lay::TY + 2);
     }
     ok = ok && make_map(&ts.cls, ct, sizeof(C), cls_base, d->X, rows, kTX >> d->kshift, Lay::TY,
                         d->cls_pitch);
@@ -966,8 +939,7 @@ int launch_tma_t(pfdtd_domain* d, const void* cur, void* past, cudaStream_t s) {
                   (const A*)(tb + 2 * as * d->n_classes),
                   (const uint32_t*)(tb + 3 * as * d->n_classes), d->n_classes};
   k_update_tma<S, C, SCHEME, Lay, BATCHED><<<dim3(gx, gy, gz), Lay::THREADS, Lay::SMEM, s>>>(
-      ts.halo[cur_i], ts.tile[past_i], ts.cls,
-      Lay::MASK ? ts.mask : (Lay::SIDE ? ts.side[cur_i] : ts.cls), (const S*)cur,
+      ts.halo[cur_i], ts.tile[past_i], ts.cls, Lay::MASK ? ts.mask : ts.cls, (const S*)cur,
       (S*)past, tab, (int)XE, (int)d->Y, d->XY * d->K, (int)(d->Z - 1), (int)zc,
       (A)d->params[1], d->d_err, d->kshift, SCHEME == 3 ? d->d_iwb_sw : nullptr, -0.0f,
       d->wait_ns);
@@ -1085,14 +1057,9 @@ int launch_tma_16(pfdtd_domain* d, const void* cur, void* past, cudaStream_t s) 
     // 2 = 256 x 8, 6 stages, two CTAs; with 8 elements (fields of one node)
     // per thread, for K a multiple of 8: 3 = 256 x 8, 8 stages, two CTAs;
     // 4 = 256 x 4, 8 stages, four CTAs; 5 (the default) = as 3 with planes
-    // z-1, z carried in registers; 6 = as 5 with the side boxes (the tile's
-    // x-edge nodes read their neighbours from shared memory, K <= 16).  Measured on the 384 x 320 x 256 room,
+    // z-1, z carried in registers.  Measured on the 384 x 320 x 256 room,
     // K = 16, FP16 (field-updates/s): 0 710 G, 3 896 G, 4 900 G, 5 928 G.
-    const int tile = d->tma_tile < 0 || d->tma_tile > 6 ? 5 : d->tma_tile;
-    if (d->K % 8 == 0 && tile == 6)
-      return launch_tma_batched<S, Layout<S, uint8_t, 256, 8, 8, false, false, 2, 8, true, true>,
-                                Layout<S, uint16_t, 256, 8, 8, false, false, 2, 8, true, true>>(
-          d, cur, past, s);
+    const int tile = d->tma_tile < 0 || d->tma_tile > 5 ? 5 : d->tma_tile;
     if (d->K % 8 == 0 && tile == 5)
       return launch_tma_batched<S, Layout<S, uint8_t, 256, 8, 8, false, false, 2, 8, true>,
                                 Layout<S, uint16_t, 256, 8, 8, false, false, 2, 8, true>>(d, cur, past, s);
