@@ -1003,13 +1003,15 @@ def test_batched_partly_filled_tiles(gpu, O, fields, prec):
 @pytest.mark.parametrize("tile", [0, 1, 2, 3, 4, 5])
 @pytest.mark.parametrize("fields,prec", [(16, "f16"), (8, "bf16"), (4, "f16")])
 @pytest.mark.parametrize("centred", [False, True])
-def test_batched_16bit_tile_shapes(gpu, O, monkeypatch, tile, fields, prec, centred):
+@pytest.mark.parametrize("dims", [(64, 48, 40), (72, 40, 32)])
+def test_batched_16bit_tile_shapes(gpu, O, monkeypatch, tile, fields, prec, centred, dims):
     """The batched 16-bit tile shapes (1: 256 x 4 elements, four CTAs per SM;
     2: 256 x 8, six stages; 3 and 4: 8 fields per thread, 5: the same with
     planes carried in registers, for K a multiple of 8, else the default
-    shape) equal an oracle run of each field alone."""
+    shape) equal an oracle run of each field alone.  X = 72 leaves the last
+    tile of a row partly filled."""
     monkeypatch.setenv("PFDTD_TMA_TILE", str(tile))
-    room = rooms.boxes_room((64, 48, 40), n_boxes=5, edge=(5, 14), n_materials=6, seed=45)
+    room = rooms.boxes_room(dims, n_boxes=5, edge=(5, 14), n_materials=6, seed=45)
     steps = 90
     pulse = rooms.gaussian_pulse(steps, 3.0)
     srcs = room.random_air_nodes(fields, seed=5)
