@@ -320,12 +320,20 @@ int pfdtd_set_kernel(pfdtd_domain* d, int variant);
 /* Tile shape of the TMA kernel for FP32 fields: 0 64x16, 1 128x8, 2 32x32,
  * 3 128x16, 4 128x4 (x halo in the TMA box); 5 128x8, 6 256x4, 7 256x8,
  * 8 256x2 (x halo read from global); -1 (default) picks the widest of
- * 256/128/64 that divides X.  FP64 always uses 64x8.  For the IWB scheme the
- * same index picks the IWB shape: 0..5 carry the closed-neighbour masks and
- * compute the closure in the kernel (0 64x16, 1 128x8, 2 128x4, 3..5 64x8
- * with 3, 4, 5 CTAs per SM); 6..8 run the open sums in the kernel and a
- * sparse pass for the nodes with a closed neighbour (6 128x8 with 3 CTAs per
- * SM, the default; 7 128x4 with 4; 8 128x8 with 2). */
+ * 256/128/64 whose partly filled last tile leaves at most 1/16 of the row's
+ * tiles empty.  FP64 always uses 64x8.  FP16/BF16 fields: 0 64x16, 1 128x8,
+ * 2 256x8, 3 256x4 with 4 nodes per thread; 4 256x8, 5 256x8 (three CTAs per
+ * SM), 6 256x4, 7 128x8 with 8 nodes per thread; 8 256x8 (default), 9 256x4,
+ * 10 128x8 with 8 nodes per thread and planes z-1, z kept in registers.
+ * Batched 16-bit fields: 0 256x8, 1 256x4, 2 256x8 with 6 stages (4 fields
+ * per thread); for K a multiple of 8, 3 256x8, 4 256x4 (8 fields per
+ * thread), 5 256x8 with planes kept in registers (default).  For the IWB
+ * scheme the same index picks the IWB shape: 0..5 carry the closed-neighbour
+ * masks and compute the closure in the kernel (0 64x16, 1 128x8, 2 128x4,
+ * 3..5 64x8 with 3, 4, 5 CTAs per SM); 6..10 run the open sums in the kernel
+ * and a sparse pass for the nodes with a closed neighbour (6 128x8 with 3
+ * CTAs per SM, the default; 7 128x4 with 4; 8 128x8 with 2; 9 128x8 with 4;
+ * 10 128x4 with 6).  Every shape gives bit-identical results. */
 int pfdtd_set_tile(pfdtd_domain* d, int tile);
 int pfdtd_get_kernel(pfdtd_domain* d, int* variant);
 
