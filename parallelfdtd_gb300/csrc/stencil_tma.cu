@@ -534,12 +534,15 @@ k_update_tma(const __grid_constant__ CUtensorMap map_cur, const __grid_constant_
 #pragma unroll
         for (int e = 0; e < VEC; ++e) cid[e] = (ws[e >> 1] >> (16 * (e & 1))) & 0xFFFFu;
       }
-      if constexpr ((SCHEME == 0 || SCHEME == 4) && sizeof(A) == 4) {
-        // Forward update of the thread's elements as packed pairs: the same
-        // operations and rounding as the scalar loop below, with every
-        // product formed as fma(x, y, -0) so that none is contracted.
-        // Batched: the pairs are fields of one node (one class); otherwise
-        // adjacent x nodes (a class each).
+      if constexpr ((SCHEME == 0 || SCHEME == 4 || (SCHEME == 1 && sizeof(S) == 4)) &&
+                    sizeof(A) == 4) {
+        // Forward and (FP32 fields) centred updates of the thread's elements
+        // as packed pairs: the same operations and rounding as the scalar
+        // loop below, with every product formed as fma(x, y, -0) so that
+        // none is contracted.  Batched: the pairs are fields of one node (one
+        // class); otherwise adjacent x nodes (a class each).  (The centred
+        // update of 16-bit fields stays scalar: packed, its 8-element tiles
+        // spill under their register cap.)
         using namespace px;
         constexpr int NP = VEC / 2;
         auto coef = [&](int e) -> PackedCoef<A> {
@@ -552,8 +555,11 @@ k_update_tma(const __grid_constant__ CUtensorMap map_cur, const __grid_constant_
           return pk2(St::load(v.v[2 * h]), St::load(v.v[2 * h + 1]));
         };
         f2 aa[NP], bb[NP], cc[NP], ee[NP], xm2[NP], xp2[NP];
+        uint32_t kp[VEC];  // class position words (centred: boundary directions)
         if constexpr (BATCHED) {
           const PackedCoef<A> k = coef(0);
+#pragma unroll
+          for (int e = 0; e < VEC; ++e) kp[e] = k.pos;
 #pragma unroll
           for (int h = 0; h < NP; ++h) {
             aa[h] = pk2(k.a, k.a);
@@ -567,6 +573,8 @@ k_update_tma(const __grid_constant__ CUtensorMap map_cur, const __grid_constant_
 #pragma unroll
           for (int h = 0; h < NP; ++h) {
             const PackedCoef<A> k0 = coef(2 * h), k1 = coef(2 * h + 1);
+            kp[2 * h] = k0.pos;
+            kp[2 * h + 1] = k1.pos;
             aa[h] = pk2(k0.a, k1.a);
             bb[h] = pk2(k0.b, k1.b);
             cc[h] = pk2(k0.c, k1.c);
@@ -580,13 +588,44 @@ k_update_tma(const __grid_constant__ CUtensorMap map_cur, const __grid_constant_
 #pragma unroll
         for (int h = 0; h < NP; ++h) {
           const f2 pc2 = pk2(fc[2 * h], fc[2 * h + 1]);
-          const f2 s6 = add2(add2(add2(add2(add2(pk2(fn[2 * h], fn[2 * h + 1]),
-                                                 pk2(fm[2 * h], fm[2 * h + 1])),
-                                            pr(vyp, h)),
-                                       pr(vym, h)),
-                                  xp2[h]),
-                             xm2[h]);
+          const f2 pn2 = pk2(fn[2 * h], fn[2 * h + 1]), pm2 = pk2(fm[2 * h], fm[2 * h + 1]);
           f2 o;
+          if constexpr (SCHEME == 1) {
+            // centred: s7 = ((((((xm + xp) + ym) + yp) + pn) + pm) + sb6, sb6
+            // = (bx dx + by dy) + bz dz with each node's boundary neighbours
+            // and directions taken from its class position word
+            float bx[2], by[2], bz[2], dx[2], dy[2], dz[2];
+#pragma unroll
+            for (int q = 0; q < 2; ++q) {
+              const int e = 2 * h + q;
+              const uint32_t cp = kp[e];
+              float xm, xp;
+              if constexpr (BATCHED) {
+                xm = St::load(vxm.v[e]);
+                xp = St::load(vxp.v[e]);
+              } else {
+                xm = e == 0 ? left : fc[e - 1];
+                xp = e == VEC - 1 ? right : fc[e + 1];
+              }
+              bx[q] = (cp & 0x10u) ? xp : xm;
+              by[q] = (cp & 0x20u) ? St::load(vyp.v[e]) : St::load(vym.v[e]);
+              bz[q] = (cp & 0x40u) ? fm[e] : fn[e];
+              dx[q] = (float)(cp & 1u);
+              dy[q] = (float)((cp >> 1) & 1u);
+              dz[q] = (float)((cp >> 2) & 1u);
+            }
+            const f2 sb6 = add2(add2(fma2(pk2(bx[0], bx[1]), pk2(dx[0], dx[1]), nz),
+                                     fma2(pk2(by[0], by[1]), pk2(dy[0], dy[1]), nz)),
+                                fma2(pk2(bz[0], bz[1]), pk2(dz[0], dz[1]), nz));
+            const f2 s7 = add2(add2(add2(add2(add2(add2(xm2[h], xp2[h]), pr(vym, h)), pr(vyp, h)),
+                                              pn2),
+                                         pm2),
+                               sb6);
+            o = mul2(aa[h], add2(sub2(fma2(s7, l22, nz), fma2(bb[h], pc2, nz)),
+                                 fma2(cc[h], pr(vpp, h), nz)));
+          } else {
+          const f2 s6 = add2(add2(add2(add2(add2(pn2, pm2), pr(vyp, h)), pr(vym, h)), xp2[h]),
+                             xm2[h]);
           if constexpr (SCHEME == 4) {
             // difference form: a (((1+beta) p + (1-beta)(p - pp)) + l2 (S - K p))
             o = mul2(aa[h], add2(add2(fma2(ee[h], pc2, nz), fma2(cc[h], sub2(pc2, pr(vpp, h)), nz)),
@@ -594,6 +633,7 @@ k_update_tma(const __grid_constant__ CUtensorMap map_cur, const __grid_constant_
           } else {
             o = mul2(aa[h], sub2(add2(fma2(bb[h], pc2, nz), fma2(l22, s6, nz)),
                                  fma2(cc[h], pr(vpp, h), nz)));
+          }
           }
           float lo, hi;
           up2(o, lo, hi);
