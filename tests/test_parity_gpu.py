@@ -3,9 +3,9 @@
 The kernels evaluate the reference's update rule with every product and sum
 rounded separately and the per-class coefficients computed with the
 reference's expressions, so receiver traces and fields are expected to be
-bit-identical to the oracle (compiled with -ffp-contract=off).  The
-tolerance written in the spec contract (relative L2 <= 1e-5 for FP32,
-<= 1e-12 for FP64) is checked as well and reported on failure.
+bit-identical to the oracle (compiled with -ffp-contract=off).  The parity
+tolerance of the path (relative L2 <= 1e-5 for FP32, <= 1e-12 for FP64) is
+checked as well and reported on failure.
 """
 import os
 

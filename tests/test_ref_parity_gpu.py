@@ -12,7 +12,7 @@ Three checks, all through this library's C ABI (parallelfdtd_gb300.Domain):
   floating-point contraction and once with -fmad=false.
   oracle/ref_gpu_runner.cpp launches them with launchFDTD3d's host sequence
   (kernels3d.cu:86-175).  Without contraction the reference must equal this
-  library bit for bit, which also meets the contract's tolerance (1e-5 FP32,
+  library bit for bit, which also meets the parity tolerance (1e-5 FP32,
   1e-12 FP64); with contraction, within TOL_CONTRACTED (see below).
 * the same at the full 512 x 384 x 256 room for the full 2000 steps.
 

@@ -6,7 +6,7 @@ gives an exactly zero Laplacian.  It is checked bit for bit against the
 oracle's statement of the same form, on every kernel path that runs it (FP32
 fields, the one storage it is built for), and
 its receiver error against an FP64 run is checked against the 1e-4 relative
-L2 bound of the contract, which the reference form misses in FP32.
+L2 bound on the error against FP64, which the reference form misses in FP32.
 """
 import numpy as np
 import pytest
@@ -113,7 +113,7 @@ def test_difference_form_batched_fields(gpu, O, prec):
 
 @pytest.mark.gpu
 def test_difference_form_c1_error_against_fp64(gpu, O):
-    """The 64^3 shoebox of the contract (500 steps, soft Gaussian, receiver
+    """The 64^3 shoebox (500 steps, soft Gaussian, receiver
     (16, 40, 24)): the difference form in FP32 on the GPU stays within 1e-4
     relative L2 of the FP64 run; the reference form does not."""
     room, steps, pulse = c1()
