@@ -4,9 +4,9 @@ The form is an addition with no counterpart in the reference: the same
 forward update, equal in exact arithmetic, written so that a uniform field
 gives an exactly zero Laplacian.  It is checked bit for bit against the
 oracle's statement of the same form, on every kernel path that runs it (FP32
-fields, the one storage it is built for), and
-its receiver error against an FP64 run is checked against the 1e-4 relative
-L2 bound on the error against FP64, which the reference form misses in FP32.
+fields, the one storage it is built for), and its receiver error against an
+FP64 run is checked against a 1e-4 relative L2 bound, which the reference
+form misses in FP32.
 """
 import numpy as np
 import pytest
