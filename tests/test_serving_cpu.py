@@ -29,6 +29,31 @@ def test_request_bytes_iwb(built):
     assert i.bytes() >= f.bytes() + 5 * n
 
 
+def test_request_bytes_split(built):
+    """A request that runs field by field on one single-field domain (IWB
+    with several fields, or fields without a source) needs the footprint of
+    that domain; a forward request whose 4 fields all carry a source runs
+    batched and holds all 4 fields."""
+    from parallelfdtd_gb300 import rooms
+    room = rooms.boxes_room((64, 48, 40), n_boxes=3, edge=(5, 10), n_materials=4, seed=3)
+    n = 64 * 48 * 40
+    pulse = np.zeros((4, 100))
+    src = [(10 + 3 * i, 20, 20) for i in range(4)]
+
+    def req(scheme, fields, n_src):
+        r = Request(room.dims, 100, fields=fields, precision="f32", scheme=scheme)
+        r.set_voxels(room.bid, room.mat)
+        r.set_sources(src[:n_src], [1] * n_src, pulse[:n_src], fields=list(range(n_src)))
+        r.set_receivers(src[:n_src], fields=list(range(n_src)))
+        return r
+
+    one = req("iwb", 1, 1).bytes()
+    assert abs(req("iwb", 4, 4).bytes() - one) < 64 * 1024      # one single-field domain
+    fwd1 = req("forward", 1, 1).bytes()
+    assert abs(req("forward", 4, 3).bytes() - fwd1) < 64 * 1024  # a field without a source
+    assert req("forward", 4, 4).bytes() > fwd1 + 6 * n * 4        # batched: 4 fields
+
+
 def test_request_validation(built):
     with pytest.raises(L.PfdtdError):
         Request((64, 48, 2), 100)
