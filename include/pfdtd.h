@@ -327,7 +327,8 @@ int pfdtd_set_kernel(pfdtd_domain* d, int variant);
  * 10 128x8 with 8 nodes per thread and planes z-1, z kept in registers.
  * Batched 16-bit fields: 0 256x8, 1 256x4, 2 256x8 with 6 stages (4 fields
  * per thread); for K a multiple of 8, 3 256x8, 4 256x4 (8 fields per
- * thread), 5 256x8 with planes kept in registers (default).  For the IWB
+ * thread), 5 256x8 with planes kept in registers (default), 6 256x4 with
+ * planes kept in registers.  For the IWB
  * scheme the same index picks the IWB shape: 0..5 carry the closed-neighbour
  * masks and compute the closure in the kernel (0 64x16, 1 128x8, 2 128x4,
  * 3..5 64x8 with 3, 4, 5 CTAs per SM); 6..10 run the open sums in the kernel

@@ -1097,9 +1097,13 @@ int launch_tma_16(pfdtd_domain* d, const void* cur, void* past, cudaStream_t s) 
     // 2 = 256 x 8, 6 stages, two CTAs; with 8 elements (fields of one node)
     // per thread, for K a multiple of 8: 3 = 256 x 8, 8 stages, two CTAs;
     // 4 = 256 x 4, 8 stages, four CTAs; 5 (the default) = as 3 with planes
-    // z-1, z carried in registers.  Measured on the 384 x 320 x 256 room,
-    // K = 16, FP16 (field-updates/s): 0 710 G, 3 896 G, 4 900 G, 5 928 G.
-    const int tile = d->tma_tile < 0 || d->tma_tile > 5 ? 5 : d->tma_tile;
+    // z-1, z carried in registers; 6 = as 4 with planes carried.  Measured on
+    // the 384 x 320 x 256 room, K = 16, FP16 (field-updates/s): 0 710 G,
+    // 3 896 G, 4 900 G, 5 928 G, 6 934 G (BF16: 5 908 G, 6 913 G).
+    const int tile = d->tma_tile < 0 || d->tma_tile > 6 ? 5 : d->tma_tile;
+    if (d->K % 8 == 0 && tile == 6)
+      return launch_tma_batched<S, Layout<S, uint8_t, 256, 4, 8, false, false, 4, 8, true>,
+                                Layout<S, uint16_t, 256, 4, 8, false, false, 4, 8, true>>(d, cur, past, s);
     if (d->K % 8 == 0 && tile == 5)
       return launch_tma_batched<S, Layout<S, uint8_t, 256, 8, 8, false, false, 2, 8, true>,
                                 Layout<S, uint16_t, 256, 8, 8, false, false, 2, 8, true>>(d, cur, past, s);

@@ -1000,7 +1000,7 @@ def test_batched_partly_filled_tiles(gpu, O, fields, prec):
         assert np.array_equal(g[f], r[0]), f"field {f}"
 
 
-@pytest.mark.parametrize("tile", [0, 1, 2, 3, 4, 5])
+@pytest.mark.parametrize("tile", [0, 1, 2, 3, 4, 5, 6])
 @pytest.mark.parametrize("fields,prec", [(16, "f16"), (8, "bf16"), (4, "f16")])
 @pytest.mark.parametrize("centred", [False, True])
 @pytest.mark.parametrize("dims", [(64, 48, 40), (72, 40, 32)])
